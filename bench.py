@@ -1,0 +1,335 @@
+"""Benchmark of the RSG elastodynamic leapfrog on one GB300 (or N replicas).
+
+Workload (default): composite laminate 400x400x40 cells (6.4 M cells,
+6.59 M nodes), 0.05 mm voxels, [0/90/+45/-45]s plies of the orthotropic ply
+(C11=140, C22=C33=10, C12=C13=6, C23=4, C44=3, C55=C66=5 GPa, rho=1600)
+rotated about z, a 5-cycle 500 kHz Hann tone burst (z force) on a 2 mm
+radius patch centred on the top face, 64 seeded top-face sensors recorded
+every step.  Synthetic inputs with the published workload's shapes.
+
+A step is one leapfrog step over the whole mesh: the node velocity update
+then the cell stress update (two kernel launches).  Every step moves more
+than the 129 MB L2 (about 1.9 GB in FP64), so no L2 flush is needed.
+
+value  = cells x steps / device time of the timed region (CUDA events on the
+         solver's stream), FP64 drop-in form, summed over ranks.
+e2e    = the same metric through the C ABI from host buffers: upload of the
+         initial state from pinned host memory, the steps (one pn_solver_solve
+         call per step, as the reference runners call Model::solve), download of
+         the traces and the final state, timed on the host.
+--impl reference times the CPU implementation of the path (the compiled
+reference HostSolver when it exists on this machine, else the C restatement
+of its algorithm) on the same workload with all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Gcell-steps/s & % HBM roofline"
+UNIT = "Gcell-steps/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=100)
+    p.add_argument("--warmup", type=int, default=10)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--case", default="laminate", choices=["laminate", "plate", "holes"])
+    p.add_argument("--no-fp32", action="store_true")
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    return p.parse_args()
+
+
+def make_case(name):
+    from pannde_gb300 import cases
+    if name == "laminate":
+        c = cases.laminate_case()
+        desc = ("laminate 400x400x40 cells (0.05 mm), [0/90/+45/-45]s orthotropic plies, "
+                "500 kHz 5-cycle tone burst, 64 sensors")
+    elif name == "plate":
+        c = cases.al_plate_case()
+        desc = "aluminium plate 64x64x8 cells (0.1 mm), 1 MHz tone burst, 16 sensors"
+    else:
+        c = cases.holed_plate_case()
+        desc = "aluminium plate 1024x1024x24 cells (0.1 mm), 12 holes, 1 MHz tone burst, 128 sensors"
+    return c, desc
+
+
+def peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(case, prec):
+    """DRAM bytes per launch from the committed ncu summary (profiles/*.txt)."""
+    out = {}
+    for f in sorted((ROOT / "profiles").glob("*.txt")):
+        for line in f.read_text().splitlines():
+            if line.startswith("traffic ") and "=" in line:
+                key, val = line[len("traffic "):].split("=", 1)
+                out[key.strip()] = float(val.split()[0])
+    return out.get(f"{case}.{prec}.velocity"), out.get(f"{case}.{prec}.stress")
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def time_device(case, prec, steps, warmup, torch, dist):
+    """Device throughput of the hot path with inputs resident in HBM."""
+    from pannde_gb300.solver import Solver
+    s = Solver.from_case(case, precision=prec, capacity=warmup + steps)
+    stream = torch.cuda.Stream()
+    s.set_stream(stream)
+    s.solve(warmup)
+    s.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    s.enable_kernel_timing(True)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    s.solve(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    kt = s.kernel_times()
+    info = s.info()
+    if dist:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    s.close()
+    return ms, kt, info
+
+
+def roofline(case, info, kt, prec, peak, peak_kind):
+    e = 8 if prec.startswith("f64") else 4
+    nc, nn = info["n_cells"], info["n_nodes"]
+    alg = {"velocity": nc * 6 * e + nn * (7 * e + 32),     # S read, V r/w, dt/rho, node slots
+           "stress": nc * (12 * e + 36) + nn * 3 * e}      # S r/w, mat id, corners, V read
+    avg = {k: kt[k][0] / max(kt[k][1], 1) for k in kt}
+    dom = max(avg, key=lambda k: avg[k])
+    achieved = alg[dom] / (avg[dom] * 1e-3) / 1e9
+    tv, ts = profile_traffic(case, prec)
+    traffic = {"velocity": tv, "stress": ts}[dom]
+    return {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+            "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+            "traffic": traffic, "algorithmic_bytes": alg[dom],
+            "avg_ms": {k: round(v, 4) for k, v in avg.items()},
+            "step_bytes_frac": round((alg["velocity"] + alg["stress"]) /
+                                     ((avg["velocity"] + avg["stress"]) * 1e-3) / 1e9 / peak, 4)}
+
+
+def e2e_run(case, prec, steps, torch):
+    """Through the C ABI with host buffers (pinned), copies inside the timed region."""
+    from pannde_gb300.solver import Solver
+    s = Solver.from_case(case, precision=prec, capacity=steps)
+    nn, nc = case.mesh.n_nodes, case.mesh.n_cells
+
+    def pinned(n):
+        return torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+
+    V0 = [pinned(nn) for _ in range(3)]
+    S0 = [pinned(nc) for _ in range(6)]
+    for a in V0 + S0:
+        a[:] = 0.0
+    V = [pinned(nn) for _ in range(3)]
+    S = [pinned(nc) for _ in range(6)]
+    s.solve(2)  # first-call setup (source tables) outside the timed region
+    s.synchronize()
+    s.clear_traces()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.set_state(V0, S0)
+    for _ in range(steps):
+        s.solve(1)
+    tr = s.traces()
+    s.get_state_into(V, S)
+    t1 = time.perf_counter()
+    sig_rows = min(steps, 1 << 16)
+    h2d = (3 * nn + 6 * nc) * 8 + sig_rows * len(case.sources) * 8
+    d2h = (3 * nn + 6 * nc) * 8 + tr.size * 8
+    s.close()
+    return (t1 - t0), h2d, d2h
+
+
+def cpu_reference(case, budget_s):
+    """The CPU implementation on a bounded sample of the workload (all threads)."""
+    import oracle
+    lib_kind = "reference" if oracle.reference() is not None else "port"
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    mat = case.material_fields()
+
+    def run(n):
+        t0 = time.perf_counter()
+        oracle.run(case.mesh, mat, case.dt, case.sources, n, case.sensors, impl=lib_kind)
+        return time.perf_counter() - t0
+
+    t1 = run(1)
+    t3 = run(3)
+    per_step = max((t3 - t1) / 2.0, 1e-9)
+    n = int(max(2, min(50, budget_s / per_step)))
+    tn = run(1 + n)
+    per_step = max((tn - t1) / n, 1e-9)
+    value = case.mesh.n_cells / per_step / 1e9
+    threads_used = threads if lib_kind == "port" else 1
+    return {"value": value, "unit": UNIT, "cores": threads_used,
+            "kind": "reference" if lib_kind == "reference" else "port",
+            "sample": f"{n} steps on the full {case.mesh.n_cells}-cell mesh "
+                      f"(setup cancelled by differencing a 1-step run), {case.name}"}
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_setup()
+    assert args.warmup >= 3 or args.impl == "reference", "at least 3 warm-up steps"
+    case, desc = make_case(args.case)
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        cb = cpu_reference(case, args.cpu_seconds)
+        line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT,
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": case.mesh.n_cells / (cb["value"] * 1e9) * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": {"workload": desc, "cells": case.mesh.n_cells,
+                                                "nodes": case.mesh.n_nodes},
+                "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    import torch
+    dist = None
+    if ws > 1:
+        import torch.distributed as tdist
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl")
+        dist = tdist
+    else:
+        torch.cuda.set_device(0)
+    from pannde_gb300 import _native
+    _native.load()
+
+    peak, peak_kind = peaks()
+    with Clocks(local) as clk:
+        ms, kt, info = time_device(case, "f64", args.steps, args.warmup, torch, dist)
+    clocks = clk.summary()
+    cells = info["n_cells"]
+    value = ws * cells * args.steps / (ms * 1e-3) / 1e9
+    line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": desc + " (FP64 drop-in form)", "cells": cells,
+                       "nodes": info["n_nodes"], "materials": info["n_materials"],
+                       "algorithmic_bytes_per_step": info["algorithmic_bytes_per_step"],
+                       "l2": "no flush: each step moves > 1.8 GB, far above the 129 MB L2",
+                       "parallelism": f"{ws} independent replica(s), one per GPU"},
+            "roofline": roofline(args.case, info, kt, "f64", peak, peak_kind),
+            "gpu_launches": int(kt["velocity"][1] + kt["stress"][1]),
+            "clocks": clocks}
+    if not args.no_fp32:
+        ms32, kt32, info32 = time_device(case, "f32", args.steps, args.warmup, torch, dist)
+        v32 = ws * cells * args.steps / (ms32 * 1e-3) / 1e9
+        line["fp32"] = {"value": round(v32, 4), "unit": UNIT,
+                        "ms_per_step": round(ms32 / args.steps, 4),
+                        "roofline": roofline(args.case, info32, kt32, "f32", peak, peak_kind)}
+    if rank == 0:
+        secs, h2d, d2h = e2e_run(case, "f64", args.steps, torch)
+        line["e2e"] = {"value": round(cells * args.steps / secs / 1e9 * ws, 4), "unit": UNIT,
+                       "h2d_bytes_per_step": int(h2d / args.steps),
+                       "d2h_bytes_per_step": int(d2h / args.steps),
+                       "how": "pn_solver_set_state from pinned host, one pn_solver_solve per step, "
+                              "pn_solver_get_traces + pn_solver_get_state to pinned host; wall clock"}
+        if ws == 1 and not args.no_cpu:
+            line["cpu_baseline"] = cpu_reference(case, args.cpu_seconds)
+        print(json.dumps(line))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

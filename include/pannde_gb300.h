@@ -1,0 +1,256 @@
+/*
+ * pannde_gb300.h -- C ABI of the GB300 (sm_103a) rotated-staggered-grid (RSG)
+ * elastodynamic leapfrog on hex meshes.
+ *
+ * This is the drop-in boundary for PanNDE's solver path
+ *   HostSolver::HostRSGTDUT::solve  (modules/HostSolver/include/HostRSGTDUT.hpp:162-169)
+ *   HostSolver::HostUTModel::solve  (modules/HostSolver/include/HostUTModel.hpp:186-193)
+ * The entry points take plain C structs of host pointers and sizes: no C++,
+ * no torch and no CUDA types cross this line (streams are passed as void*).
+ * Every call returns an int status (PN_OK on success); on failure
+ * pn_last_error() returns a message for the calling thread.  No exception
+ * ever crosses the ABI; the C++ adapter (pannde/DeviceSolver.hpp) rethrows
+ * the exception type the reference would have thrown, keyed on the status.
+ *
+ * All host-side floating-point inputs and outputs are IEEE double, as in the
+ * reference's HostField/HostArray.  The device storage type is picked by the
+ * precision argument of pn_solver_create.
+ */
+#ifndef PANNDE_GB300_H
+#define PANNDE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PN_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+enum pn_status {
+  PN_OK = 0,
+  PN_ERR_INVALID = 1,    /* bad argument: null pointer, negative size, unknown enum */
+  PN_ERR_SPACING = 2,    /* non-positive nodal spacing: reference throws
+                            std::logic_error("DX"/"DY"/"DZ"), RightHex.hpp:305-307 */
+  PN_ERR_RANGE = 3,      /* index out of range: reference throws std::out_of_range,
+                            HexMesh.hpp:252-257 (invalid node id in a cell) */
+  PN_ERR_RUNTIME = 4,    /* reference throws std::runtime_error, e.g. mismatched
+                            signal arrays, HostUnivariate.hpp:80 */
+  PN_ERR_CUDA = 5,       /* a CUDA runtime call failed */
+  PN_ERR_ALLOC = 6,      /* device allocation failed or exceeds the HBM budget */
+  PN_ERR_NOT_FINITE = 7, /* NaN/Inf in an input array (checked before upload) */
+  PN_ERR_DEVICE_CHECK = 8/* a device-side bounds check recorded an error */
+};
+
+/* ---- precision / arithmetic forms -------------------------------------- */
+enum pn_precision {
+  /* FP64 state and arithmetic in the reference's exact operation order
+     (no FMA contraction, divisions by the stored spacings): bit-identical
+     to HostSolver on the same inputs.  Parity mode; slowest. */
+  PN_PREC_F64_EXACT = 0,
+  /* FP64 state and arithmetic with constants folded (dt*C, 0.25/h, dt/rho)
+     and FMA: the drop-in fast path, <= 1e-10 relative L2 against HostSolver. */
+  PN_PREC_F64 = 1,
+  /* FP32 state, FP32 material tensors and FP32 arithmetic; traces are
+     returned in FP64.  Roughly halves the bytes per step. */
+  PN_PREC_F32 = 2
+};
+
+/* Field storage types; numbering equals PanNDE::Field::FieldType
+   (modules/PanNDE/include/Field.hpp, NODE=0, CELL=1, CONSTANT=2). */
+enum pn_field_type { PN_FIELD_NODE = 0, PN_FIELD_CELL = 1, PN_FIELD_CONSTANT = 2 };
+
+/* Source kinds. */
+enum pn_source_kind {
+  /* Force added in the velocity update at every node, evaluated at the centres
+     of the node's existing incident cells with weight 0.125 each:
+     HostRSGTDUT::evalXds (HostRSGTDUT.hpp:387-402), HostUTModel::evalXds
+     (HostUTModel.hpp:404-419).  component = direction 0..2 (x,y,z). */
+  PN_SOURCE_FORCE = 0,
+  /* Moment-tensor term added in the stress update at every cell, evaluated at
+     the cell's 8 corner nodes with weight 0.125 each: HostUTModel::evalMoments
+     (HostUTModel.hpp:296-311).  component = Voigt index 0..5 (xx,yy,zz,yz,xz,xy). */
+  PN_SOURCE_MOMENT = 1
+};
+
+/* ---- input descriptions ------------------------------------------------ */
+
+/* Hex mesh; replaces PanNDE::Mesh as read by the solver (Mesh.hpp:98-226,
+   HexMesh.hpp:75-352).  Cells list 8 corner node ids in the reference's
+   corner order (PlateBuilder.hpp makeCell: 0=(0,0,0) 1=(1,0,0) 2=(1,1,0)
+   3=(0,1,0) 4..7 the same at +z).  The node->cell links are built exactly as
+   HexMesh::buildLinks (HexMesh.hpp:300-313): corner k of cell c goes to slot
+   k^6 of that node, later cells overwrite earlier ones. */
+typedef struct pn_mesh {
+  int32_t n_nodes;
+  int32_t n_cells;
+  const double *x, *y, *z;     /* [n_nodes] node coordinates */
+  const int32_t *hexes;        /* [n_cells * 8] corner node ids */
+  const int32_t *node_owner;   /* [n_nodes] home partition, or NULL = all owned */
+  int32_t partition_id;        /* nodes with node_owner != partition_id are not updated
+                                  (HostRSGTDUT.hpp:339, updateVsAtNode) */
+} pn_mesh;
+
+/* One field of the domain bundle: NODE ([n_nodes]), CELL ([n_cells]) or
+   CONSTANT ([1]) values, read with HostField's semantics (HostField.hpp:110-153). */
+typedef struct pn_field {
+  int32_t type;                /* enum pn_field_type */
+  const double *data;
+} pn_field;
+
+/* Elastic material: ElasticMaterialNames (StandardNames.hpp:64-82).
+   cij holds the 21 unique Voigt entries in upper-triangle row order
+   C11 C12 C13 C14 C15 C16 C22 C23 C24 C25 C26 C33 C34 C35 C36 C44 C45 C46
+   C55 C56 C66; the solver reads C[i][j] = C[j][i] as the reference does. */
+typedef struct pn_material {
+  pn_field density;
+  pn_field cij[21];
+} pn_material;
+
+/* Indexed form of the same domain: cell c has density[cell_material[c]] and
+   stiffness cij[cell_material[c]][0..20] (same 21-entry order as pn_material).
+   Equivalent to CELL fields built from the table; this is how the reference's
+   case makers write per-cell properties from a few materials
+   (py_utils/Case_Makers/*: C_arr[:, cell] = C[:, Geom[i,j,k]-1]) without the
+   caller expanding them to n_cells x 22 doubles. */
+typedef struct pn_material_table {
+  int32_t n_materials;
+  const double *density;         /* [n_materials] */
+  const double *cij;             /* [n_materials * 21] */
+  const int32_t *cell_material;  /* [n_cells], values in [0, n_materials) */
+} pn_material_table;
+
+/* Piecewise-linear time series; replaces HostData::HostUnivariate
+   (HostUnivariate.hpp:69-152): linear interpolation between samples, the
+   last value held for t >= last sample time. Times need not be sorted;
+   duplicate times keep the first value (std::map::emplace semantics). */
+typedef struct pn_signal {
+  int32_t n;
+  const double *t;
+  const double *v;
+} pn_signal;
+
+/* A windowed source with a separable time signal; replaces
+   Stubs::HostNormalXDZ (HostNormalXDZ.hpp:117-145):
+   evalAt(p,t) = signal(t) * [|p_z - cz| <= 0.75*ds] * [|p - c| < radius]. */
+typedef struct pn_window_source {
+  int32_t kind;        /* enum pn_source_kind */
+  int32_t group;       /* transducer / moment-tensor index: accumulation order */
+  int32_t component;   /* force direction 0..2 or Voigt component 0..5 */
+  double center[3];
+  double radius;
+  double ds;
+  pn_signal signal;
+} pn_window_source;
+
+/* Read-only facts about a created solver. */
+typedef struct pn_solver_info {
+  int32_t n_nodes, n_cells;
+  int32_t precision;
+  int32_t n_materials;       /* unique stiffness rows after de-duplication */
+  int32_t uniform_spacing;   /* 1: one (hx,hy,hz) for every cell and node */
+  int32_t n_source_nodes;    /* nodes with a force source term */
+  int32_t n_source_cells;    /* cells with a moment source term */
+  int32_t n_sensors;
+  int64_t algorithmic_bytes_per_step; /* HBM bytes one step must move */
+  int64_t device_bytes;      /* device memory held by the solver */
+  double dt;
+  double time;
+} pn_solver_info;
+
+typedef struct pn_solver pn_solver;
+
+/* ---- entry points ------------------------------------------------------ */
+
+/* Library ABI version (PN_ABI_VERSION). */
+int pn_abi_version(void);
+
+/* Message for the last failed call on this thread ("" if none). */
+const char *pn_last_error(void);
+
+/* Build a solver on the current CUDA device: uploads connectivity, spacing,
+   material and density tables.
+   Replaces the constructors HostRSGTDUT(dt,domain,initial_condition,...)
+   (HostRSGTDUT.hpp:119-146) and HostUTModel(dt,domain,initial_condition,comm)
+   (HostUTModel.hpp:113-129) up to setup(): setupProperties, RightHex(mesh)
+   nodePrep/cellPrep (RightHex.hpp:80-90, 253-309).  State starts at zero. */
+int pn_solver_create(const pn_mesh *mesh, const pn_material *material, double dt,
+                     int32_t precision, pn_solver **out);
+
+/* Same as pn_solver_create with the domain given as a material table
+   (pn_material_table); the result is identical to passing the equivalent
+   CELL fields. */
+int pn_solver_create_indexed(const pn_mesh *mesh, const pn_material_table *material,
+                             double dt, int32_t precision, pn_solver **out);
+
+/* Enqueue all subsequent work on this CUDA stream (cudaStream_t as void*;
+   NULL = the legacy default stream). */
+int pn_solver_set_stream(pn_solver *s, void *cuda_stream);
+
+/* Upload the initial condition: V[3] = Vx,Vy,Vz ([n_nodes] each), S[6] =
+   Sxx,Syy,Szz,Syz,Sxz,Sxy ([n_cells] each); a NULL pointer means zero.
+   Replaces setupSolution (HostRSGTDUT.hpp:235-239). */
+int pn_solver_set_state(pn_solver *s, const double *const *V, const double *const *S);
+
+/* Add windowed sources.  Replaces the transducer constructor arguments
+   (HostRSGTDUT.hpp:139-146), HostUTModel::applyTransducer (HostUTModel.hpp:138-141)
+   and applyMomentExcitation (HostUTModel.hpp:152-170). */
+int pn_solver_add_sources(pn_solver *s, const pn_window_source *src, int32_t n);
+
+/* Record V at these nodes after every step (traces [step][sensor][3]).
+   The reference records the transducer-node velocities at write times
+   (TransducerModel.cpp:143-149); this records every step, fused into the
+   velocity update.  capacity_steps bounds the device trace buffer. */
+int pn_solver_set_sensors(pn_solver *s, const int32_t *nodes, int32_t n,
+                          int32_t capacity_steps);
+
+/* Advance nsteps leapfrog steps: velocity update, stress update, time += dt.
+   Enqueue only (no device synchronisation); *time_out (may be NULL) receives
+   the new time, accumulated on the host in FP64 exactly as the reference.
+   Replaces Model::solve (Model.hpp:77-106; HostRSGTDUT.hpp:162-169). */
+int pn_solver_solve(pn_solver *s, int32_t nsteps, double *time_out);
+
+/* Synchronise and download the state into caller-owned host arrays (same
+   layout as pn_solver_set_state; NULL pointers are skipped).  Replaces the
+   host reads the runners make through Model::getStates() (Model.hpp:77-106,
+   TransducerModel.cpp:143-149, VTKGrid.hpp:125-160). */
+int pn_solver_get_state(pn_solver *s, double *const *V, double *const *S);
+
+/* Synchronise and copy recorded traces ([n_records][n_sensors][3], FP64) into
+   out (capacity max_records records); *n_records receives the count. */
+int pn_solver_get_traces(pn_solver *s, double *out, int64_t max_records, int64_t *n_records);
+
+/* Forget recorded traces (the next step writes record 0). */
+int pn_solver_clear_traces(pn_solver *s);
+
+/* Current simulation time (host-side FP64 accumulation). */
+int pn_solver_get_time(pn_solver *s, double *time_out);
+
+/* Facts about the solver (sizes, bytes per step, device memory). */
+int pn_solver_get_info(pn_solver *s, pn_solver_info *info);
+
+/* Device pointers of the state arrays (double* or float* by precision), for
+   zero-copy interop; V[3], S[6] receive the pointers. */
+int pn_solver_device_state(pn_solver *s, void **V, void **S);
+
+/* Block until all work enqueued by this solver is done; reports errors from
+   the device-side checks. */
+int pn_solver_synchronize(pn_solver *s);
+
+/* Per-kernel device time.  While enabled, every launch of the velocity and
+   the stress kernel is bracketed by CUDA events on the solver's stream.
+   pn_solver_kernel_times synchronises, returns the summed milliseconds and
+   the launch counts of [velocity, stress] since timing was enabled, and
+   restarts the count.  Profiling aid; no counterpart in the reference. */
+int pn_solver_enable_kernel_timing(pn_solver *s, int32_t enable);
+int pn_solver_kernel_times(pn_solver *s, double *ms /* [2] */, int64_t *launches /* [2] */);
+
+/* Free all device memory of the solver. */
+int pn_solver_destroy(pn_solver *s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PANNDE_GB300_H */

@@ -1,0 +1,389 @@
+// pn_setup.cpp -- host-side table construction (see pn_setup.hpp).
+// Compiled with -ffp-contract=off: window predicates, cell centres and
+// spacings must round as the reference's C++ does.
+#include "pn_setup.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <unordered_map>
+
+namespace pn {
+
+namespace {
+[[noreturn]] void fail(int code, const std::string &msg) { throw SetupError{code, msg}; }
+
+bool near_equal(double a, double b) { return std::fabs(a - b) <= 1e-12 * std::fabs(b); }
+}  // namespace
+
+bool all_finite(const double *p, int64_t n) {
+  for (int64_t i = 0; i < n; i++)
+    if (!std::isfinite(p[i])) return false;
+  return true;
+}
+
+void build_mesh_tables(const pn_mesh &m, MeshTables &t) {
+  if (m.n_nodes < 0 || m.n_cells < 0) fail(PN_ERR_INVALID, "negative node or cell count");
+  if (m.n_nodes > 0 && (!m.x || !m.y || !m.z)) fail(PN_ERR_INVALID, "null node coordinates");
+  if (m.n_cells > 0 && !m.hexes) fail(PN_ERR_INVALID, "null cell connectivity");
+  const int32_t nn = m.n_nodes, nc = m.n_cells;
+  t.n_nodes = nn;
+  t.n_cells = nc;
+  if (!all_finite(m.x, nn) || !all_finite(m.y, nn) || !all_finite(m.z, nn))
+    fail(PN_ERR_NOT_FINITE, "non-finite node coordinate");
+  t.x.assign(m.x, m.x + nn);
+  t.y.assign(m.y, m.y + nn);
+  t.z.assign(m.z, m.z + nn);
+  t.hex.assign(m.hexes, m.hexes + (size_t)nc * 8);
+  // HexMesh::setCell throws std::out_of_range for an invalid node id
+  for (size_t k = 0; k < t.hex.size(); k++) {
+    if (t.hex[k] < 0 || t.hex[k] >= nn)
+      fail(PN_ERR_RANGE, "invalid node id: Node count: " + std::to_string(nn) +
+                             ", provided index: " + std::to_string(t.hex[k]));
+  }
+  t.owned.assign(nn, 1);
+  if (m.node_owner)
+    for (int32_t n = 0; n < nn; n++) t.owned[n] = (m.node_owner[n] == m.partition_id);
+
+  // buildLinks: corner k of cell c -> slot k^6 of that node; later cells win
+  t.ncc.assign((size_t)nn * 8, -1);
+  for (int32_t c = 0; c < nc; c++)
+    for (int k = 0; k < 8; k++) t.ncc[(size_t)t.hex[(size_t)c * 8 + k] * 8 + (k ^ 6)] = c;
+
+  // nodePrep (RightHex.hpp:272-309)
+  t.dxn.resize(nn);
+  t.dyn.resize(nn);
+  t.dzn.resize(nn);
+  for (int32_t n = 0; n < nn; n++) {
+    const double node[3] = {t.x[n], t.y[n], t.z[n]};
+    double lo[3] = {node[0], node[1], node[2]};
+    double hi[3] = {node[0], node[1], node[2]};
+    for (int kb = 0; kb < 8; kb++) {
+      const int32_t c = t.ncc[(size_t)n * 8 + kb];
+      if (c == -1) continue;
+      for (int kbb = 0; kbb < 8; kbb++) {
+        const int32_t q = t.hex[(size_t)c * 8 + kbb];
+        const double pt[3] = {t.x[q], t.y[q], t.z[q]};
+        for (int kd = 0; kd < 3; kd++) {
+          lo[kd] = std::min(lo[kd], pt[kd]);
+          hi[kd] = std::max(hi[kd], pt[kd]);
+        }
+      }
+    }
+    for (int kd = 0; kd < 3; kd++) {
+      if (lo[kd] == node[kd]) lo[kd] = 2. * node[kd] - hi[kd];
+      if (hi[kd] == node[kd]) hi[kd] = 2. * node[kd] - lo[kd];
+    }
+    t.dxn[n] = 0.5 * (hi[0] - lo[0]);
+    if (0 >= t.dxn[n]) fail(PN_ERR_SPACING, "DX");
+    t.dyn[n] = 0.5 * (hi[1] - lo[1]);
+    if (0 >= t.dyn[n]) fail(PN_ERR_SPACING, "DY");
+    t.dzn[n] = 0.5 * (hi[2] - lo[2]);
+    if (0 >= t.dzn[n]) fail(PN_ERR_SPACING, "DZ");
+  }
+  // cellPrep (RightHex.hpp:253-264)
+  t.dxc.resize(nc);
+  t.dyc.resize(nc);
+  t.dzc.resize(nc);
+  for (int32_t c = 0; c < nc; c++) {
+    const int32_t a = t.hex[(size_t)c * 8], b = t.hex[(size_t)c * 8 + 6];
+    t.dxc[c] = t.x[b] - t.x[a];
+    t.dyc[c] = t.y[b] - t.y[a];
+    t.dzc[c] = t.z[b] - t.z[a];
+  }
+  // one (hx,hy,hz) within 1e-12 relative for every cell and node?
+  t.uniform = nc > 0;
+  if (t.uniform) {
+    t.hx = t.dxc[0];
+    t.hy = t.dyc[0];
+    t.hz = t.dzc[0];
+    for (int32_t c = 0; c < nc && t.uniform; c++)
+      t.uniform = near_equal(t.dxc[c], t.hx) && near_equal(t.dyc[c], t.hy) && near_equal(t.dzc[c], t.hz);
+    for (int32_t n = 0; n < nn && t.uniform; n++)
+      t.uniform = near_equal(t.dxn[n], t.hx) && near_equal(t.dyn[n], t.hy) && near_equal(t.dzn[n], t.hz);
+  }
+}
+
+namespace {
+
+void check_field(const pn_field &f, const MeshTables &t, const char *what) {
+  if (f.type < PN_FIELD_NODE || f.type > PN_FIELD_CONSTANT)
+    fail(PN_ERR_INVALID, std::string("unknown field type for ") + what);
+  if (!f.data) fail(PN_ERR_INVALID, std::string("null data for ") + what);
+  const int64_t n = f.type == PN_FIELD_NODE ? t.n_nodes : f.type == PN_FIELD_CELL ? t.n_cells : 1;
+  if (!all_finite(f.data, n)) fail(PN_ERR_NOT_FINITE, std::string("non-finite value in ") + what);
+}
+
+// HostField::atCell (HostField.hpp:121-133)
+double at_cell(const pn_field &f, const MeshTables &t, int32_t c) {
+  if (f.type == PN_FIELD_NODE) {
+    double v = 0.0;
+    for (int k = 0; k < 8; k++) v += f.data[t.hex[(size_t)c * 8 + k]];
+    return v / 8.0;
+  }
+  return f.type == PN_FIELD_CONSTANT ? f.data[0] : f.data[c];
+}
+
+// HostField::atNode (HostField.hpp:142-153): a CELL or CONSTANT field sums the
+// existing incident cells and divides by 8 (the lumped nodal density)
+double at_node(const pn_field &f, const MeshTables &t, int32_t n) {
+  if (f.type == PN_FIELD_NODE) return f.data[n];
+  double v = 0.0;
+  for (int k = 0; k < 8; k++) {
+    const int32_t c = t.ncc[(size_t)n * 8 + k];
+    v += (c == -1) ? 0. : (f.type == PN_FIELD_CONSTANT ? f.data[0] : f.data[c]);
+  }
+  return v / 8.0;
+}
+
+struct RowHash {
+  size_t operator()(const std::vector<uint64_t> &r) const {
+    uint64_t h = 1469598103934665603ull;
+    for (uint64_t w : r) { h ^= w; h *= 1099511628211ull; }
+    return (size_t)h;
+  }
+};
+
+void expand36(const double *c21, double *c36) {
+  for (int i = 0; i < 6; i++)
+    for (int j = 0; j < 6; j++) c36[i * 6 + j] = c21[cij_index(i, j)];
+}
+
+}  // namespace
+
+void build_material_from_fields(const pn_material &mat, const MeshTables &t, double dt,
+                                MaterialTables &out) {
+  check_field(mat.density, t, "density");
+  for (int k = 0; k < 21; k++) check_field(mat.cij[k], t, "stiffness");
+  out.coef.resize(t.n_nodes);
+  for (int32_t n = 0; n < t.n_nodes; n++)
+    out.coef[n] = t.owned[n] ? dt / at_node(mat.density, t, n) : 0.;
+  // de-duplicate the per-cell stiffness rows (bit patterns) into a table
+  std::unordered_map<std::vector<uint64_t>, int32_t, RowHash> ids;
+  out.cell_mat.resize(t.n_cells);
+  out.c36.clear();
+  std::vector<uint64_t> key(21);
+  double row[21];
+  for (int32_t c = 0; c < t.n_cells; c++) {
+    for (int k = 0; k < 21; k++) {
+      row[k] = at_cell(mat.cij[k], t, c);
+      std::memcpy(&key[k], &row[k], 8);
+    }
+    auto it = ids.find(key);
+    if (it == ids.end()) {
+      const int32_t id = (int32_t)ids.size();
+      ids.emplace(key, id);
+      out.c36.resize(out.c36.size() + 36);
+      expand36(row, &out.c36[(size_t)id * 36]);
+      out.cell_mat[c] = id;
+    } else {
+      out.cell_mat[c] = it->second;
+    }
+  }
+  out.n_mat = (int32_t)ids.size();
+}
+
+void build_material_from_table(const pn_material_table &mat, const MeshTables &t, double dt,
+                               MaterialTables &out) {
+  if (mat.n_materials <= 0 || !mat.density || !mat.cij || (t.n_cells > 0 && !mat.cell_material))
+    fail(PN_ERR_INVALID, "material table");
+  if (!all_finite(mat.density, mat.n_materials) || !all_finite(mat.cij, (int64_t)mat.n_materials * 21))
+    fail(PN_ERR_NOT_FINITE, "non-finite value in material table");
+  for (int32_t c = 0; c < t.n_cells; c++)
+    if (mat.cell_material[c] < 0 || mat.cell_material[c] >= mat.n_materials)
+      fail(PN_ERR_RANGE, "cell material id out of range");
+  out.n_mat = mat.n_materials;
+  out.c36.resize((size_t)out.n_mat * 36);
+  for (int32_t i = 0; i < out.n_mat; i++) expand36(mat.cij + (size_t)i * 21, &out.c36[(size_t)i * 36]);
+  out.cell_mat.assign(mat.cell_material, mat.cell_material + t.n_cells);
+  out.coef.resize(t.n_nodes);
+  for (int32_t n = 0; n < t.n_nodes; n++) {
+    double v = 0.0;
+    for (int k = 0; k < 8; k++) {
+      const int32_t c = t.ncc[(size_t)n * 8 + k];
+      v += (c == -1) ? 0. : mat.density[mat.cell_material[c]];
+    }
+    out.coef[n] = t.owned[n] ? dt / (v / 8.0) : 0.;
+  }
+}
+
+void Series::build(const pn_signal &s) {
+  if (s.n <= 0 || !s.t || !s.v) fail(PN_ERR_RUNTIME, "empty or null signal arrays");
+  if (!all_finite(s.t, s.n) || !all_finite(s.v, s.n)) fail(PN_ERR_NOT_FINITE, "non-finite signal sample");
+  std::map<double, double> m;  // std::map::emplace keeps the first value per time
+  for (int32_t k = 0; k < s.n; k++) m.emplace(s.t[k], s.v[k]);
+  t.clear();
+  v.clear();
+  for (auto &kv : m) { t.push_back(kv.first); v.push_back(kv.second); }
+}
+
+double Series::eval(double time) const {
+  if (time < t.back()) {
+    // first sample with time < t[k]; before the first sample the reference
+    // steps before begin() (undefined), here the first value is held
+    const size_t k = std::upper_bound(t.begin(), t.end(), time) - t.begin();
+    if (k == 0) return v[0];
+    const double Dt = t[k] - t[k - 1];
+    const double Dv = v[k] - v[k - 1];
+    return (Dv / Dt) * (time - t[k - 1]) + v[k - 1];
+  }
+  return v.back();
+}
+
+namespace {
+
+bool window_at(const pn_window_source &w, const double p[3]) {
+  double res = 0.0;
+  for (int k = 0; k < 3; k++) {
+    const double d = p[k] - w.center[k];
+    res += d * d;
+  }
+  const double dist = std::sqrt(res);
+  const double distz = std::fabs(p[2] - w.center[2]);
+  return (distz <= 0.75 * w.ds) && (dist < w.radius) && (dist >= 0.);
+}
+
+// xducers[g][3] / moment_excitation[g][6]: slot -> source index or -1
+std::vector<int32_t> group_slots(const std::vector<pn_window_source> &src, int kind, int ncomp,
+                                 int32_t &ngroups) {
+  int32_t maxg = -1;
+  for (auto &s : src) {
+    if (s.kind != kind) continue;
+    if (s.group < 0) fail(PN_ERR_INVALID, "negative source group");
+    if (s.component < 0 || s.component >= ncomp) fail(PN_ERR_INVALID, "source component out of range");
+    maxg = std::max(maxg, s.group);
+  }
+  ngroups = maxg + 1;
+  std::vector<int32_t> slot((size_t)std::max(ngroups, 0) * ncomp, -1);
+  for (size_t i = 0; i < src.size(); i++) {
+    if (src[i].kind != kind) continue;
+    int32_t &s = slot[(size_t)src[i].group * ncomp + src[i].component];
+    if (s != -1) fail(PN_ERR_INVALID, "two sources in one group slot");
+    s = (int32_t)i;
+  }
+  return slot;
+}
+
+void push_entry(std::vector<SourceEntry> &out, bool exact, int32_t elem, int32_t comp, int32_t sig) {
+  if (!exact) {
+    // merge with an earlier entry of the same element, component and source
+    for (size_t i = out.size(); i-- > 0;) {
+      if (out[i].elem != elem) break;
+      if (out[i].comp == comp && out[i].sig == sig) { out[i].w += 0.125; return; }
+    }
+  }
+  out.push_back(SourceEntry{elem, comp, sig, 0.125});
+}
+
+}  // namespace
+
+void build_source_entries(const MeshTables &t, const std::vector<pn_window_source> &src, bool exact,
+                          std::vector<SourceEntry> &force, std::vector<SourceEntry> &moment) {
+  force.clear();
+  moment.clear();
+  for (auto &s : src) {
+    if (s.kind != PN_SOURCE_FORCE && s.kind != PN_SOURCE_MOMENT) fail(PN_ERR_INVALID, "unknown source kind");
+    const double g[5] = {s.center[0], s.center[1], s.center[2], s.radius, s.ds};
+    if (!all_finite(g, 5)) fail(PN_ERR_NOT_FINITE, "non-finite source geometry");
+  }
+  int32_t ngf = 0, ngm = 0;
+  const std::vector<int32_t> fslot = group_slots(src, PN_SOURCE_FORCE, 3, ngf);
+  const std::vector<int32_t> mslot = group_slots(src, PN_SOURCE_MOMENT, 6, ngm);
+
+  if (ngf > 0) {
+    // cell centres, HostRSGTDUT::cellcenter order (corner order, += 0.125*pt)
+    std::vector<double> cc((size_t)t.n_cells * 3);
+    for (int32_t c = 0; c < t.n_cells; c++) {
+      double p[3] = {0., 0., 0.};
+      for (int kb = 0; kb < 8; kb++) {
+        const int32_t q = t.hex[(size_t)c * 8 + kb];
+        p[0] += 0.125 * t.x[q];
+        p[1] += 0.125 * t.y[q];
+        p[2] += 0.125 * t.z[q];
+      }
+      cc[(size_t)c * 3] = p[0];
+      cc[(size_t)c * 3 + 1] = p[1];
+      cc[(size_t)c * 3 + 2] = p[2];
+    }
+    // in-window flag per (cell, force source) -- evaluated once per cell
+    std::vector<int32_t> fsrc;
+    for (size_t i = 0; i < src.size(); i++)
+      if (src[i].kind == PN_SOURCE_FORCE) fsrc.push_back((int32_t)i);
+    std::vector<uint8_t> hit((size_t)t.n_cells * src.size(), 0);
+    std::vector<uint8_t> any_cell(t.n_cells, 0);
+    for (int32_t c = 0; c < t.n_cells; c++)
+      for (int32_t i : fsrc)
+        if (window_at(src[i], &cc[(size_t)c * 3])) {
+          hit[(size_t)c * src.size() + i] = 1;
+          any_cell[c] = 1;
+        }
+    // evalXds loop order per node: dir, then slot kb, then transducer g
+    for (int32_t n = 0; n < t.n_nodes; n++) {
+      if (!t.owned[n]) continue;
+      bool any = false;
+      for (int kb = 0; kb < 8 && !any; kb++) {
+        const int32_t c = t.ncc[(size_t)n * 8 + kb];
+        any = (c != -1) && any_cell[c];
+      }
+      if (!any) continue;
+      for (int dir = 0; dir < 3; dir++)
+        for (int kb = 0; kb < 8; kb++) {
+          const int32_t c = t.ncc[(size_t)n * 8 + kb];
+          if (c == -1 || !any_cell[c]) continue;
+          for (int32_t gi = 0; gi < ngf; gi++) {
+            const int32_t si = fslot[(size_t)gi * 3 + dir];
+            if (si >= 0 && hit[(size_t)c * src.size() + si]) push_entry(force, exact, n, dir, si);
+          }
+        }
+    }
+  }
+  if (ngm > 0) {
+    std::vector<int32_t> msrc;
+    for (size_t i = 0; i < src.size(); i++)
+      if (src[i].kind == PN_SOURCE_MOMENT) msrc.push_back((int32_t)i);
+    std::vector<uint8_t> hit((size_t)t.n_nodes * src.size(), 0);
+    std::vector<uint8_t> any_node(t.n_nodes, 0);
+    for (int32_t n = 0; n < t.n_nodes; n++) {
+      const double r[3] = {t.x[n], t.y[n], t.z[n]};
+      for (int32_t i : msrc)
+        if (window_at(src[i], r)) {
+          hit[(size_t)n * src.size() + i] = 1;
+          any_node[n] = 1;
+        }
+    }
+    // evalMoments loop order per cell: component, then corner kb, then tensor g
+    for (int32_t c = 0; c < t.n_cells; c++) {
+      bool any = false;
+      for (int kb = 0; kb < 8 && !any; kb++) any = any_node[t.hex[(size_t)c * 8 + kb]];
+      if (!any) continue;
+      for (int comp = 0; comp < 6; comp++)
+        for (int kb = 0; kb < 8; kb++) {
+          const int32_t q = t.hex[(size_t)c * 8 + kb];
+          if (!any_node[q]) continue;
+          for (int32_t gi = 0; gi < ngm; gi++) {
+            const int32_t si = mslot[(size_t)gi * 6 + comp];
+            if (si >= 0 && hit[(size_t)q * src.size() + si]) push_entry(moment, exact, c, comp, si);
+          }
+        }
+    }
+  }
+}
+
+void tile_ranges(const std::vector<int32_t> &elems, int32_t n_elems, int tile,
+                 std::vector<int32_t> &ranges) {
+  const int64_t n_tiles = ((int64_t)n_elems + tile - 1) / tile;
+  ranges.assign((size_t)n_tiles * 2, 0);
+  size_t i = 0;
+  for (int64_t b = 0; b < n_tiles; b++) {
+    const int64_t lo = b * tile, hi = lo + tile;
+    while (i < elems.size() && elems[i] < lo) i++;
+    ranges[(size_t)b * 2] = (int32_t)i;
+    size_t j = i;
+    while (j < elems.size() && elems[j] < hi) j++;
+    ranges[(size_t)b * 2 + 1] = (int32_t)j;
+    i = j;
+  }
+}
+
+}  // namespace pn

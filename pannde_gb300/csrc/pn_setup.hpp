@@ -1,0 +1,97 @@
+// pn_setup.hpp -- host-side preparation of the device tables from a
+// reference-style mesh / domain description.  Pure C++ (no CUDA calls), so
+// every validation and error path here runs without a GPU.
+//
+// Each step restates the reference semantics it replaces:
+//   links      HexMesh::buildLinks            HexMesh.hpp:300-313
+//   spacings   RightHex::nodePrep / cellPrep  RightHex.hpp:253-309
+//   density    HostField::atNode              HostField.hpp:142-153
+//   stiffness  HostField::atCell              HostField.hpp:121-133
+//   windows    HostNormalXDZ::evalAt          HostNormalXDZ.hpp:117-123,174-177
+//   centres    HostRSGTDUT::cellcenter        HostRSGTDUT.hpp:419-428
+//   signals    HostUnivariate::evalAt         HostUnivariate.hpp:109-142
+// This file must be compiled with -ffp-contract=off so that the window
+// predicates and spacings round exactly as the reference's C++ does.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/pannde_gb300.h"
+
+namespace pn {
+
+struct SetupError {
+  int code;
+  std::string msg;
+};
+
+// Voigt (i,j) -> index into the 21 unique entries.
+inline int cij_index(int i, int j) {
+  if (i > j) { int t = i; i = j; j = t; }
+  return i * 6 - i * (i - 1) / 2 + (j - i);
+}
+
+struct MeshTables {
+  int32_t n_nodes = 0, n_cells = 0;
+  std::vector<double> x, y, z;
+  std::vector<int32_t> hex;       // [n_cells*8]
+  std::vector<int32_t> ncc;       // [n_nodes*8], -1 = none
+  std::vector<uint8_t> owned;     // [n_nodes]
+  std::vector<double> dxc, dyc, dzc, dxn, dyn, dzn;
+  bool uniform = false;
+  double hx = 0, hy = 0, hz = 0;
+};
+
+// Validates and builds links + spacings.  Throws SetupError.
+void build_mesh_tables(const pn_mesh &m, MeshTables &t);
+
+struct MaterialTables {
+  int32_t n_mat = 0;
+  std::vector<double> c36;        // [n_mat][36] raw stiffness (C[i][j])
+  std::vector<int32_t> cell_mat;  // [n_cells]
+  std::vector<double> coef;       // [n_nodes] dt / rho_node, 0 = not owned
+};
+
+// From reference-style fields (density + 21 Cij, NODE/CELL/CONSTANT).
+void build_material_from_fields(const pn_material &mat, const MeshTables &t, double dt,
+                                MaterialTables &out);
+// From an indexed table (density[n_mat], cij[n_mat][21], cell_material[n_cells]),
+// equivalent to CELL fields density[c] = density[mat[c]] etc.
+void build_material_from_table(const pn_material_table &mat, const MeshTables &t, double dt,
+                               MaterialTables &out);
+
+// Piecewise-linear signal with HostUnivariate semantics.
+struct Series {
+  std::vector<double> t, v;
+  void build(const pn_signal &s);  // throws SetupError
+  double eval(double time) const;
+  double last_time() const { return t.back(); }
+};
+
+// One sparse source entry: element (node or cell), component, source index,
+// weight.  Entries are sorted by element; within an element they keep the
+// reference's accumulation order.
+struct SourceEntry {
+  int32_t elem;
+  int32_t comp;
+  int32_t sig;
+  double w;
+};
+
+// Builds force entries (per node, per direction) and moment entries (per
+// cell, per Voigt component).  exact=true keeps one 0.125-weight entry per
+// in-window (element, source) pair in reference order; exact=false merges
+// equal (element, component, source) entries into one weight.
+void build_source_entries(const MeshTables &t, const std::vector<pn_window_source> &src,
+                          bool exact, std::vector<SourceEntry> &force,
+                          std::vector<SourceEntry> &moment);
+
+// Per-tile [begin,end) ranges of a list sorted by element.
+void tile_ranges(const std::vector<int32_t> &elems, int32_t n_elems, int tile,
+                 std::vector<int32_t> &ranges /* [n_tiles*2] */);
+
+// NaN / Inf scan.
+bool all_finite(const double *p, int64_t n);
+
+}  // namespace pn

@@ -1,0 +1,151 @@
+"""Thin object wrapper over the C ABI solver handle (pn_solver_*).
+
+Every call goes to the CUDA library; nothing here computes the physics.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import c_double, c_int64, c_void_p
+
+import numpy as np
+
+from . import _native as N
+from .cases import Case, HexMesh, sources_struct
+
+PRECISIONS = {"f64_exact": N.PN_PREC_F64_EXACT, "f64": N.PN_PREC_F64, "f32": N.PN_PREC_F32}
+
+
+def _precision(p) -> int:
+    return PRECISIONS[p] if isinstance(p, str) else int(p)
+
+
+class Solver:
+    """One RSG leapfrog instance resident on the current CUDA device.
+
+    ``material`` is either a Case (indexed material table) or a
+    (PnMaterial, keepalive) pair of reference-style fields.
+    """
+
+    def __init__(self, mesh: HexMesh, material, dt: float, precision="f64"):
+        self._lib = N.load()
+        self.mesh = mesh
+        self.precision = _precision(precision)
+        m, keep = mesh.as_struct()
+        h = c_void_p()
+        if isinstance(material, Case):
+            tab, keep_t = material.material_table()
+            rc = self._lib.pn_solver_create_indexed(ctypes.byref(m), ctypes.byref(tab), float(dt),
+                                                    self.precision, ctypes.byref(h))
+        else:
+            mat, keep_t = material
+            rc = self._lib.pn_solver_create(ctypes.byref(m), ctypes.byref(mat), float(dt),
+                                            self.precision, ctypes.byref(h))
+        N.check(rc)
+        self._h = h
+        self.n_sensors = 0
+        del keep, keep_t
+
+    @classmethod
+    def from_case(cls, case: Case, precision="f64", sensors=True, capacity=None):
+        s = cls(case.mesh, case, case.dt, precision)
+        if case.sources:
+            s.add_sources(case.sources)
+        if sensors and case.sensors.size:
+            s.set_sensors(case.sensors, capacity if capacity is not None else case.nsteps)
+        return s
+
+    # -- lifecycle --
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.pn_solver_destroy(self._h)
+            self._h = c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- calls --
+    def set_stream(self, stream):
+        """stream: a torch.cuda.Stream, a raw cudaStream_t int, or None."""
+        handle = getattr(stream, "cuda_stream", stream)
+        N.check(self._lib.pn_solver_set_stream(self._h, c_void_p(handle or 0)))
+
+    def set_state(self, V=None, S=None):
+        v = [N.f64(a) if a is not None else None for a in (V or [None] * 3)]
+        s = [N.f64(a) if a is not None else None for a in (S or [None] * 6)]
+        N.check(self._lib.pn_solver_set_state(self._h, N.ptr_array(v), N.ptr_array(s)))
+
+    def add_sources(self, sources):
+        arr, keep = sources_struct(sources)
+        N.check(self._lib.pn_solver_add_sources(self._h, arr, len(sources)))
+        del keep
+
+    def set_sensors(self, nodes, capacity_steps):
+        nd = N.i32(nodes)
+        N.check(self._lib.pn_solver_set_sensors(self._h, N.iptr(nd), int(nd.shape[0]),
+                                                int(capacity_steps)))
+        self.n_sensors = int(nd.shape[0])
+
+    def solve(self, nsteps=1) -> float:
+        t = c_double(0.0)
+        N.check(self._lib.pn_solver_solve(self._h, int(nsteps), ctypes.byref(t)))
+        return t.value
+
+    def get_state(self):
+        V = [np.empty(self.mesh.n_nodes) for _ in range(3)]
+        S = [np.empty(self.mesh.n_cells) for _ in range(6)]
+        N.check(self._lib.pn_solver_get_state(self._h, N.ptr_array(V), N.ptr_array(S)))
+        return V, S
+
+    def get_state_into(self, V, S):
+        """Download into caller-owned float64 arrays (None entries skipped)."""
+        N.check(self._lib.pn_solver_get_state(self._h, N.ptr_array(V), N.ptr_array(S)))
+
+    def traces(self, max_records=None) -> np.ndarray:
+        n = c_int64(0)
+        N.check(self._lib.pn_solver_get_traces(self._h, N.P_double(), 0, ctypes.byref(n)))
+        rec = n.value if max_records is None else min(n.value, max_records)
+        out = np.zeros((max(rec, 1), max(self.n_sensors, 1), 3))
+        N.check(self._lib.pn_solver_get_traces(self._h, N.dptr(out), rec, ctypes.byref(n)))
+        return out[:rec, :self.n_sensors]
+
+    def clear_traces(self):
+        N.check(self._lib.pn_solver_clear_traces(self._h))
+
+    @property
+    def time(self) -> float:
+        t = c_double(0.0)
+        N.check(self._lib.pn_solver_get_time(self._h, ctypes.byref(t)))
+        return t.value
+
+    def info(self) -> dict:
+        inf = N.PnSolverInfo()
+        N.check(self._lib.pn_solver_get_info(self._h, ctypes.byref(inf)))
+        return {k: getattr(inf, k) for k, _ in N.PnSolverInfo._fields_}
+
+    def device_state(self):
+        V = (c_void_p * 3)()
+        S = (c_void_p * 6)()
+        N.check(self._lib.pn_solver_device_state(self._h, V, S))
+        return [v for v in V], [s for s in S]
+
+    def enable_kernel_timing(self, on=True):
+        N.check(self._lib.pn_solver_enable_kernel_timing(self._h, 1 if on else 0))
+
+    def kernel_times(self):
+        """{"velocity": (ms_total, launches), "stress": (ms_total, launches)}"""
+        ms = (c_double * 2)()
+        n = (c_int64 * 2)()
+        N.check(self._lib.pn_solver_kernel_times(self._h, ms, n))
+        return {"velocity": (ms[0], n[0]), "stress": (ms[1], n[1])}
+
+    def synchronize(self):
+        N.check(self._lib.pn_solver_synchronize(self._h))
