@@ -38,6 +38,9 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "Gcell-steps/s & % HBM roofline"
+DTYPES = {"f64": "f64", "f64_exact": "f64", "f32": "f32", "df64": "f32x2 (double-float)"}
+FORMS = {"f64": "FP64 drop-in form", "f64_exact": "FP64 reference-order form",
+         "f32": "FP32 form", "df64": "double-float FP64-class form"}
 UNIT = "Gcell-steps/s"
 
 
@@ -48,17 +51,24 @@ def parse():
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--case", default="laminate", choices=["laminate", "plate", "holes"])
+    p.add_argument("--nx", type=int, default=None, help="laminate size override (profiling)")
+    p.add_argument("--ny", type=int, default=None)
+    p.add_argument("--nz", type=int, default=None)
+    p.add_argument("--precisions", default="f64,f32",
+                   help="forms to time; the first is the headline value")
+    p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fp32", action="store_true")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     return p.parse_args()
 
 
-def make_case(name):
+def make_case(name, nx=None, ny=None, nz=None):
     from pannde_gb300 import cases
     if name == "laminate":
-        c = cases.laminate_case()
-        desc = ("laminate 400x400x40 cells (0.05 mm), [0/90/+45/-45]s orthotropic plies, "
+        nx, ny, nz = nx or 400, ny or 400, nz or 40
+        c = cases.laminate_case(nx=nx, ny=ny, nz=nz)
+        desc = (f"laminate {nx}x{ny}x{nz} cells (0.05 mm), [0/90/+45/-45]s orthotropic plies, "
                 "500 kHz 5-cycle tone burst, 64 sensors")
     elif name == "plate":
         c = cases.al_plate_case()
@@ -180,7 +190,7 @@ def time_device(case, prec, steps, warmup, torch, dist):
 
 
 def roofline(case, info, kt, prec, peak, peak_kind):
-    e = 8 if prec.startswith("f64") else 4
+    e = 4 if prec == "f32" else 8
     nc, nn = info["n_cells"], info["n_nodes"]
     alg = {"velocity": nc * 6 * e + nn * (7 * e + 32),     # S read, V r/w, dt/rho, node slots
            "stress": nc * (12 * e + 36) + nn * 3 * e}      # S r/w, mat id, corners, V read
@@ -261,7 +271,10 @@ def main():
     args = parse()
     ws, rank, local = dist_setup()
     assert args.warmup >= 3 or args.impl == "reference", "at least 3 warm-up steps"
-    case, desc = make_case(args.case)
+    case, desc = make_case(args.case, args.nx, args.ny, args.nz)
+    precs = [p for p in args.precisions.split(",") if p]
+    if args.no_fp32:
+        precs = [p for p in precs if p != "f32"]
 
     if args.impl == "reference":
         if rank != 0:
@@ -292,31 +305,39 @@ def main():
     _native.load()
 
     peak, peak_kind = peaks()
+    head = precs[0]
     with Clocks(local) as clk:
-        ms, kt, info = time_device(case, "f64", args.steps, args.warmup, torch, dist)
+        ms, kt, info = time_device(case, head, args.steps, args.warmup, torch, dist)
     clocks = clk.summary()
     cells = info["n_cells"]
     value = ws * cells * args.steps / (ms * 1e-3) / 1e9
     line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic",
-            "config": {"workload": desc + " (FP64 drop-in form)", "cells": cells,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": DTYPES[head], "data": "synthetic",
+            "config": {"workload": desc + f" ({FORMS[head]})", "cells": cells,
                        "nodes": info["n_nodes"], "materials": info["n_materials"],
                        "algorithmic_bytes_per_step": info["algorithmic_bytes_per_step"],
-                       "l2": "no flush: each step moves > 1.8 GB, far above the 129 MB L2",
+                       "l2": "no flush: each step moves far more than the 129 MB L2",
                        "parallelism": f"{ws} independent replica(s), one per GPU"},
-            "roofline": roofline(args.case, info, kt, "f64", peak, peak_kind),
+            "roofline": roofline(args.case, info, kt, head, peak, peak_kind),
             "gpu_launches": int(kt["velocity"][1] + kt["stress"][1]),
             "clocks": clocks}
-    if not args.no_fp32:
-        ms32, kt32, info32 = time_device(case, "f32", args.steps, args.warmup, torch, dist)
-        v32 = ws * cells * args.steps / (ms32 * 1e-3) / 1e9
-        line["fp32"] = {"value": round(v32, 4), "unit": UNIT,
-                        "ms_per_step": round(ms32 / args.steps, 4),
-                        "roofline": roofline(args.case, info32, kt32, "f32", peak, peak_kind)}
+    forms = {}
+    for prec in precs[1:]:
+        msp, ktp, infop = time_device(case, prec, args.steps, args.warmup, torch, dist)
+        vp = ws * cells * args.steps / (msp * 1e-3) / 1e9
+        forms[prec] = {"value": round(vp, 4), "unit": UNIT, "dtype": DTYPES[prec],
+                       "ms_per_step": round(msp / args.steps, 4),
+                       "roofline": roofline(args.case, infop, ktp, prec, peak, peak_kind)}
+    if forms:
+        line["other_forms"] = forms
+    if args.no_e2e:
+        if rank == 0:
+            print(json.dumps(line))
+        return 0
     if rank == 0:
-        secs, h2d, d2h = e2e_run(case, "f64", args.steps, torch)
+        secs, h2d, d2h = e2e_run(case, head, args.steps, torch)
         line["e2e"] = {"value": round(cells * args.steps / secs / 1e9 * ws, 4), "unit": UNIT,
                        "h2d_bytes_per_step": int(h2d / args.steps),
                        "d2h_bytes_per_step": int(d2h / args.steps),

@@ -54,7 +54,14 @@ enum pn_precision {
   PN_PREC_F64 = 1,
   /* FP32 state, FP32 material tensors and FP32 arithmetic; traces are
      returned in FP64.  Roughly halves the bytes per step. */
-  PN_PREC_F32 = 2
+  PN_PREC_F32 = 2,
+  /* FP64-class form for GB300, whose FP64 pipe issues about 2 FMAs per SM
+     per clock: state and arithmetic in double-float (each value the
+     unevaluated sum of two floats, a 48-bit significand) on the FP32 pipes,
+     8 bytes per value like FP64.  Host-side inputs and outputs stay FP64.
+     Values must stay within the float exponent range (|x| < 3e38, and
+     magnitudes below 1e-38 flush towards zero). */
+  PN_PREC_DF64 = 3
 };
 
 /* Field storage types; numbering equals PanNDE::Field::FieldType
@@ -159,6 +166,16 @@ typedef struct pn_solver_info {
   double time;
 } pn_solver_info;
 
+/* What pn_solver_create would build, computed on the host only. */
+typedef struct pn_plan {
+  int32_t n_nodes, n_cells;
+  int32_t n_materials;
+  int32_t uniform_spacing;
+  double hx, hy, hz;                  /* the spacings when uniform_spacing */
+  int64_t device_bytes;               /* device memory pn_solver_create allocates */
+  int64_t algorithmic_bytes_per_step;
+} pn_plan;
+
 typedef struct pn_solver pn_solver;
 
 /* ---- entry points ------------------------------------------------------ */
@@ -168,6 +185,29 @@ int pn_abi_version(void);
 
 /* Message for the last failed call on this thread ("" if none). */
 const char *pn_last_error(void);
+
+/* Validate a mesh and domain exactly as pn_solver_create does (same status
+   codes and messages: "DX"/"DY"/"DZ", invalid node id, non-finite input)
+   and report sizes, spacing and the device footprint, without any CUDA
+   call.  Pass one of material / table (the other NULL).  Replaces nothing
+   in the reference (whose constructor does this work, RightHex.hpp:80-90);
+   serving admission uses the footprint before allocating. */
+int pn_plan_solver(const pn_mesh *mesh, const pn_material *material,
+                   const pn_material_table *table, double dt, int32_t precision,
+                   pn_plan *out);
+
+/* Source weights on the host, without any CUDA call: node_force_w[n*3+d] =
+   0.125 * number of (incident cell, force source of direction d) pairs whose
+   cell centre is in the window (HostRSGTDUT::evalXds, HostRSGTDUT.hpp:387-402);
+   cell_moment_w[c*6+k] the same over (corner node, moment source of Voigt
+   component k) pairs (HostUTModel::evalMoments, HostUTModel.hpp:296-311).
+   Either output may be NULL. */
+int pn_plan_sources(const pn_mesh *mesh, const pn_window_source *src, int32_t n,
+                    double *node_force_w, double *cell_moment_w,
+                    int32_t *n_source_nodes, int32_t *n_source_cells);
+
+/* HostUnivariate::evalAt at n times (HostUnivariate.hpp:109-142), on the host. */
+int pn_signal_eval(const pn_signal *signal, const double *t, int32_t n, double *out);
 
 /* Build a solver on the current CUDA device: uploads connectivity, spacing,
    material and density tables.

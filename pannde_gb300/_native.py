@@ -28,6 +28,7 @@ PN_ERR_DEVICE_CHECK = 8
 PN_PREC_F64_EXACT = 0
 PN_PREC_F64 = 1
 PN_PREC_F32 = 2
+PN_PREC_DF64 = 3
 
 # field types (enum pn_field_type) == PanNDE::Field::FieldType
 PN_FIELD_NODE = 0
@@ -79,10 +80,21 @@ class PnSolverInfo(ctypes.Structure):
                 ("dt", c_double), ("time", c_double)]
 
 
+class PnPlan(ctypes.Structure):
+    _fields_ = [("n_nodes", c_int32), ("n_cells", c_int32), ("n_materials", c_int32),
+                ("uniform_spacing", c_int32), ("hx", c_double), ("hy", c_double), ("hz", c_double),
+                ("device_bytes", c_int64), ("algorithmic_bytes_per_step", c_int64)]
+
+
 # every entry point the header declares: name -> (restype, argtypes)
 SIGNATURES = {
     "pn_abi_version": (c_int, []),
     "pn_last_error": (c_char_p, []),
+    "pn_plan_solver": (c_int, [POINTER(PnMesh), POINTER(PnMaterial), POINTER(PnMaterialTable),
+                               c_double, c_int32, POINTER(PnPlan)]),
+    "pn_plan_sources": (c_int, [POINTER(PnMesh), POINTER(PnWindowSource), c_int32, P_double,
+                                P_double, P_int32, P_int32]),
+    "pn_signal_eval": (c_int, [POINTER(PnSignal), P_double, c_int32, P_double]),
     "pn_solver_create": (c_int, [POINTER(PnMesh), POINTER(PnMaterial), c_double, c_int32,
                                  POINTER(c_void_p)]),
     "pn_solver_create_indexed": (c_int, [POINTER(PnMesh), POINTER(PnMaterialTable), c_double,

@@ -124,16 +124,40 @@ struct pn_solver {
     p = nullptr;
   }
 
-  // upload a double host array as T (double or float)
+  bool is_df64() const { return precision == PN_PREC_DF64; }
+
+  // upload a double host array in the storage type (double, float, or the
+  // (hi, lo) float pair of the double-float form)
   void upload_real(void *dst, const double *src_, size_t n) {
     if (n == 0) return;
-    if (esz == 8) {
+    if (is_df64()) {
+      std::vector<float> tmp(2 * n);
+      for (size_t i = 0; i < n; i++) pn::split_df(src_[i], tmp[2 * i], tmp[2 * i + 1]);
+      ck(cudaMemcpyAsync(dst, tmp.data(), n * 8, cudaMemcpyHostToDevice, stream), "upload");
+      ck(cudaStreamSynchronize(stream), "upload sync");
+    } else if (esz == 8) {
       ck(cudaMemcpyAsync(dst, src_, n * 8, cudaMemcpyHostToDevice, stream), "upload");
     } else {
       std::vector<float> tmp(n);
       for (size_t i = 0; i < n; i++) tmp[i] = (float)src_[i];
       ck(cudaMemcpyAsync(dst, tmp.data(), n * 4, cudaMemcpyHostToDevice, stream), "upload");
       ck(cudaStreamSynchronize(stream), "upload sync");
+    }
+  }
+
+  // download n values of the storage type into doubles
+  void download_real(double *dst, const void *src_, size_t n) {
+    if (n == 0 || !dst) return;
+    if (is_df64()) {
+      std::vector<float> tmp(2 * n);
+      ck(cudaMemcpy(tmp.data(), src_, n * 8, cudaMemcpyDeviceToHost), "download");
+      for (size_t i = 0; i < n; i++) dst[i] = (double)tmp[2 * i] + (double)tmp[2 * i + 1];
+    } else if (esz == 8) {
+      ck(cudaMemcpy(dst, src_, n * 8, cudaMemcpyDeviceToHost), "download");
+    } else {
+      std::vector<float> tmp(n);
+      ck(cudaMemcpy(tmp.data(), src_, n * 4, cudaMemcpyDeviceToHost), "download");
+      for (size_t i = 0; i < n; i++) dst[i] = (double)tmp[i];
     }
   }
   void upload_raw(void *dst, const void *src_, size_t bytes) {
@@ -164,15 +188,25 @@ int64_t algorithmic_bytes(const pn_solver *s) {
          (int64_t)s->mesh.n_nodes * (6 * e + 3 * e + e + 32);
 }
 
+// device bytes of the fixed tables and state (sources, sensors and signal
+// rows come on top and are small)
+int64_t footprint(const pn::MeshTables &m, const pn::MaterialTables &mt, int precision) {
+  const int64_t nn = m.n_nodes, nc = m.n_cells;
+  const int64_t e = precision == PN_PREC_F32 ? 4 : 8;
+  const bool per_elem = precision == PN_PREC_F64_EXACT || !m.uniform;
+  int64_t need = nn * 3 * e + nc * 6 * e + nc * 32 + nn * 32 + nn * e + nc * 4 +
+                 (int64_t)mt.n_mat * 36 * e;
+  if (per_elem) need += nn * 3 * e + nc * 3 * e;
+  return need;
+}
+
 void create_device(pn_solver *s) {
   const int32_t nn = s->mesh.n_nodes, nc = s->mesh.n_cells;
   const size_t e = s->esz;
   const bool exact = s->precision == PN_PREC_F64_EXACT;
   const bool per_elem = exact || !s->mesh.uniform;
   // size everything first so that a budget failure allocates nothing
-  int64_t need = (int64_t)nn * 3 * e + (int64_t)nc * 6 * e + (int64_t)nc * 32 + (int64_t)nn * 32 +
-                 (int64_t)nn * e + (int64_t)nc * 4 + (int64_t)s->mat.n_mat * 36 * e;
-  if (per_elem) need += (int64_t)nn * 3 * e + (int64_t)nc * 3 * e;
+  const int64_t need = footprint(s->mesh, s->mat, s->precision);
   const int64_t budget = hbm_budget();
   if (budget >= 0 && need > budget)
     throw pn::SetupError{PN_ERR_ALLOC, "solver needs " + std::to_string(need) +
@@ -211,6 +245,16 @@ void create_device(pn_solver *s) {
   ck(cudaStreamSynchronize(s->stream), "create sync");
 }
 
+// a host double in the storage type T
+template <typename T> T to_store(double v);
+template <> double to_store<double>(double v) { return v; }
+template <> float to_store<float>(double v) { return (float)v; }
+template <> float2 to_store<float2>(double v) {
+  float2 r;
+  pn::split_df(v, r.x, r.y);
+  return r;
+}
+
 template <typename T>
 void fill_launch_args(pn_solver *s, pn::VelArgs<T> &va, pn::StressArgs<T> &sa) {
   std::memset(&va, 0, sizeof(va));
@@ -222,7 +266,9 @@ void fill_launch_args(pn_solver *s, pn::VelArgs<T> &va, pn::StressArgs<T> &sa) {
   va.S0 = (const T *)s->S[0]; va.S1 = (const T *)s->S[1]; va.S2 = (const T *)s->S[2];
   va.S3 = (const T *)s->S[3]; va.S4 = (const T *)s->S[4]; va.S5 = (const T *)s->S[5];
   va.coef = (const T *)s->d_coef;
-  va.gx = (T)(0.25 / s->mesh.hx); va.gy = (T)(0.25 / s->mesh.hy); va.gz = (T)(0.25 / s->mesh.hz);
+  va.gx = to_store<T>(0.25 / s->mesh.hx);
+  va.gy = to_store<T>(0.25 / s->mesh.hy);
+  va.gz = to_store<T>(0.25 / s->mesh.hz);
   va.gnode = (const T *)s->d_gnode;
   if (s->n_force > 0) {
     va.tile_src = s->d_ftile; va.src_elem = s->d_felem; va.src_code = s->d_fcode;
@@ -242,7 +288,7 @@ void fill_launch_args(pn_solver *s, pn::VelArgs<T> &va, pn::StressArgs<T> &sa) {
   sa.ctab = (const T *)s->d_ctab;
   sa.gx = va.gx; sa.gy = va.gy; sa.gz = va.gz;
   sa.gcell = (const T *)s->d_gcell;
-  sa.dt = (T)s->dt;
+  sa.dt = to_store<T>(s->dt);
   if (s->n_moment > 0) {
     sa.tile_src = s->d_mtile; sa.src_elem = s->d_melem; sa.src_code = s->d_mcode;
     sa.src_w = (const T *)s->d_mw;
@@ -368,7 +414,11 @@ void run_steps(pn_solver *s, int32_t nsteps) {
         ck(cudaEventRecord(mv.b, s->stream), "event");
         ck(cudaEventRecord(ms.a, s->stream), "event");
       };
-      if constexpr (std::is_same<T, double>::value) {
+      if constexpr (std::is_same<T, float2>::value) {
+        e1 = pn::launch_velocity_df64(va, k, s->mesh.uniform, s->stream);
+        between();
+        e2 = pn::launch_stress_df64(sa, k, s->mesh.uniform, s->stream);
+      } else if constexpr (std::is_same<T, double>::value) {
         if (s->precision == PN_PREC_F64_EXACT) {
           e1 = pn::launch_velocity_exact(va, k, s->stream);
           between();
@@ -421,7 +471,7 @@ int create_common(const pn_mesh *mesh, double dt, int32_t precision, pn_solver *
     if (!out) return set_err(PN_ERR_INVALID, "null output handle");
     *out = nullptr;
     if (!mesh) return set_err(PN_ERR_INVALID, "null mesh");
-    if (precision < PN_PREC_F64_EXACT || precision > PN_PREC_F32)
+    if (precision < PN_PREC_F64_EXACT || precision > PN_PREC_DF64)
       return set_err(PN_ERR_INVALID, "unknown precision");
     if (!std::isfinite(dt)) return set_err(PN_ERR_NOT_FINITE, "non-finite dt");
     std::unique_ptr<pn_solver> s(new pn_solver());
@@ -444,6 +494,73 @@ extern "C" {
 int pn_abi_version(void) { return PN_ABI_VERSION; }
 
 const char *pn_last_error(void) { return g_err.c_str(); }
+
+int pn_plan_solver(const pn_mesh *mesh, const pn_material *material, const pn_material_table *table,
+                   double dt, int32_t precision, pn_plan *out) {
+  return guarded([&]() -> int {
+    if (!mesh || !out || (!material && !table) || (material && table))
+      return set_err(PN_ERR_INVALID, "plan arguments");
+    if (precision < PN_PREC_F64_EXACT || precision > PN_PREC_DF64)
+      return set_err(PN_ERR_INVALID, "unknown precision");
+    if (!std::isfinite(dt)) return set_err(PN_ERR_NOT_FINITE, "non-finite dt");
+    pn::MeshTables m;
+    pn::MaterialTables mt;
+    pn::build_mesh_tables(*mesh, m);
+    if (material) pn::build_material_from_fields(*material, m, dt, mt);
+    else pn::build_material_from_table(*table, m, dt, mt);
+    std::memset(out, 0, sizeof(*out));
+    out->n_nodes = m.n_nodes;
+    out->n_cells = m.n_cells;
+    out->n_materials = mt.n_mat;
+    out->uniform_spacing = m.uniform ? 1 : 0;
+    out->hx = m.hx;
+    out->hy = m.hy;
+    out->hz = m.hz;
+    out->device_bytes = footprint(m, mt, precision);
+    const int64_t e = precision == PN_PREC_F32 ? 4 : 8;
+    out->algorithmic_bytes_per_step =
+        (int64_t)m.n_cells * (18 * e + 36) + (int64_t)m.n_nodes * (10 * e + 32);
+    return PN_OK;
+  });
+}
+
+int pn_plan_sources(const pn_mesh *mesh, const pn_window_source *src, int32_t n, double *node_force_w,
+                    double *cell_moment_w, int32_t *n_source_nodes, int32_t *n_source_cells) {
+  return guarded([&]() -> int {
+    if (!mesh || n < 0 || (n > 0 && !src)) return set_err(PN_ERR_INVALID, "plan arguments");
+    pn::MeshTables m;
+    pn::build_mesh_tables(*mesh, m);
+    std::vector<pn_window_source> all(src, src + n);
+    std::vector<pn::SourceEntry> fe, me;
+    pn::build_source_entries(m, all, false, fe, me);
+    if (node_force_w)
+      std::fill(node_force_w, node_force_w + (size_t)m.n_nodes * 3, 0.0);
+    if (cell_moment_w)
+      std::fill(cell_moment_w, cell_moment_w + (size_t)m.n_cells * 6, 0.0);
+    int32_t nn = 0, nc = 0;
+    for (size_t i = 0; i < fe.size(); i++) {
+      if (node_force_w) node_force_w[(size_t)fe[i].elem * 3 + fe[i].comp] += fe[i].w;
+      if (i == 0 || fe[i].elem != fe[i - 1].elem) nn++;
+    }
+    for (size_t i = 0; i < me.size(); i++) {
+      if (cell_moment_w) cell_moment_w[(size_t)me[i].elem * 6 + me[i].comp] += me[i].w;
+      if (i == 0 || me[i].elem != me[i - 1].elem) nc++;
+    }
+    if (n_source_nodes) *n_source_nodes = nn;
+    if (n_source_cells) *n_source_cells = nc;
+    return PN_OK;
+  });
+}
+
+int pn_signal_eval(const pn_signal *signal, const double *t, int32_t n, double *out) {
+  return guarded([&]() -> int {
+    if (!signal || n < 0 || (n > 0 && (!t || !out))) return set_err(PN_ERR_INVALID, "signal arguments");
+    pn::Series s;
+    s.build(*signal);
+    for (int32_t i = 0; i < n; i++) out[i] = s.eval(t[i]);
+    return PN_OK;
+  });
+}
 
 int pn_solver_create(const pn_mesh *mesh, const pn_material *material, double dt,
                      int32_t precision, pn_solver **out) {
@@ -563,7 +680,8 @@ int pn_solver_solve(pn_solver *s, int32_t nsteps, double *time_out) {
     if (!s) return set_err(PN_ERR_INVALID, "null solver");
     if (nsteps < 0) return set_err(PN_ERR_INVALID, "negative step count");
     if (s->src_dirty) rebuild_sources(s);
-    if (s->esz == 8) run_steps<double>(s, nsteps);
+    if (s->is_df64()) run_steps<float2>(s, nsteps);
+    else if (s->esz == 8) run_steps<double>(s, nsteps);
     else run_steps<float>(s, nsteps);
     if (time_out) *time_out = s->time;
     return PN_OK;
@@ -574,18 +692,8 @@ int pn_solver_get_state(pn_solver *s, double *const *V, double *const *S) {
   return guarded([&]() -> int {
     if (!s) return set_err(PN_ERR_INVALID, "null solver");
     ck(cudaStreamSynchronize(s->stream), "get_state sync");
-    auto down = [&](double *dst, const void *src_, size_t n) {
-      if (!dst || n == 0) return;
-      if (s->esz == 8) {
-        ck(cudaMemcpy(dst, src_, n * 8, cudaMemcpyDeviceToHost), "download");
-      } else {
-        std::vector<float> tmp(n);
-        ck(cudaMemcpy(tmp.data(), src_, n * 4, cudaMemcpyDeviceToHost), "download");
-        for (size_t i = 0; i < n; i++) dst[i] = (double)tmp[i];
-      }
-    };
-    for (int k = 0; k < 3; k++) if (V) down(V[k], s->V[k], (size_t)s->mesh.n_nodes);
-    for (int k = 0; k < 6; k++) if (S) down(S[k], s->S[k], (size_t)s->mesh.n_cells);
+    for (int k = 0; k < 3; k++) if (V) s->download_real(V[k], s->V[k], (size_t)s->mesh.n_nodes);
+    for (int k = 0; k < 6; k++) if (S) s->download_real(S[k], s->S[k], (size_t)s->mesh.n_cells);
     return PN_OK;
   });
 }

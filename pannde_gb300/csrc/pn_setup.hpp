@@ -94,4 +94,11 @@ void tile_ranges(const std::vector<int32_t> &elems, int32_t n_elems, int tile,
 // NaN / Inf scan.
 bool all_finite(const double *p, int64_t n);
 
+// Split a double into the (hi, lo) float pair of the double-float form:
+// hi = the nearest float, lo = the nearest float to the remainder.
+inline void split_df(double d, float &hi, float &lo) {
+  hi = (float)d;
+  lo = (float)(d - (double)hi);
+}
+
 }  // namespace pn

@@ -90,6 +90,8 @@ cudaError_t launch_velocity_f64(const VelArgs<double> &a, int step, bool uniform
 cudaError_t launch_stress_f64(const StressArgs<double> &a, int step, bool uniform, cudaStream_t st);
 cudaError_t launch_velocity_f32(const VelArgs<float> &a, int step, bool uniform, cudaStream_t st);
 cudaError_t launch_stress_f32(const StressArgs<float> &a, int step, bool uniform, cudaStream_t st);
+cudaError_t launch_velocity_df64(const VelArgs<float2> &a, int step, bool uniform, cudaStream_t st);
+cudaError_t launch_stress_df64(const StressArgs<float2> &a, int step, bool uniform, cudaStream_t st);
 cudaError_t launch_velocity_exact(const VelArgs<double> &a, int step, cudaStream_t st);
 cudaError_t launch_stress_exact(const StressArgs<double> &a, int step, cudaStream_t st);
 

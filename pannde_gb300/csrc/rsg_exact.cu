@@ -56,11 +56,30 @@ __device__ __forceinline__ double dd_cc(const double *__restrict__ f, const int 
   return (value * 0.25) / d;
 }
 
+// sensor traces: V after this step at the sensors of this tile
+__device__ __forceinline__ void record(const VelArgs<double> &a, int n, int step, double v0,
+                                       double v1, double v2) {
+  if (!a.tile_sens) return;
+  const int2 r = a.tile_sens[blockIdx.x];
+  const int64_t rec = a.rec_base + step;
+  if (rec >= a.rec_cap) return;
+  for (int i = r.x; i < r.y; i++) {
+    if (a.sens_node[i] != n) continue;
+    double *t = a.traces + (rec * a.n_sens + a.sens_idx[i]) * 3;
+    t[0] = v0;
+    t[1] = v1;
+    t[2] = v2;
+  }
+}
+
 __global__ void __launch_bounds__(kTile) k_velocity_exact(const VelArgs<double> a, int step) {
   const int n = blockIdx.x * kTile + threadIdx.x;
   if (n >= a.n_nodes) return;
   const double cf = a.coef[n];
-  if (cf == 0.) return;
+  if (cf == 0.) {  // node owned by another partition: not updated, still recorded
+    record(a, n, step, a.V0[n], a.V1[n], a.V2[n]);
+    return;
+  }
   const int4 lo = a.ncc[2 * n], hi = a.ncc[2 * n + 1];
   const int s[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
   const double dxn = a.gnode[n], dyn = a.gnode[a.n_nodes + n], dzn = a.gnode[2 * a.n_nodes + n];
@@ -86,19 +105,7 @@ __global__ void __launch_bounds__(kTile) k_velocity_exact(const VelArgs<double> 
   a.V0[n] = v0;
   a.V1[n] = v1;
   a.V2[n] = v2;
-  if (a.tile_sens) {
-    const int2 r = a.tile_sens[blockIdx.x];
-    const int64_t rec = a.rec_base + step;
-    if (rec < a.rec_cap) {
-      for (int i = r.x; i < r.y; i++) {
-        if (a.sens_node[i] != n) continue;
-        double *t = a.traces + (rec * a.n_sens + a.sens_idx[i]) * 3;
-        t[0] = v0;
-        t[1] = v1;
-        t[2] = v2;
-      }
-    }
-  }
+  record(a, n, step, v0, v1, v2);
 }
 
 __global__ void __launch_bounds__(kTile) k_stress_exact(const StressArgs<double> a, int step) {

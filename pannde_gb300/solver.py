@@ -12,7 +12,8 @@ import numpy as np
 from . import _native as N
 from .cases import Case, HexMesh, sources_struct
 
-PRECISIONS = {"f64_exact": N.PN_PREC_F64_EXACT, "f64": N.PN_PREC_F64, "f32": N.PN_PREC_F32}
+PRECISIONS = {"f64_exact": N.PN_PREC_F64_EXACT, "f64": N.PN_PREC_F64, "f32": N.PN_PREC_F32,
+              "df64": N.PN_PREC_DF64}
 
 
 def _precision(p) -> int:
