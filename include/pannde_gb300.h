@@ -64,6 +64,24 @@ enum pn_precision {
   PN_PREC_DF64 = 3
 };
 
+/* Device forms; OR one into the precision argument of pn_solver_create*.
+   The reference has a single (host) form; these choose how the device holds
+   the same mesh. */
+enum pn_form {
+  /* the grid form when the mesh is a voxel grid (every node on a uniform
+     lattice, every cell a lattice box in the reference corner order, at most
+     half of the lattice box void) and the precision is not PN_PREC_F64_EXACT;
+     else the table form */
+  PN_FORM_AUTO = 0,
+  /* connectivity tables on the device (cell -> 8 nodes, node -> 8 cell
+     slots), two kernels per step; any hex mesh */
+  PN_FORM_TABLE = 0x100,
+  /* implicit lattice indices, one fused kernel per step, double-buffered
+     state; PN_ERR_INVALID when the mesh is not a voxel grid */
+  PN_FORM_GRID = 0x200
+};
+#define PN_FORM_MASK 0xF00
+
 /* Field storage types; numbering equals PanNDE::Field::FieldType
    (modules/PanNDE/include/Field.hpp, NODE=0, CELL=1, CONSTANT=2). */
 enum pn_field_type { PN_FIELD_NODE = 0, PN_FIELD_CELL = 1, PN_FIELD_CONSTANT = 2 };
@@ -160,10 +178,12 @@ typedef struct pn_solver_info {
   int32_t n_source_nodes;    /* nodes with a force source term */
   int32_t n_source_cells;    /* cells with a moment source term */
   int32_t n_sensors;
-  int64_t algorithmic_bytes_per_step; /* HBM bytes one step must move */
+  int64_t algorithmic_bytes_per_step; /* HBM bytes one step must move in this form */
   int64_t device_bytes;      /* device memory held by the solver */
   double dt;
   double time;
+  int32_t form;              /* PN_FORM_TABLE or PN_FORM_GRID */
+  int32_t grid[3];           /* grid form: cells per axis */
 } pn_solver_info;
 
 /* What pn_solver_create would build, computed on the host only. */
@@ -174,6 +194,8 @@ typedef struct pn_plan {
   double hx, hy, hz;                  /* the spacings when uniform_spacing */
   int64_t device_bytes;               /* device memory pn_solver_create allocates */
   int64_t algorithmic_bytes_per_step;
+  int32_t form;                       /* the form PN_FORM_AUTO would pick */
+  int32_t grid[3];                    /* grid form: cells per axis */
 } pn_plan;
 
 typedef struct pn_solver pn_solver;
@@ -270,8 +292,11 @@ int pn_solver_get_time(pn_solver *s, double *time_out);
 /* Facts about the solver (sizes, bytes per step, device memory). */
 int pn_solver_get_info(pn_solver *s, pn_solver_info *info);
 
-/* Device pointers of the state arrays (double* or float* by precision), for
-   zero-copy interop; V[3], S[6] receive the pointers. */
+/* Device pointers of the current state arrays, for zero-copy interop; V[3],
+   S[6] receive the pointers.  Element type by precision (double, float, or
+   float2 (hi, lo) for PN_PREC_DF64); order by form: the caller's node / cell
+   numbering in the table form, the lattice numbering (x fastest) in the grid
+   form. */
 int pn_solver_device_state(pn_solver *s, void **V, void **S);
 
 /* Block until all work enqueued by this solver is done; reports errors from
@@ -281,10 +306,11 @@ int pn_solver_synchronize(pn_solver *s);
 /* Per-kernel device time.  While enabled, every launch of the velocity and
    the stress kernel is bracketed by CUDA events on the solver's stream.
    pn_solver_kernel_times synchronises, returns the summed milliseconds and
-   the launch counts of [velocity, stress] since timing was enabled, and
-   restarts the count.  Profiling aid; no counterpart in the reference. */
+   the launch counts of [velocity, stress, fused grid step] since timing was
+   enabled, and restarts the count.  Profiling aid; no counterpart in the
+   reference. */
 int pn_solver_enable_kernel_timing(pn_solver *s, int32_t enable);
-int pn_solver_kernel_times(pn_solver *s, double *ms /* [2] */, int64_t *launches /* [2] */);
+int pn_solver_kernel_times(pn_solver *s, double *ms /* [3] */, int64_t *launches /* [3] */);
 
 /* Free all device memory of the solver. */
 int pn_solver_destroy(pn_solver *s);

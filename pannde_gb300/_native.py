@@ -30,6 +30,11 @@ PN_PREC_F64 = 1
 PN_PREC_F32 = 2
 PN_PREC_DF64 = 3
 
+# device forms (OR into the precision argument)
+PN_FORM_AUTO = 0
+PN_FORM_TABLE = 0x100
+PN_FORM_GRID = 0x200
+
 # field types (enum pn_field_type) == PanNDE::Field::FieldType
 PN_FIELD_NODE = 0
 PN_FIELD_CELL = 1
@@ -77,13 +82,14 @@ class PnSolverInfo(ctypes.Structure):
                 ("n_materials", c_int32), ("uniform_spacing", c_int32),
                 ("n_source_nodes", c_int32), ("n_source_cells", c_int32), ("n_sensors", c_int32),
                 ("algorithmic_bytes_per_step", c_int64), ("device_bytes", c_int64),
-                ("dt", c_double), ("time", c_double)]
+                ("dt", c_double), ("time", c_double), ("form", c_int32), ("grid", c_int32 * 3)]
 
 
 class PnPlan(ctypes.Structure):
     _fields_ = [("n_nodes", c_int32), ("n_cells", c_int32), ("n_materials", c_int32),
                 ("uniform_spacing", c_int32), ("hx", c_double), ("hy", c_double), ("hz", c_double),
-                ("device_bytes", c_int64), ("algorithmic_bytes_per_step", c_int64)]
+                ("device_bytes", c_int64), ("algorithmic_bytes_per_step", c_int64),
+                ("form", c_int32), ("grid", c_int32 * 3)]
 
 
 # every entry point the header declares: name -> (restype, argtypes)

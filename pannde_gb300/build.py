@@ -3,7 +3,10 @@
 Sources (``pannde_gb300/csrc``):
   rsg_fast.cu   fast FP64 / FP32 kernels      nvcc, sm_103a
   rsg_exact.cu  reference-order FP64 kernels  nvcc, sm_103a, -fmad=false
+  rsg_grid.cu   fused voxel-grid step kernel  nvcc, sm_103a
   pn_setup.cpp  host table construction       g++, -ffp-contract=off
+  pn_table.cpp  table form (any hex mesh)     g++
+  pn_grid.cpp   grid form (voxel meshes)      g++
   pn_capi.cpp   C ABI                         g++
 Translation units compile in parallel; the link uses nvcc (static cudart).
 Output: ``pannde_gb300/_build/libpannde_gb300.so``.
@@ -46,7 +49,10 @@ def _jobs() -> list[tuple[list[str], Path]]:
     jobs = [
         (common_cu + ["-c", str(CSRC / "rsg_fast.cu")], OUT / "rsg_fast.o"),
         (common_cu + ["-fmad=false", "-c", str(CSRC / "rsg_exact.cu")], OUT / "rsg_exact.o"),
+        (common_cu + ["-c", str(CSRC / "rsg_grid.cu")], OUT / "rsg_grid.o"),
         (common_cc + ["-c", str(CSRC / "pn_setup.cpp")], OUT / "pn_setup.o"),
+        (common_cc + ["-c", str(CSRC / "pn_table.cpp")], OUT / "pn_table.o"),
+        (common_cc + ["-c", str(CSRC / "pn_grid.cpp")], OUT / "pn_grid.o"),
         (common_cc + ["-c", str(CSRC / "pn_capi.cpp")], OUT / "pn_capi.o"),
     ]
     return [(cmd + ["-o", str(obj)], obj) for cmd, obj in jobs]

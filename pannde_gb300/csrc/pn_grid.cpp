@@ -1,0 +1,333 @@
+// pn_grid.cpp -- grid form of the solver: voxel-grid meshes, implicit
+// indices, one fused plane-marching kernel per step (rsg_grid.cu) with
+// double-buffered state.  Host arrays stay in the caller's numbering; the
+// device holds the lattice numbering (x fastest) and this file maps between.
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <type_traits>
+
+#include "pn_solver.hpp"
+
+namespace pn {
+
+namespace {
+
+struct Tiles {
+  int tx, ty, bx_count, by_count;
+  int32_t nx, ny, nz;
+  // owning block and local index of lattice column (i, j)
+  void locate(int64_t i, int64_t j, int32_t &blk, int32_t &t) const {
+    const int64_t bx = i / (tx - 1), by = j / (ty - 1);
+    blk = (int32_t)(by * bx_count + bx);
+    t = (int32_t)((i - bx * (tx - 1)) + tx * (j - by * (ty - 1)));
+  }
+  int64_t blocks() const { return (int64_t)bx_count * by_count; }
+};
+
+Tiles tiles_of(const GridMap &g) {
+  Tiles T;
+  T.tx = grid_tile_x();
+  T.ty = grid_tile_y();
+  T.nx = g.nx;
+  T.ny = g.ny;
+  T.nz = g.nz;
+  T.bx_count = g.nx / (T.tx - 1) + 1;
+  T.by_count = g.ny / (T.ty - 1) + 1;
+  return T;
+}
+
+void node_ijk(const GridMap &g, int64_t q, int64_t &i, int64_t &j, int64_t &k) {
+  const int64_t w = g.nx + 1, h = g.ny + 1;
+  i = q % w;
+  j = (q / w) % h;
+  k = q / (w * h);
+}
+
+void cell_ijk(const GridMap &g, int64_t q, int64_t &i, int64_t &j, int64_t &k) {
+  i = q % g.nx;
+  j = (q / g.nx) % g.ny;
+  k = q / ((int64_t)g.nx * g.ny);
+}
+
+// 2: only the C11..C33 block and the shear diagonal; 1: monoclinic about z;
+// 0: general (see c_used in rsg_grid.cu)
+int symmetry_class(const MaterialTables &mt) {
+  bool ortho = true, mono = true;
+  for (int32_t m = 0; m < mt.n_mat; m++) {
+    const double *c = &mt.c36[(size_t)m * 36];
+    for (int k = 0; k < 6; k++)
+      for (int j = 0; j < 6; j++) {
+        const double v = c[k * 6 + j];
+        if (v == 0.0) continue;
+        const bool in_ortho = (k < 3 && j < 3) || k == j;
+        const bool in_mono = in_ortho || (k == 5 && j < 3) || (j == 5 && k < 3) || (k == 3 && j == 4) ||
+                             (k == 4 && j == 3);
+        ortho = ortho && in_ortho;
+        mono = mono && in_mono;
+      }
+  }
+  return ortho ? 2 : mono ? 1 : 0;
+}
+
+// (block, layer, local, payload) rows sorted by (block, layer) with the
+// per (block, layer) ranges
+struct Keyed {
+  int64_t slot;  // block * layers + layer
+  int32_t key, sig, idx;
+  double w;
+};
+
+void ranges_of(std::vector<Keyed> &L, int64_t n_slots, std::vector<int32_t> &rng) {
+  std::stable_sort(L.begin(), L.end(), [](const Keyed &a, const Keyed &b) { return a.slot < b.slot; });
+  rng.assign((size_t)n_slots * 2, 0);
+  size_t e = 0;
+  for (int64_t sl = 0; sl < n_slots; sl++) {
+    rng[(size_t)sl * 2] = (int32_t)e;
+    while (e < L.size() && L[e].slot == sl) e++;
+    rng[(size_t)sl * 2 + 1] = (int32_t)e;
+  }
+}
+
+}  // namespace
+
+bool grid_eligible(const MeshTables &m, const MaterialTables &mt, int precision, const GridMap &g) {
+  (void)m;
+  return g.ok && precision != PN_PREC_F64_EXACT && mt.n_mat < 255;
+}
+
+int64_t grid_footprint(const GridMap &g, const MaterialTables &mt, int precision) {
+  const int64_t e = precision == PN_PREC_F32 ? 4 : 8;
+  const int64_t gn = g.grid_nodes(), gc = g.grid_cells();
+  return 2 * (3 * gn + 6 * gc) * e + gn * e + gc + (int64_t)(mt.n_mat + 1) * 36 * e;
+}
+
+void grid_create(pn_solver *s) {
+  const GridMap &g = s->grid;
+  const int64_t gn = g.grid_nodes(), gc = g.grid_cells();
+  const size_t e = s->esz;
+  for (int b = 0; b < 2; b++) {
+    for (int k = 0; k < 3; k++) {
+      s->V[b][k] = s->alloc<void>((size_t)gn * e);
+      ck(cudaMemsetAsync(s->V[b][k], 0, (size_t)gn * e, s->stream), "memset");
+    }
+    for (int k = 0; k < 6; k++) {
+      s->S[b][k] = s->alloc<void>((size_t)gc * e);
+      ck(cudaMemsetAsync(s->S[b][k], 0, (size_t)gc * e, s->stream), "memset");
+    }
+  }
+  std::vector<double> coef((size_t)gn, 0.0);
+  for (int32_t u = 0; u < s->mesh.n_nodes; u++) coef[g.node_grid[u]] = s->mat.coef[u];
+  s->d_coef = s->alloc<void>((size_t)gn * e);
+  s->upload_real(s->d_coef, coef.data(), coef.size());
+  std::vector<uint8_t> gm((size_t)gc, (uint8_t)s->mat.n_mat);  // void row
+  for (int32_t c = 0; c < s->mesh.n_cells; c++) gm[g.cell_grid[c]] = (uint8_t)s->mat.cell_mat[c];
+  s->d_gmat = s->alloc<uint8_t>((size_t)gc);
+  s->upload_raw(s->d_gmat, gm.data(), gm.size());
+  std::vector<double> ct((size_t)(s->mat.n_mat + 1) * 36, 0.0);
+  for (size_t q = 0; q < s->mat.c36.size(); q++) ct[q] = s->dt * s->mat.c36[q];
+  s->d_ctab = s->alloc<void>(ct.size() * e);
+  s->upload_real(s->d_ctab, ct.data(), ct.size());
+  s->sym = symmetry_class(s->mat);
+  s->cur = 0;
+  ck(cudaStreamSynchronize(s->stream), "create sync");
+}
+
+void grid_put_state(pn_solver *s, const double *const *V, const double *const *S) {
+  const GridMap &g = s->grid;
+  const int64_t gn = g.grid_nodes(), gc = g.grid_cells();
+  std::vector<double> buf;
+  for (int k = 0; k < 3; k++) {
+    buf.assign((size_t)gn, 0.0);
+    if (V && V[k])
+      for (int32_t u = 0; u < s->mesh.n_nodes; u++) buf[g.node_grid[u]] = V[k][u];
+    s->upload_real(s->V[s->cur][k], buf.data(), buf.size());
+    ck(cudaStreamSynchronize(s->stream), "put_state");
+  }
+  for (int k = 0; k < 6; k++) {
+    buf.assign((size_t)gc, 0.0);
+    if (S && S[k])
+      for (int32_t c = 0; c < s->mesh.n_cells; c++) buf[g.cell_grid[c]] = S[k][c];
+    s->upload_real(s->S[s->cur][k], buf.data(), buf.size());
+    ck(cudaStreamSynchronize(s->stream), "put_state");
+  }
+}
+
+void grid_get_state(pn_solver *s, double *const *V, double *const *S) {
+  const GridMap &g = s->grid;
+  std::vector<double> buf;
+  for (int k = 0; k < 3; k++) {
+    if (!V || !V[k]) continue;
+    buf.resize((size_t)g.grid_nodes());
+    s->download_real(buf.data(), s->V[s->cur][k], buf.size());
+    for (int32_t u = 0; u < s->mesh.n_nodes; u++) V[k][u] = buf[g.node_grid[u]];
+  }
+  for (int k = 0; k < 6; k++) {
+    if (!S || !S[k]) continue;
+    buf.resize((size_t)g.grid_cells());
+    s->download_real(buf.data(), s->S[s->cur][k], buf.size());
+    for (int32_t c = 0; c < s->mesh.n_cells; c++) S[k][c] = buf[g.cell_grid[c]];
+  }
+}
+
+void grid_sources(pn_solver *s) {
+  std::vector<SourceEntry> fe, me;
+  build_source_entries(s->mesh, s->src, false, fe, me);
+  ck(cudaStreamSynchronize(s->stream), "sources sync");
+  s->release(s->d_frng); s->release(s->d_fkey); s->release(s->d_fsig); s->release(s->d_fw);
+  s->release(s->d_mrng); s->release(s->d_mkey); s->release(s->d_msig); s->release(s->d_mw);
+  const GridMap &g = s->grid;
+  const Tiles T = tiles_of(g);
+  s->n_force = (int32_t)fe.size();
+  s->n_moment = (int32_t)me.size();
+  s->n_src_nodes = s->n_src_cells = 0;
+  auto upload = [&](std::vector<Keyed> &L, int64_t layers, int2 *&rng, int32_t *&key, int32_t *&sig,
+                    void *&w) {
+    if (L.empty()) return;
+    std::vector<int32_t> r;
+    ranges_of(L, T.blocks() * layers, r);
+    std::vector<int32_t> k(L.size()), sg(L.size());
+    std::vector<double> wt(L.size());
+    for (size_t q = 0; q < L.size(); q++) {
+      k[q] = L[q].key;
+      sg[q] = L[q].sig;
+      wt[q] = L[q].w;
+    }
+    rng = s->alloc<int2>(r.size() * 4);
+    key = s->alloc<int32_t>(k.size() * 4);
+    sig = s->alloc<int32_t>(sg.size() * 4);
+    w = s->alloc<void>(wt.size() * s->esz);
+    s->upload_raw(rng, r.data(), r.size() * 4);
+    s->upload_raw(key, k.data(), k.size() * 4);
+    s->upload_raw(sig, sg.data(), sg.size() * 4);
+    s->upload_real(w, wt.data(), wt.size());
+  };
+  std::vector<Keyed> F, M;
+  for (size_t q = 0; q < fe.size(); q++) {
+    int64_t i, j, k;
+    node_ijk(g, g.node_grid[fe[q].elem], i, j, k);
+    int32_t blk, t;
+    T.locate(i, j, blk, t);
+    F.push_back(Keyed{(int64_t)blk * (g.nz + 1) + k, t | (fe[q].comp << 16), fe[q].sig, 0, fe[q].w});
+    if (q == 0 || fe[q].elem != fe[q - 1].elem) s->n_src_nodes++;
+  }
+  for (size_t q = 0; q < me.size(); q++) {
+    int64_t i, j, k;
+    cell_ijk(g, g.cell_grid[me[q].elem], i, j, k);
+    int32_t blk, t;
+    T.locate(i, j, blk, t);
+    M.push_back(Keyed{(int64_t)blk * g.nz + k, t | (me[q].comp << 16), me[q].sig, 0, s->dt * me[q].w});
+    if (q == 0 || me[q].elem != me[q - 1].elem) s->n_src_cells++;
+  }
+  upload(F, g.nz + 1, s->d_frng, s->d_fkey, s->d_fsig, s->d_fw);
+  upload(M, g.nz, s->d_mrng, s->d_mkey, s->d_msig, s->d_mw);
+  ck(cudaStreamSynchronize(s->stream), "sources upload");
+}
+
+void grid_sensors(pn_solver *s, const std::vector<std::pair<int32_t, int32_t>> &pr) {
+  const GridMap &g = s->grid;
+  const Tiles T = tiles_of(g);
+  std::vector<Keyed> L;
+  for (auto &p : pr) {
+    int64_t i, j, k;
+    node_ijk(g, g.node_grid[p.first], i, j, k);
+    int32_t blk, t;
+    T.locate(i, j, blk, t);
+    L.push_back(Keyed{(int64_t)blk * (g.nz + 1) + k, t, 0, p.second, 0.0});
+  }
+  std::vector<int32_t> r;
+  ranges_of(L, T.blocks() * (g.nz + 1), r);
+  std::vector<int32_t> key(L.size()), idx(L.size());
+  for (size_t q = 0; q < L.size(); q++) {
+    key[q] = L[q].key;
+    idx[q] = L[q].idx;
+  }
+  s->d_srng = s->alloc<int2>(r.size() * 4);
+  s->d_skey = s->alloc<int32_t>(key.size() * 4);
+  s->d_sidx = s->alloc<int32_t>(idx.size() * 4);
+  s->upload_raw(s->d_srng, r.data(), r.size() * 4);
+  s->upload_raw(s->d_skey, key.data(), key.size() * 4);
+  s->upload_raw(s->d_sidx, idx.data(), idx.size() * 4);
+}
+
+namespace {
+
+template <typename T>
+void run(pn_solver *s, int32_t nsteps) {
+  const GridMap &g = s->grid;
+  GridArgs<T> a;
+  std::memset(&a, 0, sizeof(a));
+  a.nx = g.nx;
+  a.ny = g.ny;
+  a.nz = g.nz;
+  a.coef = (const T *)s->d_coef;
+  a.mat = s->d_gmat;
+  a.ctab = (const T *)s->d_ctab;
+  a.g[0] = to_store<T>(0.25 / s->mesh.hx);
+  a.g[1] = to_store<T>(0.25 / s->mesh.hy);
+  a.g[2] = to_store<T>(0.25 / s->mesh.hz);
+  if (s->n_force > 0) {
+    a.f_rng = s->d_frng; a.f_key = s->d_fkey; a.f_sig = s->d_fsig; a.f_w = (const T *)s->d_fw;
+  }
+  if (s->n_moment > 0) {
+    a.m_rng = s->d_mrng; a.m_key = s->d_mkey; a.m_sig = s->d_msig; a.m_w = (const T *)s->d_mw;
+  }
+  a.n_sens = s->n_sens;
+  a.traces = s->d_traces;
+  const int64_t nsig = (int64_t)s->src.size();
+  int32_t done = 0;
+  while (done < nsteps) {
+    int32_t chunk = nsteps - done;
+    ensure_signal_rows(s, chunk);
+    if (nsig > 0 && !s->sig_hold)
+      chunk = (int32_t)std::min<int64_t>(chunk, s->sig_step0 + s->sig_rows - s->step);
+    for (int32_t k = 0; k < chunk; k++) {
+      const int in = s->cur, out = s->cur ^ 1;
+      for (int c = 0; c < 3; c++) {
+        a.V_in[c] = (const T *)s->V[in][c];
+        a.V_out[c] = (T *)s->V[out][c];
+      }
+      for (int c = 0; c < 6; c++) {
+        a.S_in[c] = (const T *)s->S[in][c];
+        a.S_out[c] = (T *)s->S[out][c];
+      }
+      a.sigval = nsig > 0 ? (const T *)s->d_sig + sig_row(s, k) * nsig : nullptr;
+      a.rec = s->rec_count + k;
+      const bool rec_on = s->n_sens > 0 && a.rec < s->rec_cap;
+      a.s_rng = rec_on ? s->d_srng : nullptr;
+      a.s_key = s->d_skey;
+      a.s_idx = s->d_sidx;
+      pn_solver::Mark m{};
+      if (s->timing) {
+        ck(cudaEventCreate(&m.a), "event");
+        ck(cudaEventCreate(&m.b), "event");
+        m.kind = 2;
+        ck(cudaEventRecord(m.a, s->stream), "event");
+      }
+      cudaError_t e;
+      if constexpr (std::is_same<T, float2>::value) e = launch_grid_df64(a, s->sym, s->stream);
+      else if constexpr (std::is_same<T, double>::value) e = launch_grid_f64(a, s->sym, s->stream);
+      else e = launch_grid_f32(a, s->sym, s->stream);
+      if (s->timing) {
+        ck(cudaEventRecord(m.b, s->stream), "event");
+        s->marks.push_back(m);
+      }
+      ck(e, "grid step launch");
+      s->cur ^= 1;
+      s->time += s->dt;  // HostRSGTDUT.hpp:166
+    }
+    s->step += chunk;
+    s->rec_count += chunk;
+    done += chunk;
+  }
+}
+
+}  // namespace
+
+void grid_run(pn_solver *s, int32_t nsteps) {
+  if (s->is_df64()) run<float2>(s, nsteps);
+  else if (s->esz == 8) run<double>(s, nsteps);
+  else run<float>(s, nsteps);
+}
+
+}  // namespace pn

@@ -370,6 +370,87 @@ void build_source_entries(const MeshTables &t, const std::vector<pn_window_sourc
   }
 }
 
+void detect_grid(const MeshTables &t, GridMap &g, double max_void_fraction) {
+  g = GridMap();
+  if (!t.uniform || t.n_cells == 0) {
+    g.why = t.n_cells == 0 ? "no cells" : "spacing not uniform";
+    return;
+  }
+  double x0 = t.x[0], y0 = t.y[0], z0 = t.z[0];
+  for (int32_t n = 0; n < t.n_nodes; n++) {
+    x0 = std::min(x0, t.x[n]);
+    y0 = std::min(y0, t.y[n]);
+    z0 = std::min(z0, t.z[n]);
+  }
+  std::vector<int64_t> gi(t.n_nodes), gj(t.n_nodes), gk(t.n_nodes);
+  int64_t mi = 0, mj = 0, mk = 0;
+  auto lattice = [](double v, double o, double h, int64_t &out) {
+    const double f = (v - o) / h;
+    out = (int64_t)std::llround(f);
+    return std::fabs(f - (double)out) <= 1e-6 && out >= 0 && out < (1 << 20);
+  };
+  for (int32_t n = 0; n < t.n_nodes; n++) {
+    if (!lattice(t.x[n], x0, t.hx, gi[n]) || !lattice(t.y[n], y0, t.hy, gj[n]) ||
+        !lattice(t.z[n], z0, t.hz, gk[n])) {
+      g.why = "node off the lattice";
+      return;
+    }
+    mi = std::max(mi, gi[n]);
+    mj = std::max(mj, gj[n]);
+    mk = std::max(mk, gk[n]);
+  }
+  if (mi < 1 || mj < 1 || mk < 1) {
+    g.why = "degenerate lattice";
+    return;
+  }
+  const int64_t nx = mi, ny = mj, nz = mk;
+  const int64_t gnodes = (nx + 1) * (ny + 1) * (nz + 1), gcells = nx * ny * nz;
+  if (gnodes >= (int64_t(1) << 31) - 1) {
+    g.why = "lattice too large for 32-bit indices";
+    return;
+  }
+  if ((double)(gcells - t.n_cells) > max_void_fraction * (double)gcells) {
+    g.why = "lattice box mostly void";
+    return;
+  }
+  g.nx = (int32_t)nx;
+  g.ny = (int32_t)ny;
+  g.nz = (int32_t)nz;
+  g.node_grid.resize(t.n_nodes);
+  std::vector<uint8_t> taken((size_t)gnodes, 0);
+  for (int32_t n = 0; n < t.n_nodes; n++) {
+    const int64_t q = (gk[n] * (ny + 1) + gj[n]) * (nx + 1) + gi[n];
+    if (taken[q]) {
+      g.why = "two nodes on one lattice site";
+      return;
+    }
+    taken[q] = 1;
+    g.node_grid[n] = q;
+  }
+  static const int bx[8] = {0, 1, 1, 0, 0, 1, 1, 0}, by[8] = {0, 0, 1, 1, 0, 0, 1, 1},
+                   bz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+  g.cell_grid.resize(t.n_cells);
+  std::vector<uint8_t> ctaken((size_t)gcells, 0);
+  for (int32_t c = 0; c < t.n_cells; c++) {
+    const int32_t *h = &t.hex[(size_t)c * 8];
+    const int64_t i0 = gi[h[0]], j0 = gj[h[0]], k0 = gk[h[0]];
+    for (int kb = 0; kb < 8; kb++) {
+      if (gi[h[kb]] != i0 + bx[kb] || gj[h[kb]] != j0 + by[kb] || gk[h[kb]] != k0 + bz[kb]) {
+        g.why = "cell is not a lattice box in corner order";
+        return;
+      }
+    }
+    const int64_t q = (k0 * ny + j0) * nx + i0;
+    if (ctaken[q]) {
+      g.why = "two cells on one lattice site";
+      return;
+    }
+    ctaken[q] = 1;
+    g.cell_grid[c] = q;
+  }
+  g.ok = true;
+}
+
 void tile_ranges(const std::vector<int32_t> &elems, int32_t n_elems, int tile,
                  std::vector<int32_t> &ranges) {
   const int64_t n_tiles = ((int64_t)n_elems + tile - 1) / tile;

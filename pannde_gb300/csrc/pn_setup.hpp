@@ -87,6 +87,28 @@ void build_source_entries(const MeshTables &t, const std::vector<pn_window_sourc
                           bool exact, std::vector<SourceEntry> &force,
                           std::vector<SourceEntry> &moment);
 
+// Voxel-grid view of a mesh: every node on the lattice x0 + i*hx (etc.),
+// every cell the axis-aligned box (i..i+1, j..j+1, k..k+1) with its corners
+// in the reference's corner order, no two nodes or cells on one lattice site.
+// Lattice sites without a mesh node / cell are "void": their velocity and
+// stress stay zero, which is what a missing (-1) slot contributes in the
+// reference (RightHex.hpp:225-231).  Internal numbering is x fastest:
+//   grid node (i,j,k) -> (k*(ny+1) + j)*(nx+1) + i
+//   grid cell (i,j,k) -> (k*ny + j)*nx + i
+struct GridMap {
+  bool ok = false;
+  std::string why;               // reason when not a grid
+  int32_t nx = 0, ny = 0, nz = 0;  // cells per axis
+  std::vector<int64_t> node_grid;  // mesh node -> grid node
+  std::vector<int64_t> cell_grid;  // mesh cell -> grid cell
+  int64_t grid_nodes() const { return (int64_t)(nx + 1) * (ny + 1) * (nz + 1); }
+  int64_t grid_cells() const { return (int64_t)nx * ny * nz; }
+};
+
+// Detects the voxel-grid structure of a uniformly spaced mesh; gives up
+// (ok=false) when the lattice box holds more than max_void_fraction void cells.
+void detect_grid(const MeshTables &t, GridMap &g, double max_void_fraction = 0.5);
+
 // Per-tile [begin,end) ranges of a list sorted by element.
 void tile_ranges(const std::vector<int32_t> &elems, int32_t n_elems, int tile,
                  std::vector<int32_t> &ranges /* [n_tiles*2] */);

@@ -1,0 +1,233 @@
+// pn_solver.hpp -- the solver object behind the C ABI (private).
+//
+// Two device forms share it:
+//   table form  connectivity tables (cell->8 nodes, node->8 cell slots) and
+//               two kernels per step (rsg_fast.cu / rsg_exact.cu); any hex mesh
+//   grid form   voxel-grid meshes (pn::detect_grid): implicit indices, one fused
+//               kernel per step, double-buffered state (rsg_grid.cu)
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstdlib>
+#include <string>
+#include <vector>
+
+#include "../../include/pannde_gb300.h"
+#include "pn_setup.hpp"
+#include "rsg_common.cuh"
+#include "rsg_grid.cuh"
+
+namespace pn {
+
+struct CudaError {
+  cudaError_t e;
+  const char *what;
+};
+
+inline void ck(cudaError_t e, const char *what) {
+  if (e != cudaSuccess) throw CudaError{e, what};
+}
+
+// Optional artificial HBM budget (bytes) for allocation-failure tests:
+// PN_HBM_BUDGET_BYTES caps the device memory one solver may hold.
+inline int64_t hbm_budget() {
+  const char *s = std::getenv("PN_HBM_BUDGET_BYTES");
+  if (!s || !*s) return -1;
+  return std::strtoll(s, nullptr, 10);
+}
+
+constexpr int64_t kSigRowsCap = 1 << 16;  // signal rows uploaded at once
+
+// a host double in the storage type T
+template <typename T> inline T to_store(double v);
+template <> inline double to_store<double>(double v) { return v; }
+template <> inline float to_store<float>(double v) { return (float)v; }
+template <> inline float2 to_store<float2>(double v) {
+  float2 r;
+  split_df(v, r.x, r.y);
+  return r;
+}
+
+}  // namespace pn
+
+struct pn_solver {
+  int device = 0;
+  int precision = PN_PREC_F64;
+  int form = PN_FORM_TABLE;
+  cudaStream_t stream = nullptr;
+  double dt = 0., time = 0.;
+  int64_t step = 0;
+  size_t esz = 8;  // bytes per state value
+
+  pn::MeshTables mesh;
+  pn::MaterialTables mat;
+
+  std::vector<void *> allocs;
+  int64_t dev_bytes = 0;
+
+  // state: V[3] over nodes, S[6] over cells (grid form: buffer `cur` of two)
+  void *V[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+  void *S[2][6] = {{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr},
+                   {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}};
+  int cur = 0;
+  void *d_coef = nullptr, *d_ctab = nullptr;
+
+  // table form
+  int4 *d_hex = nullptr, *d_ncc = nullptr;
+  void *d_gnode = nullptr, *d_gcell = nullptr;
+  int32_t *d_mat = nullptr;
+
+  // grid form
+  pn::GridMap grid;
+  int sym = 0;             // material symmetry class of the stiffness table
+  uint8_t *d_gmat = nullptr;
+
+  // sources (both forms)
+  std::vector<pn_window_source> src;
+  std::vector<std::vector<double>> src_t, src_v;  // owned copies of signal arrays
+  std::vector<pn::Series> series;
+  bool src_dirty = false;
+  bool has_moments = false;
+  int32_t n_force = 0, n_moment = 0, n_src_nodes = 0, n_src_cells = 0;
+  // table-form lists: per-tile ranges, element, code, weight
+  int2 *d_ftile = nullptr, *d_mtile = nullptr;
+  int32_t *d_felem = nullptr, *d_fcode = nullptr, *d_melem = nullptr, *d_mcode = nullptr;
+  // grid-form lists: per (block, layer) ranges, key, signal
+  int2 *d_frng = nullptr, *d_mrng = nullptr;
+  int32_t *d_fkey = nullptr, *d_fsig = nullptr, *d_mkey = nullptr, *d_msig = nullptr;
+  void *d_fw = nullptr, *d_mw = nullptr;
+  // signal table: rows [sig_step0, sig_step0 + sig_rows) of [n_sig] values;
+  // sig_hold: the last row holds for every later step
+  void *d_sig = nullptr;
+  int64_t sig_step0 = 0, sig_rows = 0, sig_alloc_rows = 0;
+  bool sig_hold = false, sig_valid = false;
+
+  // sensors
+  int32_t n_sens = 0;
+  int2 *d_stile = nullptr, *d_srng = nullptr;
+  int32_t *d_snode = nullptr, *d_sidx = nullptr, *d_skey = nullptr;
+  double *d_traces = nullptr;
+  int64_t rec_cap = 0, rec_count = 0;
+
+  // optional per-kernel event timing (kind 0 velocity, 1 stress, 2 fused step)
+  bool timing = false;
+  struct Mark {
+    cudaEvent_t a, b;
+    int kind;
+  };
+  std::vector<Mark> marks;
+
+  bool is_df64() const { return precision == PN_PREC_DF64; }
+
+  template <typename P>
+  P *alloc(size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    const int64_t budget = pn::hbm_budget();
+    if (budget >= 0 && dev_bytes + (int64_t)bytes > budget)
+      throw pn::SetupError{PN_ERR_ALLOC, "device allocation exceeds PN_HBM_BUDGET_BYTES"};
+    void *p = nullptr;
+    const cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      throw pn::SetupError{PN_ERR_ALLOC, std::string("cudaMalloc failed: ") + cudaGetErrorString(e)};
+    }
+    allocs.push_back(p);
+    dev_bytes += (int64_t)bytes;
+    return (P *)p;
+  }
+
+  template <typename P>
+  void release(P *&p) {
+    if (!p) return;
+    auto it = std::find(allocs.begin(), allocs.end(), (void *)p);
+    if (it != allocs.end()) allocs.erase(it);
+    cudaFree((void *)p);
+    p = nullptr;
+  }
+
+  // upload a double host array in the storage type (double, float, or the
+  // (hi, lo) float pair of the double-float form)
+  void upload_real(void *dst, const double *src_, size_t n) {
+    if (n == 0) return;
+    if (is_df64()) {
+      std::vector<float> tmp(2 * n);
+      for (size_t i = 0; i < n; i++) pn::split_df(src_[i], tmp[2 * i], tmp[2 * i + 1]);
+      pn::ck(cudaMemcpyAsync(dst, tmp.data(), n * 8, cudaMemcpyHostToDevice, stream), "upload");
+      pn::ck(cudaStreamSynchronize(stream), "upload sync");
+    } else if (esz == 8) {
+      pn::ck(cudaMemcpyAsync(dst, src_, n * 8, cudaMemcpyHostToDevice, stream), "upload");
+    } else {
+      std::vector<float> tmp(n);
+      for (size_t i = 0; i < n; i++) tmp[i] = (float)src_[i];
+      pn::ck(cudaMemcpyAsync(dst, tmp.data(), n * 4, cudaMemcpyHostToDevice, stream), "upload");
+      pn::ck(cudaStreamSynchronize(stream), "upload sync");
+    }
+  }
+
+  // download n values of the storage type into doubles
+  void download_real(double *dst, const void *src_, size_t n) {
+    if (n == 0 || !dst) return;
+    if (is_df64()) {
+      std::vector<float> tmp(2 * n);
+      pn::ck(cudaMemcpy(tmp.data(), src_, n * 8, cudaMemcpyDeviceToHost), "download");
+      for (size_t i = 0; i < n; i++) dst[i] = (double)tmp[2 * i] + (double)tmp[2 * i + 1];
+    } else if (esz == 8) {
+      pn::ck(cudaMemcpy(dst, src_, n * 8, cudaMemcpyDeviceToHost), "download");
+    } else {
+      std::vector<float> tmp(n);
+      pn::ck(cudaMemcpy(tmp.data(), src_, n * 4, cudaMemcpyDeviceToHost), "download");
+      for (size_t i = 0; i < n; i++) dst[i] = (double)tmp[i];
+    }
+  }
+
+  void upload_raw(void *dst, const void *src_, size_t bytes) {
+    if (bytes == 0) return;
+    pn::ck(cudaMemcpyAsync(dst, src_, bytes, cudaMemcpyHostToDevice, stream), "upload");
+  }
+
+  void clear_marks() {
+    for (auto &m : marks) {
+      cudaEventDestroy(m.a);
+      cudaEventDestroy(m.b);
+    }
+    marks.clear();
+  }
+
+  ~pn_solver() {
+    clear_marks();
+    for (void *p : allocs) cudaFree(p);
+    allocs.clear();
+  }
+};
+
+namespace pn {
+
+// shared by both forms (pn_capi.cpp)
+void ensure_signal_rows(pn_solver *s, int64_t nsteps);
+int64_t sig_row(const pn_solver *s, int64_t step_in_call);  // row of this step
+
+// table form (pn_table.cpp)
+int64_t table_footprint(const MeshTables &m, const MaterialTables &mt, int precision);
+void table_create(pn_solver *s);
+void table_sources(pn_solver *s);
+void table_sensors(pn_solver *s, const std::vector<std::pair<int32_t, int32_t>> &sorted);
+void table_run(pn_solver *s, int32_t nsteps);
+void table_put_state(pn_solver *s, const double *const *V, const double *const *S);
+void table_get_state(pn_solver *s, double *const *V, double *const *S);
+
+// grid form (pn_grid.cpp)
+bool grid_eligible(const MeshTables &m, const MaterialTables &mt, int precision, const GridMap &g);
+int64_t grid_footprint(const GridMap &g, const MaterialTables &mt, int precision);
+void grid_create(pn_solver *s);
+void grid_sources(pn_solver *s);
+void grid_sensors(pn_solver *s, const std::vector<std::pair<int32_t, int32_t>> &sorted);
+void grid_run(pn_solver *s, int32_t nsteps);
+void grid_put_state(pn_solver *s, const double *const *V, const double *const *S);
+void grid_get_state(pn_solver *s, double *const *V, double *const *S);
+
+// algorithmic HBM bytes of one step in the solver's form
+int64_t step_bytes(const pn_solver *s);
+
+}  // namespace pn

@@ -1,0 +1,323 @@
+// rsg_grid.cu -- the RSG leapfrog on voxel-grid meshes: one fused kernel per
+// step that marches node layers along z through shared-memory tiles.
+//
+// The mesh is a lattice of nx*ny*nz cells (void sites hold zero stress and
+// velocity, which is what a missing incident cell contributes in the
+// reference, RightHex.hpp:225-231).  Indices are implicit: no connectivity
+// table is read.  State is double-buffered (read *_in, write *_out) so that
+// neighbouring tiles never see a half-updated step.
+//
+// A block owns a (TX-1) x (TY-1) column of cells and the same column of
+// nodes; its TX x TY threads are the nodes of the column plus a one-node
+// apron on the +x / +y side.  For each node layer k = 0..nz:
+//   A  stage cell layer k of S_in (a (TX+1) x (TY+1) tile with a one-cell
+//      apron on the -x / -y side) in shared memory; issue the loads of layer
+//      k+1 into registers (software pipelining)
+//   B  velocity update of node layer k (HostRSGTDUT.hpp:338-362): the eight
+//      incident cells are the four tile neighbours in cell layers k-1 and k;
+//      per layer the four values give px=(B+C)-(A+D), py=(C+D)-(A+B),
+//      s=(A+B)+(C+D), and Dx=px[k-1]+px[k], Dy=py[k-1]+py[k], Dz=s[k]-s[k-1]
+//      with layer k-1's partial sums kept in registers.  New V goes to shared
+//      memory and, for owned nodes, to V_out.
+//   C  stress update of cell layer k-1 (HostRSGTDUT.hpp:278-293): the same
+//      partial sums over the corner velocities of node layers k-1 and k.
+// The apron node row/column is computed by both neighbouring tiles
+// (identical inputs, identical result) and written only by its owner.
+#include <cstdint>
+
+#include "df64.cuh"
+#include "rsg_common.cuh"
+#include "rsg_grid.cuh"
+
+namespace pn {
+namespace {
+
+template <typename R> struct GNum;
+template <> struct GNum<float> {
+  using S = float;
+  static __device__ __forceinline__ float ld(const float *p, int64_t i) { return __ldg(p + i); }
+  static __device__ __forceinline__ void st(float *p, int64_t i, float v) { p[i] = v; }
+  static __device__ __forceinline__ float val(float v) { return v; }
+  static __device__ __forceinline__ float sto(float v) { return v; }
+  static __device__ __forceinline__ double dbl(float v) { return (double)v; }
+};
+template <> struct GNum<double> {
+  using S = double;
+  static __device__ __forceinline__ double ld(const double *p, int64_t i) { return __ldg(p + i); }
+  static __device__ __forceinline__ void st(double *p, int64_t i, double v) { p[i] = v; }
+  static __device__ __forceinline__ double val(double v) { return v; }
+  static __device__ __forceinline__ double sto(double v) { return v; }
+  static __device__ __forceinline__ double dbl(double v) { return v; }
+};
+template <> struct GNum<df64> {
+  using S = float2;
+  static __device__ __forceinline__ df64 ld(const float2 *p, int64_t i) {
+    const float2 v = __ldg(p + i);
+    return df64(v.x, v.y);
+  }
+  static __device__ __forceinline__ void st(float2 *p, int64_t i, df64 v) { p[i] = make_float2(v.hi, v.lo); }
+  static __device__ __forceinline__ df64 val(float2 v) { return df64(v.x, v.y); }
+  static __device__ __forceinline__ float2 sto(df64 v) { return make_float2(v.hi, v.lo); }
+  static __device__ __forceinline__ double dbl(df64 v) { return (double)v.hi + (double)v.lo; }
+};
+
+// stiffness entries kept by material symmetry class (all others are zero):
+// 0 general, 1 monoclinic about z (no C14 C15 C24 C25 C34 C35 C46 C56),
+// 2 orthotropic in the axes (C11..C33 block and the three shear diagonals)
+__host__ __device__ constexpr bool c_used(int sym, int k, int j) {
+  return sym == 0 ? true
+       : sym == 2 ? ((k < 3 && j < 3) || k == j)
+                  : ((k < 3 && j < 3) || k == j || (k == 5 && j < 3) || (j == 5 && k < 3) ||
+                     (k == 3 && j == 4) || (k == 4 && j == 3));
+}
+
+template <typename R, int TX, int TY, int SYM>
+__global__ void __launch_bounds__(TX *TY) k_grid_step(const GridArgs<typename GNum<R>::S> a) {
+  using N = GNum<R>;
+  using St = typename N::S;
+  constexpr int NT = TX * TY;
+  constexpr int CW = TX + 1, CH = TY + 1, CT = CW * CH;  // cell tile
+  constexpr int PF = (CT + NT - 1) / NT;                  // staged cells per thread
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  St *sS = reinterpret_cast<St *>(smem_raw);  // [3][6][CT]
+  St *sV = sS + 3 * 6 * CT;                    // [2][3][NT]
+
+  const int t = threadIdx.x;
+  const int tx = t % TX, ty = t / TX;
+  const int i0 = blockIdx.x * (TX - 1), j0 = blockIdx.y * (TY - 1);
+  const int blk = blockIdx.y * gridDim.x + blockIdx.x;
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+  const int i = i0 + tx, j = j0 + ty;
+  const bool node_in = (i <= nx) && (j <= ny);
+  const bool node_own = node_in && tx < TX - 1 && ty < TY - 1;
+  const bool cell_own = tx < TX - 1 && ty < TY - 1 && i < nx && j < ny;
+  const int64_t nplane = (int64_t)(nx + 1) * (ny + 1), cplane = (int64_t)nx * ny;
+  const int64_t nidx0 = (int64_t)j * (nx + 1) + i;  // node index in its layer
+  const int64_t cidx0 = (int64_t)j * nx + i;        // cell index in its layer
+  const R gx = N::val(a.g[0]), gy = N::val(a.g[1]), gz = N::val(a.g[2]);
+
+  // staged cells of this thread: tile position and validity per layer
+  int pf_off[PF];
+  bool pf_ok[PF];
+#pragma unroll
+  for (int p = 0; p < PF; p++) {
+    const int q = t + p * NT;
+    const int cx = q % CW, cy = q / CW;
+    const int ci = i0 - 1 + cx, cj = j0 - 1 + cy;
+    pf_ok[p] = q < CT && ci >= 0 && ci < nx && cj >= 0 && cj < ny;
+    pf_off[p] = pf_ok[p] ? cj * nx + ci : 0;
+  }
+  R pf[PF][6];
+  auto issue = [&](int kc) {  // loads of cell layer kc (zeros outside)
+#pragma unroll
+    for (int p = 0; p < PF; p++) {
+      const bool ok = pf_ok[p] && kc < nz;
+      const int64_t g = (int64_t)kc * cplane + pf_off[p];
+#pragma unroll
+      for (int f = 0; f < 6; f++) pf[p][f] = ok ? N::ld(a.S_in[f], g) : R();
+    }
+  };
+  issue(0);
+
+  // layer k-1 partial sums: velocity (per stress field) and stress (per V comp)
+  R vpx0 = R(), vpx4 = R(), vpx5 = R(), vpy1 = R(), vpy3 = R(), vpy5 = R(), vs2 = R(), vs3 = R(),
+    vs4 = R();
+  R spx[3], spy[3], ss[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) spx[c] = spy[c] = ss[c] = R();
+
+  for (int k = 0; k <= nz; k++) {
+    const int slot = (k + 1) % 3;  // cell layer k; layer -1 uses slot 0
+    St *Sk = sS + slot * 6 * CT;
+    // ---- A: stage cell layer k, prefetch layer k+1
+#pragma unroll
+    for (int p = 0; p < PF; p++) {
+      const int q = t + p * NT;
+      if (q < CT) {
+#pragma unroll
+        for (int f = 0; f < 6; f++) Sk[f * CT + q] = N::sto(pf[p][f]);
+      }
+    }
+    if (k < nz) issue(k + 1);
+    R vold[3], cf = R();
+    if (node_in) {
+      const int64_t n = (int64_t)k * nplane + nidx0;
+      cf = N::ld(a.coef, n);
+#pragma unroll
+      for (int c = 0; c < 3; c++) vold[c] = N::ld(a.V_in[c], n);
+    }
+    __syncthreads();
+
+    // ---- B: velocity of node layer k
+    St *Vk = sV + (k & 1) * 3 * NT;
+    if (node_in) {
+      const int ia = ty * CW + tx, ib = ia + 1, ic = ia + CW + 1, id = ia + CW;
+      auto cellv = [&](int f, int q) { return N::val(Sk[f * CT + q]); };
+      R A, B, C, D;
+      // S0: x only
+      A = cellv(0, ia); B = cellv(0, ib); C = cellv(0, ic); D = cellv(0, id);
+      const R px0 = (B + C) - (A + D);
+      A = cellv(1, ia); B = cellv(1, ib); C = cellv(1, ic); D = cellv(1, id);
+      const R py1 = (C + D) - (A + B);
+      A = cellv(2, ia); B = cellv(2, ib); C = cellv(2, ic); D = cellv(2, id);
+      const R s2 = (A + B) + (C + D);
+      A = cellv(3, ia); B = cellv(3, ib); C = cellv(3, ic); D = cellv(3, id);
+      R ab = A + B, cd = C + D;
+      const R py3 = cd - ab, s3 = ab + cd;
+      A = cellv(4, ia); B = cellv(4, ib); C = cellv(4, ic); D = cellv(4, id);
+      R bc = B + C, ad = A + D;
+      const R px4 = bc - ad, s4 = bc + ad;
+      A = cellv(5, ia); B = cellv(5, ib); C = cellv(5, ic); D = cellv(5, id);
+      const R px5 = (B + C) - (A + D), py5 = (C + D) - (A + B);
+      // node derivatives (x: S0,S5,S4  y: S5,S1,S3  z: S4,S3,S2)
+      R ax = gx * (vpx0 + px0) + gy * (vpy5 + py5) + gz * (s4 - vs4);
+      R ay = gx * (vpx5 + px5) + gy * (vpy1 + py1) + gz * (s3 - vs3);
+      R az = gx * (vpx4 + px4) + gy * (vpy3 + py3) + gz * (s2 - vs2);
+      vpx0 = px0; vpx4 = px4; vpx5 = px5; vpy1 = py1; vpy3 = py3; vpy5 = py5;
+      vs2 = s2; vs3 = s3; vs4 = s4;
+      if (a.f_rng) {  // force sources of this block and layer
+        const int2 r = a.f_rng[(int64_t)blk * (nz + 1) + k];
+        for (int e = r.x; e < r.y; e++) {
+          const int key = a.f_key[e];
+          if ((key & 0xffff) != t) continue;
+          const R v = N::val(a.f_w[e]) * N::val(a.sigval[a.f_sig[e]]);
+          const int d = key >> 16;
+          if (d == 0) ax = ax + v;
+          else if (d == 1) ay = ay + v;
+          else az = az + v;
+        }
+      }
+      R vn[3] = {vold[0], vold[1], vold[2]};
+      if (!(cf == R())) {
+        vn[0] = vold[0] + cf * ax;
+        vn[1] = vold[1] + cf * ay;
+        vn[2] = vold[2] + cf * az;
+      }
+#pragma unroll
+      for (int c = 0; c < 3; c++) Vk[c * NT + t] = N::sto(vn[c]);
+      if (node_own) {
+        const int64_t n = (int64_t)k * nplane + nidx0;
+#pragma unroll
+        for (int c = 0; c < 3; c++) N::st(a.V_out[c], n, vn[c]);
+        if (a.s_rng) {  // sensor traces
+          const int2 r = a.s_rng[(int64_t)blk * (nz + 1) + k];
+          for (int e = r.x; e < r.y; e++) {
+            if (a.s_key[e] != t) continue;
+            double *tr = a.traces + ((int64_t)a.rec * a.n_sens + a.s_idx[e]) * 3;
+            tr[0] = N::dbl(vn[0]);
+            tr[1] = N::dbl(vn[1]);
+            tr[2] = N::dbl(vn[2]);
+          }
+        }
+      }
+    }
+    __syncthreads();
+
+    // ---- C: stress of cell layer k-1 (partial sums of node layer k always)
+    if (tx < TX - 1 && ty < TY - 1) {
+      const int ia = t, ib = t + 1, ic = t + TX + 1, id = t + TX;
+      R px[3], py[3], s[3];
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const R A = N::val(Vk[c * NT + ia]), B = N::val(Vk[c * NT + ib]);
+        const R C = N::val(Vk[c * NT + ic]), D = N::val(Vk[c * NT + id]);
+        const R ab = A + B, cd = C + D;
+        px[c] = (B + C) - (A + D);
+        py[c] = cd - ab;
+        s[c] = ab + cd;
+      }
+      if (k >= 1 && cell_own) {
+        // d_ij = d/dx_i V_j over the cell of layer k-1
+        const R d00 = spx[0] + px[0], d10 = spy[0] + py[0], d20 = s[0] - ss[0];
+        const R d01 = spx[1] + px[1], d11 = spy[1] + py[1], d21 = s[1] - ss[1];
+        const R d02 = spx[2] + px[2], d12 = spy[2] + py[2], d22 = s[2] - ss[2];
+        R e[6];
+        e[0] = gx * d00;
+        e[1] = gy * d11;
+        e[2] = gz * d22;
+        e[3] = gy * d12 + gz * d21;
+        e[4] = gx * d02 + gz * d20;
+        e[5] = gx * d01 + gy * d10;
+        const int kc = k - 1;
+        const int64_t cg = (int64_t)kc * cplane + cidx0;
+        const St *Cm = a.ctab + 36 * (int)a.mat[cg];
+        const St *Sprev = sS + (kc + 1) % 3 * 6 * CT;
+        const int q = (ty + 1) * CW + tx + 1;
+        R acc[6];
+#pragma unroll
+        for (int f = 0; f < 6; f++) acc[f] = N::val(Sprev[f * CT + q]);
+        if (a.m_rng) {  // moment sources of this block and cell layer
+          const int2 r = a.m_rng[(int64_t)blk * nz + kc];
+          for (int ee = r.x; ee < r.y; ee++) {
+            const int key = a.m_key[ee];
+            if ((key & 0xffff) != t) continue;
+            const R v = N::val(a.m_w[ee]) * N::val(a.sigval[a.m_sig[ee]]);
+            const int kk = key >> 16;
+#pragma unroll
+            for (int f = 0; f < 6; f++)
+              if (f == kk) acc[f] = acc[f] + v;
+          }
+        }
+#pragma unroll
+        for (int kk = 0; kk < 6; kk++) {
+#pragma unroll
+          for (int jj = 0; jj < 6; jj++)
+            if (c_used(SYM, kk, jj)) acc[kk] = acc[kk] + N::ld(Cm, 6 * kk + jj) * e[jj];
+          N::st(a.S_out[kk], cg, acc[kk]);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        spx[c] = px[c];
+        spy[c] = py[c];
+        ss[c] = s[c];
+      }
+    }
+  }
+}
+
+template <typename R, int TX, int TY, int SYM>
+cudaError_t launch_t(const GridArgs<typename GNum<R>::S> &a, cudaStream_t st) {
+  using St = typename GNum<R>::S;
+  constexpr int CT = (TX + 1) * (TY + 1);
+  const size_t smem = sizeof(St) * (3 * 6 * CT + 2 * 3 * TX * TY);
+  static unsigned long long opted = 0;  // one opt-in per instantiation and device (< 64)
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (!(opted & bit)) {
+    e = cudaFuncSetAttribute(k_grid_step<R, TX, TY, SYM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    if (e != cudaSuccess) return e;
+    opted |= bit;
+  }
+  const dim3 grid((unsigned)(a.nx / (TX - 1) + 1), (unsigned)(a.ny / (TY - 1) + 1));
+  k_grid_step<R, TX, TY, SYM><<<grid, TX * TY, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_sym(const GridArgs<typename GNum<R>::S> &a, int sym, cudaStream_t st) {
+  if (a.nx <= 0 || a.ny <= 0 || a.nz <= 0) return cudaSuccess;
+  if (sym == 2) return launch_t<R, 32, 8, 2>(a, st);
+  if (sym == 1) return launch_t<R, 32, 8, 1>(a, st);
+  return launch_t<R, 32, 8, 0>(a, st);
+}
+
+}  // namespace
+
+int grid_tile_x() { return 32; }
+int grid_tile_y() { return 8; }
+
+cudaError_t launch_grid_f32(const GridArgs<float> &a, int sym, cudaStream_t st) {
+  return launch_sym<float>(a, sym, st);
+}
+cudaError_t launch_grid_f64(const GridArgs<double> &a, int sym, cudaStream_t st) {
+  return launch_sym<double>(a, sym, st);
+}
+cudaError_t launch_grid_df64(const GridArgs<float2> &a, int sym, cudaStream_t st) {
+  return launch_sym<df64>(a, sym, st);
+}
+
+}  // namespace pn

@@ -1,0 +1,52 @@
+// rsg_grid.cuh -- arguments of the fused voxel-grid step kernel (rsg_grid.cu).
+//
+// Layout (x fastest): grid node (i,j,k) at (k*(ny+1)+j)*(nx+1)+i, grid cell
+// (i,j,k) at (k*ny+j)*nx+i.  Block (bx,by) owns node and cell columns
+// i in [bx*(TX-1), bx*(TX-1)+TX-1), j likewise with TY; its local index of the
+// node / cell (i,j) is (i-i0) + TX*(j-j0).  Sparse sources and sensors are
+// sorted by (block, layer, local index) with one [begin,end) range per
+// (block, layer).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pn {
+
+template <typename T>
+struct GridArgs {
+  int32_t nx, ny, nz;  // cells per axis
+  const T *V_in[3];
+  T *V_out[3];
+  const T *S_in[6];
+  T *S_out[6];
+  const T *coef;       // [grid nodes] dt/rho_node; 0 = void or not owned
+  const uint8_t *mat;  // [grid cells] material row; the last row is zero (void)
+  const T *ctab;       // [rows][36] dt*C
+  T g[3];              // 0.25/h per axis
+  // force sources, ranges per (block, node layer): [blocks][nz+1]
+  const int2 *f_rng;
+  const int32_t *f_key;  // local node | direction << 16
+  const int32_t *f_sig;
+  const T *f_w;
+  // moment sources, ranges per (block, cell layer): [blocks][nz]
+  const int2 *m_rng;
+  const int32_t *m_key;  // local cell | Voigt component << 16
+  const int32_t *m_sig;
+  const T *m_w;          // weights carry dt
+  const T *sigval;       // signal values of this step
+  // sensors, ranges per (block, node layer)
+  const int2 *s_rng;
+  const int32_t *s_key;  // local node
+  const int32_t *s_idx;  // sensor number
+  double *traces;        // [records][n_sens][3]
+  int32_t n_sens;
+  int64_t rec;           // record written by this step
+};
+
+int grid_tile_x();
+int grid_tile_y();
+cudaError_t launch_grid_f32(const GridArgs<float> &a, int sym, cudaStream_t st);
+cudaError_t launch_grid_f64(const GridArgs<double> &a, int sym, cudaStream_t st);
+cudaError_t launch_grid_df64(const GridArgs<float2> &a, int sym, cudaStream_t st);
+
+}  // namespace pn

@@ -16,8 +16,12 @@ PRECISIONS = {"f64_exact": N.PN_PREC_F64_EXACT, "f64": N.PN_PREC_F64, "f32": N.P
               "df64": N.PN_PREC_DF64}
 
 
-def _precision(p) -> int:
-    return PRECISIONS[p] if isinstance(p, str) else int(p)
+FORMS = {"auto": N.PN_FORM_AUTO, "table": N.PN_FORM_TABLE, "grid": N.PN_FORM_GRID}
+
+
+def _precision(p, form="auto") -> int:
+    prec = PRECISIONS[p] if isinstance(p, str) else int(p)
+    return prec | (FORMS[form] if isinstance(form, str) else int(form))
 
 
 class Solver:
@@ -27,10 +31,10 @@ class Solver:
     (PnMaterial, keepalive) pair of reference-style fields.
     """
 
-    def __init__(self, mesh: HexMesh, material, dt: float, precision="f64"):
+    def __init__(self, mesh: HexMesh, material, dt: float, precision="f64", form="auto"):
         self._lib = N.load()
         self.mesh = mesh
-        self.precision = _precision(precision)
+        self.precision = _precision(precision, form)
         m, keep = mesh.as_struct()
         h = c_void_p()
         if isinstance(material, Case):
@@ -47,8 +51,8 @@ class Solver:
         del keep, keep_t
 
     @classmethod
-    def from_case(cls, case: Case, precision="f64", sensors=True, capacity=None):
-        s = cls(case.mesh, case, case.dt, precision)
+    def from_case(cls, case: Case, precision="f64", sensors=True, capacity=None, form="auto"):
+        s = cls(case.mesh, case, case.dt, precision, form)
         if case.sources:
             s.add_sources(case.sources)
         if sensors and case.sensors.size:
@@ -130,7 +134,10 @@ class Solver:
     def info(self) -> dict:
         inf = N.PnSolverInfo()
         N.check(self._lib.pn_solver_get_info(self._h, ctypes.byref(inf)))
-        return {k: getattr(inf, k) for k, _ in N.PnSolverInfo._fields_}
+        d = {k: getattr(inf, k) for k, _ in N.PnSolverInfo._fields_}
+        d["grid"] = tuple(d["grid"])
+        d["form_name"] = {N.PN_FORM_GRID: "grid", N.PN_FORM_TABLE: "table"}.get(d["form"], "?")
+        return d
 
     def device_state(self):
         V = (c_void_p * 3)()
@@ -142,11 +149,11 @@ class Solver:
         N.check(self._lib.pn_solver_enable_kernel_timing(self._h, 1 if on else 0))
 
     def kernel_times(self):
-        """{"velocity": (ms_total, launches), "stress": (ms_total, launches)}"""
-        ms = (c_double * 2)()
-        n = (c_int64 * 2)()
+        """{"velocity" | "stress" | "grid_step": (ms_total, launches)} since enabled"""
+        ms = (c_double * 3)()
+        n = (c_int64 * 3)()
         N.check(self._lib.pn_solver_kernel_times(self._h, ms, n))
-        return {"velocity": (ms[0], n[0]), "stress": (ms[1], n[1])}
+        return {"velocity": (ms[0], n[0]), "stress": (ms[1], n[1]), "grid_step": (ms[2], n[2])}
 
     def synchronize(self):
         N.check(self._lib.pn_solver_synchronize(self._h))

@@ -48,14 +48,41 @@ def plan(mesh, material=None, table=None, dt=1e-9, precision=N.PN_PREC_F64):
 
 def test_plan_plate():
     c = cases.al_plate_case(nx=10, ny=8, nz=3)
-    rc, p, _ = plan(c.mesh, table=c.material_table())
-    assert rc == 0
+    table = N.PN_FORM_TABLE
+    rc, p, _ = plan(c.mesh, table=c.material_table(), precision=N.PN_PREC_F64 | table)
+    assert rc == 0 and p.form == table
     assert (p.n_nodes, p.n_cells, p.n_materials, p.uniform_spacing) == (11 * 9 * 4, 240, 1, 1)
     assert abs(p.hx - 1e-4) < 1e-18 and abs(p.hz - 1e-4) < 1e-18
     assert p.algorithmic_bytes_per_step == 240 * 180 + 396 * 112
-    rc32, p32, _ = plan(c.mesh, table=c.material_table(), precision=N.PN_PREC_F32)
+    rc32, p32, _ = plan(c.mesh, table=c.material_table(), precision=N.PN_PREC_F32 | table)
     assert p32.algorithmic_bytes_per_step == 240 * 108 + 396 * 72
     assert p32.device_bytes < p.device_bytes
+
+
+def test_form_selection():
+    """Voxel meshes get the grid form (no connectivity tables: S r/w + 1 material
+    byte per lattice cell, V r/w + dt/rho per lattice node); the exact FP64
+    form and non-lattice meshes get the table form."""
+    c = cases.al_plate_case(nx=10, ny=8, nz=3)
+    rc, p, _ = plan(c.mesh, table=c.material_table(), precision=N.PN_PREC_F64)
+    assert rc == 0 and p.form == N.PN_FORM_GRID and list(p.grid) == [10, 8, 3]
+    assert p.algorithmic_bytes_per_step == 240 * (96 + 1) + 396 * 56
+    rc, p, _ = plan(c.mesh, table=c.material_table(), precision=N.PN_PREC_F32)
+    assert p.algorithmic_bytes_per_step == 240 * (48 + 1) + 396 * 28
+    rc, p, _ = plan(c.mesh, table=c.material_table(), precision=N.PN_PREC_F64_EXACT)
+    assert rc == 0 and p.form == N.PN_FORM_TABLE
+    h = cases.holed_plate_case(nx=120, ny=100, nz=3, n_holes=2)
+    rc, p, _ = plan(h.mesh, table=h.material_table(), precision=N.PN_PREC_DF64)
+    assert rc == 0 and p.form == N.PN_FORM_GRID and p.n_cells < 120 * 100 * 3
+    g = cases.plate_builder(1.0, 1.0, 0.25, 3, 2)
+    g.x = g.x * (1 + 0.1 * g.x)
+    gc = cases.Case("g", g, np.array([1.0]), np.ones((1, 21)), np.zeros(g.n_cells, np.int32), 1.0)
+    rc, p, _ = plan(g, table=gc.material_table(), precision=N.PN_PREC_F64)
+    assert rc == 0 and p.form == N.PN_FORM_TABLE
+    rc, p, msg = plan(g, table=gc.material_table(), precision=N.PN_PREC_F64 | N.PN_FORM_GRID)
+    assert rc == N.PN_ERR_INVALID and "grid form unavailable" in msg
+    rc, p, msg = plan(c.mesh, table=c.material_table(), precision=N.PN_PREC_F64_EXACT | N.PN_FORM_GRID)
+    assert rc == N.PN_ERR_INVALID
 
 
 def test_plan_dedups_field_materials():

@@ -1,0 +1,143 @@
+"""Parity of the grid form (voxel meshes: implicit lattice indices, one fused
+kernel per step, double-buffered state) against the CPU oracle, through the
+C ABI.  Tolerances (relative L2 over every field and every trace): FP64 and
+double-float 1e-10, FP32 1e-4.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from pannde_gb300 import _native as N
+from pannde_gb300 import cases
+from pannde_gb300.solver import Solver
+from tests.test_parity_gpu import compare, random_state, water_column_sources
+
+pytestmark = pytest.mark.gpu
+
+PRECS = ["f64", "df64", "f32"]
+
+
+def run_grid(mesh, material, dt, sources, nsteps, sensors=None, prec="f64", V0=None, S0=None,
+             chunks=None):
+    with Solver(mesh, material, dt, prec, "grid") as s:
+        assert s.info()["form_name"] == "grid"
+        if V0 is not None or S0 is not None:
+            s.set_state(V0, S0)
+        if sources:
+            s.add_sources(sources)
+        if sensors is not None and len(sensors):
+            s.set_sensors(sensors, nsteps)
+        t = 0.0
+        for n in (chunks or [nsteps]):
+            t = s.solve(n)
+        V, S = s.get_state()
+        tr = s.traces() if sensors is not None and len(sensors) else None
+        return (V, S, tr), t
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_grid_transducer_plate(cuda_device, prec):
+    c = cases.al_plate_case(nx=40, ny=19, nz=5, nsteps=60, radius=0.6e-3, n_sensors=9)
+    ref = oracle.run(c.mesh, c.material_fields(), c.dt, c.sources, c.nsteps, c.sensors)
+    dev, t = run_grid(c.mesh, c, c.dt, c.sources, c.nsteps, c.sensors, prec)
+    assert t == ref["time"]
+    compare(prec, dev, ref)
+    assert np.abs(ref["traces"]).max() > 0
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_grid_holes_random_state(cuda_device, prec):
+    """Void lattice sites (holes, a notch) behave as the reference's missing cells."""
+    solid = np.ones((45, 17, 6), dtype=bool)
+    solid[10:14, 5:9, :] = False
+    solid[30:, 0:4, 3:] = False
+    solid[:, 12:, 5] = False
+    m = cases.voxel_mesh(solid, (1e-4, 1.5e-4, 0.8e-4))
+    c = cases.Case("g", m, np.array([2700.0]),
+                   cases.c21_from_6x6(cases.isotropic(70e9, 0.33))[None], np.zeros(m.n_cells, np.int32), 4e-9)
+    V0, S0 = random_state(m, 3)
+    sens = np.array([0, 17, m.n_nodes // 2, m.n_nodes - 1], np.int32)
+    ref = oracle.run(m, c.material_fields(), c.dt, [], 30, sens, V0=V0, S0=S0)
+    dev, _ = run_grid(m, c, c.dt, [], 30, sens, prec, V0=V0, S0=S0)
+    compare(prec, dev, ref)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_grid_laminate_moments_and_forces(cuda_device, prec):
+    c = cases.laminate_case(nx=33, ny=29, nz=8, nsteps=40, radius=0.5e-3, n_sensors=6)
+    h = c.meta["h"]
+    t, v = c.sources[0].times, c.sources[0].values
+    src = list(c.sources)
+    src += water_column_sources((0.6e-3, 0.5e-3, 0.4e-3), 0.3e-3, h, t, v)
+    src.append(cases.WindowSource(N.PN_SOURCE_FORCE, 1, 0, (1.1e-3, 0.9e-3, 0.4e-3), 0.3e-3, h, t, -v))
+    V0, S0 = random_state(c.mesh, 9)
+    ref = oracle.run(c.mesh, c.material_fields(), c.dt, src, c.nsteps, c.sensors, V0=V0, S0=S0)
+    dev, _ = run_grid(c.mesh, c, c.dt, src, c.nsteps, c.sensors, prec, V0=V0, S0=S0)
+    compare(prec, dev, ref)
+
+
+def test_grid_general_anisotropy(cuda_device):
+    """A stiffness with every entry non-zero takes the general (36-entry) path."""
+    m = cases.voxel_mesh(np.ones((20, 11, 4), dtype=bool), 1e-4)
+    rng = np.random.default_rng(4)
+    a = rng.uniform(-1, 1, (6, 6))
+    c6 = cases.isotropic(70e9, 0.3) + 5e9 * (a + a.T)
+    c = cases.Case("g", m, np.array([2000.0]), cases.c21_from_6x6(c6)[None],
+                   np.zeros(m.n_cells, np.int32), 1e-9)
+    V0, S0 = random_state(m, 5)
+    ref = oracle.run(m, c.material_fields(), c.dt, [], 12, None, V0=V0, S0=S0)
+    for prec in PRECS:
+        dev, _ = run_grid(m, c, c.dt, [], 12, None, prec, V0=V0, S0=S0)
+        compare(prec, dev, ref)
+
+
+def test_grid_partition_ownership(cuda_device):
+    c = cases.al_plate_case(nx=35, ny=10, nz=3, nsteps=10, radius=0.3e-3, n_sensors=4)
+    m = c.mesh
+    m.node_owner = (m.node_ijk[:, 0] >= 20).astype(np.int32)
+    V0, S0 = random_state(m, 5)
+    sens = np.array([0, m.n_nodes - 1], np.int32)  # one owned, one not
+    ref = oracle.run(m, c.material_fields(), c.dt, c.sources, 10, sens, V0=V0, S0=S0)
+    dev, _ = run_grid(m, c, c.dt, c.sources, 10, sens, "f64", V0=V0, S0=S0)
+    compare("f64", dev, ref)
+    off = m.node_owner == 1
+    assert np.array_equal(dev[0][0][off], V0[0][off])
+    m.node_owner = None
+
+
+def test_grid_chunked_solve_is_deterministic(cuda_device):
+    c = cases.al_plate_case(nx=40, ny=19, nz=5, nsteps=40, radius=0.6e-3, n_sensors=9)
+    a, ta = run_grid(c.mesh, c, c.dt, c.sources, 40, c.sensors, "df64")
+    b, tb = run_grid(c.mesh, c, c.dt, c.sources, 40, c.sensors, "df64", chunks=[1] * 5 + [3, 32])
+    assert ta == tb
+    for k in range(3):
+        assert np.array_equal(a[0][k], b[0][k])
+    for k in range(6):
+        assert np.array_equal(a[1][k], b[1][k])
+    assert np.array_equal(a[2], b[2])
+
+
+@pytest.mark.parametrize("dims", [(1, 1, 1), (31, 7, 2), (32, 8, 3), (62, 14, 1), (5, 40, 3)])
+def test_grid_tile_edges(cuda_device, dims):
+    """Lattices at, below and above the 31 x 7 owned-cell tile sizes."""
+    m = cases.voxel_mesh(np.ones(dims, dtype=bool), 1e-4)
+    c = cases.Case("g", m, np.array([2700.0]),
+                   cases.c21_from_6x6(cases.isotropic(70e9, 0.33))[None], np.zeros(m.n_cells, np.int32), 5e-9)
+    V0, S0 = random_state(m, 1)
+    ref = oracle.run(m, c.material_fields(), c.dt, [], 7, None, V0=V0, S0=S0)
+    dev, _ = run_grid(m, c, c.dt, [], 7, None, "f64", V0=V0, S0=S0)
+    compare("f64", dev, ref)
+
+
+def test_grid_and_table_forms_agree(cuda_device):
+    c = cases.laminate_case(nx=24, ny=20, nz=8, nsteps=30, radius=0.4e-3, n_sensors=5)
+    out = {}
+    for form in ("grid", "table"):
+        with Solver.from_case(c, precision="f64", form=form) as s:
+            s.solve(c.nsteps)
+            out[form] = (s.get_state(), s.traces())
+    (Vg, Sg), tg = out["grid"]
+    (Vt, St), tt = out["table"]
+    for k in range(3):
+        np.testing.assert_allclose(Vg[k], Vt[k], rtol=0, atol=1e-12 * np.abs(Vt[k]).max())
+    np.testing.assert_allclose(tg, tt, rtol=0, atol=1e-12 * np.abs(tt).max())

@@ -1,4 +1,6 @@
-"""Parity of the CUDA RSG leapfrog against the CPU oracle (through the C ABI).
+"""Parity of the CUDA RSG leapfrog against the CPU oracle (through the C ABI),
+table form (connectivity tables, any hex mesh).  tests/test_grid_gpu.py covers
+the grid form.
 
 Tolerances (relative L2 over every field and every trace):
   f64_exact  bit-identical (np.array_equal)
@@ -46,8 +48,8 @@ def compare(prec, dev, ref):
 
 
 def run_dev(mesh, material, dt, sources, nsteps, sensors=None, prec="f64", V0=None, S0=None,
-            chunks=None):
-    with Solver(mesh, material, dt, prec) as s:
+            chunks=None, form="table"):
+    with Solver(mesh, material, dt, prec, form) as s:
         if V0 is not None or S0 is not None:
             s.set_state(V0, S0)
         if sources:
