@@ -56,6 +56,8 @@ def parse():
     p.add_argument("--nz", type=int, default=None)
     p.add_argument("--precisions", default="f64,f32",
                    help="forms to time; the first is the headline value")
+    p.add_argument("--form", default="auto", choices=["auto", "table", "grid"],
+                   help="device form: voxel-grid kernels or connectivity tables")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fp32", action="store_true")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
@@ -87,15 +89,19 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic(case, prec):
-    """DRAM bytes per launch from the committed ncu summary (profiles/*.txt)."""
+def profile_traffic(case, form, prec):
+    """DRAM bytes per launch from the committed ncu summaries (profiles/*.txt),
+    lines 'traffic <case>.<form>.<precision>.<kernel> = <bytes>'."""
     out = {}
+    prefix = f"{case}.{form}.{prec}."
     for f in sorted((ROOT / "profiles").glob("*.txt")):
         for line in f.read_text().splitlines():
             if line.startswith("traffic ") and "=" in line:
                 key, val = line[len("traffic "):].split("=", 1)
-                out[key.strip()] = float(val.split()[0])
-    return out.get(f"{case}.{prec}.velocity"), out.get(f"{case}.{prec}.stress")
+                key = key.strip()
+                if key.startswith(prefix):
+                    out[key[len(prefix):]] = float(val.split()[0])
+    return out
 
 
 class Clocks:
@@ -160,10 +166,13 @@ def dist_setup():
     return ws, rank, local
 
 
+FORM = "auto"
+
+
 def time_device(case, prec, steps, warmup, torch, dist):
     """Device throughput of the hot path with inputs resident in HBM."""
     from pannde_gb300.solver import Solver
-    s = Solver.from_case(case, precision=prec, capacity=warmup + steps)
+    s = Solver.from_case(case, precision=prec, capacity=warmup + steps, form=FORM)
     stream = torch.cuda.Stream()
     s.set_stream(stream)
     s.solve(warmup)
@@ -190,27 +199,37 @@ def time_device(case, prec, steps, warmup, torch, dist):
 
 
 def roofline(case, info, kt, prec, peak, peak_kind):
+    """HBM roofline of the dominant kernel from its CUDA-event average.
+
+    Algorithmic bytes per launch:
+      table form  velocity: S read (6e/cell), V read+write, dt/rho, node slots (7e+32 /node)
+                  stress:   S read+write, material id, corner table (12e+36 /cell), V read (3e /node)
+      grid form   fused step: S read+write + material byte (12e+1 /lattice cell),
+                  V read+write + dt/rho (7e /lattice node) -- pn_solver_info
+    with e the bytes per value (4 FP32, 8 FP64 and double-float)."""
     e = 4 if prec == "f32" else 8
     nc, nn = info["n_cells"], info["n_nodes"]
-    alg = {"velocity": nc * 6 * e + nn * (7 * e + 32),     # S read, V r/w, dt/rho, node slots
-           "stress": nc * (12 * e + 36) + nn * 3 * e}      # S r/w, mat id, corners, V read
-    avg = {k: kt[k][0] / max(kt[k][1], 1) for k in kt}
+    avg = {k: kt[k][0] / max(kt[k][1], 1) for k in kt if kt[k][1] > 0}
+    if info.get("form_name") == "grid":
+        alg = {"grid_step": info["algorithmic_bytes_per_step"]}
+    else:
+        alg = {"velocity": nc * 6 * e + nn * (7 * e + 32),
+               "stress": nc * (12 * e + 36) + nn * 3 * e}
     dom = max(avg, key=lambda k: avg[k])
     achieved = alg[dom] / (avg[dom] * 1e-3) / 1e9
-    tv, ts = profile_traffic(case, prec)
-    traffic = {"velocity": tv, "stress": ts}[dom]
-    return {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
-            "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+    traffic = profile_traffic(case, info.get("form_name", "table"), prec).get(dom)
+    step_ms = sum(avg.values())
+    return {"bound": "hbm", "kernel": dom, "form": info.get("form_name"), "achieved": round(achieved, 1),
+            "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
             "traffic": traffic, "algorithmic_bytes": alg[dom],
             "avg_ms": {k: round(v, 4) for k, v in avg.items()},
-            "step_bytes_frac": round((alg["velocity"] + alg["stress"]) /
-                                     ((avg["velocity"] + avg["stress"]) * 1e-3) / 1e9 / peak, 4)}
+            "step_bytes_frac": round(sum(alg.values()) / (step_ms * 1e-3) / 1e9 / peak, 4)}
 
 
 def e2e_run(case, prec, steps, torch):
     """Through the C ABI with host buffers (pinned), copies inside the timed region."""
     from pannde_gb300.solver import Solver
-    s = Solver.from_case(case, precision=prec, capacity=steps)
+    s = Solver.from_case(case, precision=prec, capacity=steps, form=FORM)
     nn, nc = case.mesh.n_nodes, case.mesh.n_cells
 
     def pinned(n):
@@ -269,6 +288,8 @@ def cpu_reference(case, budget_s):
 
 def main():
     args = parse()
+    global FORM
+    FORM = args.form
     ws, rank, local = dist_setup()
     assert args.warmup >= 3 or args.impl == "reference", "at least 3 warm-up steps"
     case, desc = make_case(args.case, args.nx, args.ny, args.nz)
@@ -321,7 +342,7 @@ def main():
                        "l2": "no flush: each step moves far more than the 129 MB L2",
                        "parallelism": f"{ws} independent replica(s), one per GPU"},
             "roofline": roofline(args.case, info, kt, head, peak, peak_kind),
-            "gpu_launches": int(kt["velocity"][1] + kt["stress"][1]),
+            "gpu_launches": int(sum(v[1] for v in kt.values())),
             "clocks": clocks}
     forms = {}
     for prec in precs[1:]:

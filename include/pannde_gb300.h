@@ -169,6 +169,19 @@ typedef struct pn_window_source {
   pn_signal signal;
 } pn_window_source;
 
+/* A windowed source given by its window instead of its geometry, for callers
+   that hold the reference's own PanNDE::MultiVariate objects: inside[] is the
+   caller's MultiVariate::checkAt (MultiVariate.hpp:118-141) evaluated at every
+   cell centre (PN_SOURCE_FORCE; centres as HostRSGTDUT::cellcenter,
+   HostRSGTDUT.hpp:419-428) or at every node (PN_SOURCE_MOMENT).  Its signal
+   values come per step from pn_solver_solve_signals. */
+typedef struct pn_window_mask {
+  int32_t kind;            /* enum pn_source_kind */
+  int32_t group;
+  int32_t component;
+  const uint8_t *inside;   /* [n_cells] (force) or [n_nodes] (moment), 0 or 1 */
+} pn_window_mask;
+
 /* Read-only facts about a created solver. */
 typedef struct pn_solver_info {
   int32_t n_nodes, n_cells;
@@ -260,6 +273,13 @@ int pn_solver_set_state(pn_solver *s, const double *const *V, const double *cons
    and applyMomentExcitation (HostUTModel.hpp:152-170). */
 int pn_solver_add_sources(pn_solver *s, const pn_window_source *src, int32_t n);
 
+/* Add sources given by window masks (pn_window_mask).  They take part in
+   every later solve like pn_solver_add_sources' sources, in addition order;
+   their signal values must come from pn_solver_solve_signals.  Replaces the
+   same constructor / apply calls as pn_solver_add_sources for arbitrary
+   separable MultiVariate sources (evalAt(p,t) = checkAt(p) * signal(t)). */
+int pn_solver_add_window_masks(pn_solver *s, const pn_window_mask *masks, int32_t n);
+
 /* Record V at these nodes after every step (traces [step][sensor][3]).
    The reference records the transducer-node velocities at write times
    (TransducerModel.cpp:143-149); this records every step, fused into the
@@ -272,6 +292,14 @@ int pn_solver_set_sensors(pn_solver *s, const int32_t *nodes, int32_t n,
    the new time, accumulated on the host in FP64 exactly as the reference.
    Replaces Model::solve (Model.hpp:77-106; HostRSGTDUT.hpp:162-169). */
 int pn_solver_solve(pn_solver *s, int32_t nsteps, double *time_out);
+
+/* pn_solver_solve with the signal values of every source given by the caller
+   for each step: values[k * n_sources + i] is source i's signal at the time
+   of step k of this call (sources numbered in addition order, geometry
+   sources and mask sources alike).  This is how a caller reproduces the
+   reference's per-step MultiVariate::evalAt (HostRSGTDUT.hpp:387-402) with
+   its own objects. */
+int pn_solver_solve_signals(pn_solver *s, int32_t nsteps, const double *values, double *time_out);
 
 /* Synchronise and download the state into caller-owned host arrays (same
    layout as pn_solver_set_state; NULL pointers are skipped).  Replaces the

@@ -77,6 +77,11 @@ class PnWindowSource(ctypes.Structure):
                 ("signal", PnSignal)]
 
 
+class PnWindowMask(ctypes.Structure):
+    _fields_ = [("kind", c_int32), ("group", c_int32), ("component", c_int32),
+                ("inside", POINTER(ctypes.c_uint8))]
+
+
 class PnSolverInfo(ctypes.Structure):
     _fields_ = [("n_nodes", c_int32), ("n_cells", c_int32), ("precision", c_int32),
                 ("n_materials", c_int32), ("uniform_spacing", c_int32),
@@ -108,8 +113,10 @@ SIGNATURES = {
     "pn_solver_set_stream": (c_int, [c_void_p, c_void_p]),
     "pn_solver_set_state": (c_int, [c_void_p, POINTER(P_double), POINTER(P_double)]),
     "pn_solver_add_sources": (c_int, [c_void_p, POINTER(PnWindowSource), c_int32]),
+    "pn_solver_add_window_masks": (c_int, [c_void_p, POINTER(PnWindowMask), c_int32]),
     "pn_solver_set_sensors": (c_int, [c_void_p, P_int32, c_int32, c_int32]),
     "pn_solver_solve": (c_int, [c_void_p, c_int32, P_double]),
+    "pn_solver_solve_signals": (c_int, [c_void_p, c_int32, P_double, P_double]),
     "pn_solver_get_state": (c_int, [c_void_p, POINTER(P_double), POINTER(P_double)]),
     "pn_solver_get_traces": (c_int, [c_void_p, P_double, c_int64, POINTER(c_int64)]),
     "pn_solver_clear_traces": (c_int, [c_void_p]),

@@ -17,7 +17,7 @@ namespace pn {
 
 void ensure_signal_rows(pn_solver *s, int64_t nsteps) {
   const int64_t nsig = (int64_t)s->src.size();
-  if (nsig == 0) return;
+  if (nsig == 0 || s->caller_signals) return;  // caller rows cover the whole call
   const int64_t first = s->step, last = s->step + nsteps - 1;
   if (s->sig_valid && first >= s->sig_step0 && (s->sig_hold || last < s->sig_step0 + s->sig_rows))
     return;
@@ -302,9 +302,46 @@ int pn_solver_add_sources(pn_solver *s, const pn_window_source *src, int32_t n) 
     s->src_t.swap(ts);
     s->src_v.swap(vs);
     s->series.swap(ser);
+    s->src_mask.resize(s->src.size());  // geometry sources carry no mask
     bool mom = false;
     for (auto &w : s->src) mom = mom || (w.kind == PN_SOURCE_MOMENT);
     s->has_moments = mom;
+    s->src_dirty = true;
+    s->sig_valid = false;
+    return PN_OK;
+  });
+}
+
+int pn_solver_add_window_masks(pn_solver *s, const pn_window_mask *masks, int32_t n) {
+  return guarded([&]() -> int {
+    if (!s) return set_err(PN_ERR_INVALID, "null solver");
+    if (n < 0 || (n > 0 && !masks)) return set_err(PN_ERR_INVALID, "mask list");
+    std::vector<pn_window_source> all(s->src);
+    for (int32_t i = 0; i < n; i++) {
+      if (!masks[i].inside) return set_err(PN_ERR_INVALID, "null window mask");
+      pn_window_source w;
+      std::memset(&w, 0, sizeof(w));
+      w.kind = masks[i].kind;
+      w.group = masks[i].group;
+      w.component = masks[i].component;
+      all.push_back(w);
+    }
+    {  // validate kinds, groups and slots with the existing sources
+      std::vector<pn::SourceEntry> fe, me;
+      pn::MeshTables empty;
+      pn::build_source_entries(empty, all, true, fe, me);
+    }
+    for (int32_t i = 0; i < n; i++) {
+      const size_t len = masks[i].kind == PN_SOURCE_FORCE ? (size_t)s->mesh.n_cells : (size_t)s->mesh.n_nodes;
+      std::vector<uint8_t> m(masks[i].inside, masks[i].inside + len);
+      if (len == 0) m.push_back(0);  // keep the entry non-empty: marks a mask source
+      s->src.push_back(all[s->src.size()]);
+      s->src_t.emplace_back();
+      s->src_v.emplace_back();
+      s->series.emplace_back();
+      s->src_mask.push_back(std::move(m));
+      s->has_moments = s->has_moments || masks[i].kind == PN_SOURCE_MOMENT;
+    }
     s->src_dirty = true;
     s->sig_valid = false;
     return PN_OK;
@@ -337,18 +374,67 @@ int pn_solver_set_sensors(pn_solver *s, const int32_t *nodes, int32_t n, int32_t
   });
 }
 
+namespace {
+void refresh_sources(pn_solver *s) {
+  if (!s->src_dirty) return;
+  if (s->form == PN_FORM_GRID) pn::grid_sources(s);
+  else pn::table_sources(s);
+  s->src_dirty = false;
+  s->sig_valid = false;
+}
+
+void run_any(pn_solver *s, int32_t nsteps) {
+  if (s->form == PN_FORM_GRID) pn::grid_run(s, nsteps);
+  else pn::table_run(s, nsteps);
+}
+}  // namespace
+
 int pn_solver_solve(pn_solver *s, int32_t nsteps, double *time_out) {
   return guarded([&]() -> int {
     if (!s) return set_err(PN_ERR_INVALID, "null solver");
     if (nsteps < 0) return set_err(PN_ERR_INVALID, "negative step count");
-    if (s->src_dirty) {
-      if (s->form == PN_FORM_GRID) pn::grid_sources(s);
-      else pn::table_sources(s);
-      s->src_dirty = false;
-      s->sig_valid = false;
+    if (s->has_mask_sources())
+      return set_err(PN_ERR_INVALID, "window-mask sources need pn_solver_solve_signals");
+    refresh_sources(s);
+    run_any(s, nsteps);
+    if (time_out) *time_out = s->time;
+    return PN_OK;
+  });
+}
+
+int pn_solver_solve_signals(pn_solver *s, int32_t nsteps, const double *values, double *time_out) {
+  return guarded([&]() -> int {
+    if (!s) return set_err(PN_ERR_INVALID, "null solver");
+    if (nsteps < 0) return set_err(PN_ERR_INVALID, "negative step count");
+    const int64_t nsig = (int64_t)s->src.size();
+    if (nsig > 0 && nsteps > 0 && !values) return set_err(PN_ERR_INVALID, "null signal values");
+    if (nsig > 0 && !pn::all_finite(values, (int64_t)nsteps * nsig))
+      return set_err(PN_ERR_NOT_FINITE, "non-finite signal value");
+    refresh_sources(s);
+    if (nsig > 0 && nsteps > 0) {
+      pn::ck(cudaStreamSynchronize(s->stream), "signal sync");
+      if (nsteps > s->sig_alloc_rows) {
+        s->release(s->d_sig);
+        s->d_sig = s->alloc<void>((size_t)nsteps * nsig * s->esz);
+        s->sig_alloc_rows = nsteps;
+      }
+      s->upload_real(s->d_sig, values, (size_t)nsteps * nsig);
+      pn::ck(cudaStreamSynchronize(s->stream), "signal upload");
+      s->sig_step0 = s->step;
+      s->sig_rows = nsteps;
+      s->sig_hold = false;
+      s->sig_valid = true;
     }
-    if (s->form == PN_FORM_GRID) pn::grid_run(s, nsteps);
-    else pn::table_run(s, nsteps);
+    s->caller_signals = true;
+    try {
+      run_any(s, nsteps);
+    } catch (...) {
+      s->caller_signals = false;
+      s->sig_valid = false;
+      throw;
+    }
+    s->caller_signals = false;
+    s->sig_valid = false;  // the next plain solve evaluates the sources' own signals
     if (time_out) *time_out = s->time;
     return PN_OK;
   });

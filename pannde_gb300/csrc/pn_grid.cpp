@@ -23,6 +23,24 @@ struct Tiles {
     t = (int32_t)((i - bx * (tx - 1)) + tx * (j - by * (ty - 1)));
   }
   int64_t blocks() const { return (int64_t)bx_count * by_count; }
+  // blocks whose node tile [b*(t-1), b*(t-1)+t) holds column (i, j), with the
+  // local index there: the owner and, on a tile seam, the neighbour whose
+  // apron the column is
+  template <typename F>
+  void each_block_computing(int64_t i, int64_t j, F &&f) const {
+    int64_t bxs[2], bys[2];
+    int nbx = 0, nby = 0;
+    bxs[nbx++] = i / (tx - 1);
+    if (i % (tx - 1) == 0 && i > 0) bxs[nbx++] = i / (tx - 1) - 1;
+    bys[nby++] = j / (ty - 1);
+    if (j % (ty - 1) == 0 && j > 0) bys[nby++] = j / (ty - 1) - 1;
+    for (int a = 0; a < nbx; a++)
+      for (int b = 0; b < nby; b++) {
+        const int64_t bx = bxs[a], by = bys[b];
+        if (bx >= bx_count || by >= by_count) continue;
+        f((int32_t)(by * bx_count + bx), (int32_t)((i - bx * (tx - 1)) + tx * (j - by * (ty - 1))));
+      }
+  }
 };
 
 Tiles tiles_of(const GridMap &g) {
@@ -172,7 +190,8 @@ void grid_get_state(pn_solver *s, double *const *V, double *const *S) {
 
 void grid_sources(pn_solver *s) {
   std::vector<SourceEntry> fe, me;
-  build_source_entries(s->mesh, s->src, false, fe, me);
+  const std::vector<const uint8_t *> masks = s->mask_ptrs();
+  build_source_entries(s->mesh, s->src, false, fe, me, &masks);
   ck(cudaStreamSynchronize(s->stream), "sources sync");
   s->release(s->d_frng); s->release(s->d_fkey); s->release(s->d_fsig); s->release(s->d_fw);
   s->release(s->d_mrng); s->release(s->d_mkey); s->release(s->d_msig); s->release(s->d_mw);
@@ -206,9 +225,12 @@ void grid_sources(pn_solver *s) {
   for (size_t q = 0; q < fe.size(); q++) {
     int64_t i, j, k;
     node_ijk(g, g.node_grid[fe[q].elem], i, j, k);
-    int32_t blk, t;
-    T.locate(i, j, blk, t);
-    F.push_back(Keyed{(int64_t)blk * (g.nz + 1) + k, t | (fe[q].comp << 16), fe[q].sig, 0, fe[q].w});
+    // every block that computes this node's velocity gets the entry: the
+    // owner, and the -x / -y neighbours whose apron column / row it is (they
+    // need it for the stress of their own cells)
+    T.each_block_computing(i, j, [&](int32_t blk, int32_t t) {
+      F.push_back(Keyed{(int64_t)blk * (g.nz + 1) + k, t | (fe[q].comp << 16), fe[q].sig, 0, fe[q].w});
+    });
     if (q == 0 || fe[q].elem != fe[q - 1].elem) s->n_src_nodes++;
   }
   for (size_t q = 0; q < me.size(); q++) {

@@ -279,11 +279,15 @@ void push_entry(std::vector<SourceEntry> &out, bool exact, int32_t elem, int32_t
 }  // namespace
 
 void build_source_entries(const MeshTables &t, const std::vector<pn_window_source> &src, bool exact,
-                          std::vector<SourceEntry> &force, std::vector<SourceEntry> &moment) {
+                          std::vector<SourceEntry> &force, std::vector<SourceEntry> &moment,
+                          const std::vector<const uint8_t *> *masks) {
   force.clear();
   moment.clear();
-  for (auto &s : src) {
+  auto mask_of = [&](size_t i) -> const uint8_t * { return masks ? (*masks)[i] : nullptr; };
+  for (size_t i = 0; i < src.size(); i++) {
+    const pn_window_source &s = src[i];
     if (s.kind != PN_SOURCE_FORCE && s.kind != PN_SOURCE_MOMENT) fail(PN_ERR_INVALID, "unknown source kind");
+    if (mask_of(i)) continue;
     const double g[5] = {s.center[0], s.center[1], s.center[2], s.radius, s.ds};
     if (!all_finite(g, 5)) fail(PN_ERR_NOT_FINITE, "non-finite source geometry");
   }
@@ -307,17 +311,24 @@ void build_source_entries(const MeshTables &t, const std::vector<pn_window_sourc
       cc[(size_t)c * 3 + 2] = p[2];
     }
     // in-window flag per (cell, force source) -- evaluated once per cell
-    std::vector<int32_t> fsrc;
+    std::vector<int32_t> fsrc, flocal(src.size(), -1);
     for (size_t i = 0; i < src.size(); i++)
-      if (src[i].kind == PN_SOURCE_FORCE) fsrc.push_back((int32_t)i);
-    std::vector<uint8_t> hit((size_t)t.n_cells * src.size(), 0);
+      if (src[i].kind == PN_SOURCE_FORCE) {
+        flocal[i] = (int32_t)fsrc.size();
+        fsrc.push_back((int32_t)i);
+      }
+    const size_t nf = fsrc.size();
+    std::vector<uint8_t> hit((size_t)t.n_cells * nf, 0);
     std::vector<uint8_t> any_cell(t.n_cells, 0);
     for (int32_t c = 0; c < t.n_cells; c++)
-      for (int32_t i : fsrc)
-        if (window_at(src[i], &cc[(size_t)c * 3])) {
-          hit[(size_t)c * src.size() + i] = 1;
+      for (size_t l = 0; l < nf; l++) {
+        const int32_t i = fsrc[l];
+        const uint8_t *mk = mask_of(i);
+        if (mk ? mk[c] != 0 : window_at(src[i], &cc[(size_t)c * 3])) {
+          hit[(size_t)c * nf + l] = 1;
           any_cell[c] = 1;
         }
+      }
     // evalXds loop order per node: dir, then slot kb, then transducer g
     for (int32_t n = 0; n < t.n_nodes; n++) {
       if (!t.owned[n]) continue;
@@ -333,24 +344,31 @@ void build_source_entries(const MeshTables &t, const std::vector<pn_window_sourc
           if (c == -1 || !any_cell[c]) continue;
           for (int32_t gi = 0; gi < ngf; gi++) {
             const int32_t si = fslot[(size_t)gi * 3 + dir];
-            if (si >= 0 && hit[(size_t)c * src.size() + si]) push_entry(force, exact, n, dir, si);
+            if (si >= 0 && hit[(size_t)c * nf + flocal[si]]) push_entry(force, exact, n, dir, si);
           }
         }
     }
   }
   if (ngm > 0) {
-    std::vector<int32_t> msrc;
+    std::vector<int32_t> msrc, mlocal(src.size(), -1);
     for (size_t i = 0; i < src.size(); i++)
-      if (src[i].kind == PN_SOURCE_MOMENT) msrc.push_back((int32_t)i);
-    std::vector<uint8_t> hit((size_t)t.n_nodes * src.size(), 0);
+      if (src[i].kind == PN_SOURCE_MOMENT) {
+        mlocal[i] = (int32_t)msrc.size();
+        msrc.push_back((int32_t)i);
+      }
+    const size_t nm = msrc.size();
+    std::vector<uint8_t> hit((size_t)t.n_nodes * nm, 0);
     std::vector<uint8_t> any_node(t.n_nodes, 0);
     for (int32_t n = 0; n < t.n_nodes; n++) {
       const double r[3] = {t.x[n], t.y[n], t.z[n]};
-      for (int32_t i : msrc)
-        if (window_at(src[i], r)) {
-          hit[(size_t)n * src.size() + i] = 1;
+      for (size_t l = 0; l < nm; l++) {
+        const int32_t i = msrc[l];
+        const uint8_t *mk = mask_of(i);
+        if (mk ? mk[n] != 0 : window_at(src[i], r)) {
+          hit[(size_t)n * nm + l] = 1;
           any_node[n] = 1;
         }
+      }
     }
     // evalMoments loop order per cell: component, then corner kb, then tensor g
     for (int32_t c = 0; c < t.n_cells; c++) {
@@ -363,7 +381,7 @@ void build_source_entries(const MeshTables &t, const std::vector<pn_window_sourc
           if (!any_node[q]) continue;
           for (int32_t gi = 0; gi < ngm; gi++) {
             const int32_t si = mslot[(size_t)gi * 6 + comp];
-            if (si >= 0 && hit[(size_t)q * src.size() + si]) push_entry(moment, exact, c, comp, si);
+            if (si >= 0 && hit[(size_t)q * nm + mlocal[si]]) push_entry(moment, exact, c, comp, si);
           }
         }
     }

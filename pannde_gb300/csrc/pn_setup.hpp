@@ -83,9 +83,13 @@ struct SourceEntry {
 // cell, per Voigt component).  exact=true keeps one 0.125-weight entry per
 // in-window (element, source) pair in reference order; exact=false merges
 // equal (element, component, source) entries into one weight.
+// masks (optional, parallel to src): a non-null entry replaces source i's
+// geometric window by the caller's per-cell (force) or per-node (moment)
+// in-window flags (pn_window_mask).
 void build_source_entries(const MeshTables &t, const std::vector<pn_window_source> &src,
                           bool exact, std::vector<SourceEntry> &force,
-                          std::vector<SourceEntry> &moment);
+                          std::vector<SourceEntry> &moment,
+                          const std::vector<const uint8_t *> *masks = nullptr);
 
 // Voxel-grid view of a mesh: every node on the lattice x0 + i*hx (etc.),
 // every cell the axis-aligned box (i..i+1, j..j+1, k..k+1) with its corners

@@ -88,7 +88,20 @@ struct pn_solver {
   std::vector<pn_window_source> src;
   std::vector<std::vector<double>> src_t, src_v;  // owned copies of signal arrays
   std::vector<pn::Series> series;
+  std::vector<std::vector<uint8_t>> src_mask;  // non-empty: window given by a caller's mask
   bool src_dirty = false;
+  bool caller_signals = false;  // inside pn_solver_solve_signals
+
+  bool has_mask_sources() const {
+    for (auto &m : src_mask)
+      if (!m.empty()) return true;
+    return false;
+  }
+  std::vector<const uint8_t *> mask_ptrs() const {
+    std::vector<const uint8_t *> p;
+    for (auto &m : src_mask) p.push_back(m.empty() ? nullptr : m.data());
+    return p;
+  }
   bool has_moments = false;
   int32_t n_force = 0, n_moment = 0, n_src_nodes = 0, n_src_cells = 0;
   // table-form lists: per-tile ranges, element, code, weight

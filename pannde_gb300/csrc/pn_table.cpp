@@ -77,7 +77,8 @@ void table_get_state(pn_solver *s, double *const *V, double *const *S) {
 void table_sources(pn_solver *s) {
   const bool exact = s->precision == PN_PREC_F64_EXACT;
   std::vector<SourceEntry> fe, me;
-  build_source_entries(s->mesh, s->src, exact, fe, me);
+  const std::vector<const uint8_t *> masks = s->mask_ptrs();
+  build_source_entries(s->mesh, s->src, exact, fe, me, &masks);
   ck(cudaStreamSynchronize(s->stream), "sources sync");
   s->release(s->d_ftile); s->release(s->d_felem); s->release(s->d_fcode); s->release(s->d_fw);
   s->release(s->d_mtile); s->release(s->d_melem); s->release(s->d_mcode); s->release(s->d_mw);

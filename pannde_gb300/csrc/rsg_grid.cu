@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(TX *TY) k_grid_step(const GridArgs<typename GN
 #pragma unroll
     for (int p = 0; p < PF; p++) {
       const bool ok = pf_ok[p] && kc < nz;
-      const int64_t g = (int64_t)kc * cplane + pf_off[p];
+      const int64_t g = ok ? (int64_t)kc * cplane + pf_off[p] : 0;  // in bounds either way
 #pragma unroll
       for (int f = 0; f < 6; f++) pf[p][f] = ok ? N::ld(a.S_in[f], g) : R();
     }

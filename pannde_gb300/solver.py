@@ -93,6 +93,28 @@ class Solver:
         N.check(self._lib.pn_solver_add_sources(self._h, arr, len(sources)))
         del keep
 
+    def add_window_masks(self, masks):
+        """masks: list of (kind, group, component, inside[uint8]) -- inside over
+        cells (force) or nodes (moment), the caller's own window predicate."""
+        arr = (N.PnWindowMask * max(len(masks), 1))()
+        keep = []
+        for i, (kind, group, comp, inside) in enumerate(masks):
+            a = np.ascontiguousarray(inside, dtype=np.uint8)
+            keep.append(a)
+            arr[i] = N.PnWindowMask(int(kind), int(group), int(comp),
+                                    a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+        N.check(self._lib.pn_solver_add_window_masks(self._h, arr, len(masks)))
+        del keep
+
+    def solve_signals(self, values) -> float:
+        """Advance len(values) steps with the signal of every source given per
+        step: values[k][i] for source i (addition order) at step k."""
+        v = N.f64(values)
+        nsteps = int(v.shape[0]) if v.ndim else 0
+        t = c_double(0.0)
+        N.check(self._lib.pn_solver_solve_signals(self._h, nsteps, N.dptr(v.reshape(-1)), ctypes.byref(t)))
+        return t.value
+
     def set_sensors(self, nodes, capacity_steps):
         nd = N.i32(nodes)
         N.check(self._lib.pn_solver_set_sensors(self._h, N.iptr(nd), int(nd.shape[0]),

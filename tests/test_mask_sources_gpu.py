@@ -1,0 +1,67 @@
+"""Sources given by the caller's own window predicate and per-step signal
+values (pn_solver_add_window_masks + pn_solver_solve_signals, the path the C++
+adapter uses for the reference's MultiVariate objects) reproduce the geometry
+sources exactly: the window is HostNormalXDZ::checkAt restated in numpy at the
+reference's cell centres / nodes, and the signal HostUnivariate::evalAt at the
+accumulated step times."""
+import numpy as np
+import pytest
+
+import oracle
+from pannde_gb300 import _native as N
+from pannde_gb300 import cases
+from pannde_gb300.solver import Solver
+from tests.test_parity_gpu import compare, water_column_sources
+
+pytestmark = pytest.mark.gpu
+
+
+def check_at(src, pts):
+    """Stubs::HostNormalXDZ::checkAt (HostNormalXDZ.hpp:140-145, 174-177)."""
+    d2 = (pts[:, 0] - src.center[0]) ** 2
+    d2 = d2 + (pts[:, 1] - src.center[1]) ** 2
+    d2 = d2 + (pts[:, 2] - src.center[2]) ** 2
+    dist = np.sqrt(d2)
+    distz = np.abs(pts[:, 2] - src.center[2])
+    return ((distz <= 0.75 * src.ds) & (dist < src.radius) & (dist >= 0.)).astype(np.uint8)
+
+
+def signal_values(srcs, dt, nsteps):
+    from tests.test_capi_cpu import signal_eval
+    t = np.zeros(nsteps)
+    acc = 0.0
+    for k in range(nsteps):  # time += dt in FP64, as solve() accumulates it
+        t[k] = acc
+        acc += dt
+    cols = []
+    for s in srcs:
+        rc, v = signal_eval(s.times, s.values, t)
+        assert rc == 0
+        cols.append(v)
+    return np.stack(cols, axis=1)
+
+
+@pytest.mark.parametrize("prec,form", [("f64_exact", "table"), ("f64", "grid"), ("df64", "grid")])
+def test_masks_reproduce_geometry_sources(cuda_device, prec, form):
+    c = cases.al_plate_case(nx=37, ny=15, nz=4, nsteps=45, radius=0.5e-3, n_sensors=7)
+    h = c.meta["h"]
+    t, v = c.sources[0].times, c.sources[0].values
+    src = list(c.sources) + water_column_sources((1.5e-3, 0.7e-3, 0.4e-3), 0.4e-3, h, t, v)
+    ref = oracle.run(c.mesh, c.material_fields(), c.dt, src, c.nsteps, c.sensors)
+    centres = c.mesh.cell_centers()
+    nodes = np.stack([c.mesh.x, c.mesh.y, c.mesh.z], axis=1)
+    masks = [(s.kind, s.group, s.component,
+              check_at(s, centres if s.kind == N.PN_SOURCE_FORCE else nodes)) for s in src]
+    values = signal_values(src, c.dt, c.nsteps)
+    with Solver(c.mesh, c, c.dt, prec, form) as s:
+        s.add_window_masks(masks)
+        s.set_sensors(c.sensors, c.nsteps)
+        with pytest.raises(N.PnError):
+            s.solve(1)  # mask sources need caller signal values
+        tt = 0.0
+        for a, b in ((0, 1), (1, 20), (20, c.nsteps)):
+            tt = s.solve_signals(values[a:b])
+        V, S = s.get_state()
+        tr = s.traces()
+    assert tt == ref["time"]
+    compare(prec, (V, S, tr), ref)

@@ -226,9 +226,13 @@ def test_zero_steps_and_state_roundtrip(cuda_device, plate):
 
 def test_info_bytes(cuda_device, plate):
     c = plate
-    with Solver(c.mesh, c, c.dt, "f64") as s:
+    with Solver(c.mesh, c, c.dt, "f64", "table") as s:
         inf = s.info()
-    assert inf["uniform_spacing"] == 1
+    assert inf["uniform_spacing"] == 1 and inf["form_name"] == "table"
     assert inf["algorithmic_bytes_per_step"] == c.mesh.n_cells * 180 + c.mesh.n_nodes * 112
-    with Solver(c.mesh, c, c.dt, "f32") as s:
+    with Solver(c.mesh, c, c.dt, "f32", "table") as s:
         assert s.info()["algorithmic_bytes_per_step"] == c.mesh.n_cells * 108 + c.mesh.n_nodes * 72
+    with Solver(c.mesh, c, c.dt, "f64") as s:  # a voxel plate gets the grid form
+        inf = s.info()
+    assert inf["form_name"] == "grid" and inf["grid"] == (16, 16, 4)
+    assert inf["algorithmic_bytes_per_step"] == c.mesh.n_cells * 97 + c.mesh.n_nodes * 56
