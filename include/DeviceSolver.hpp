@@ -88,6 +88,8 @@ class DeviceModel : public PanNDE::Model {
     time_ = o.time_;
     sources_ = std::move(o.sources_);
     stale_ = o.stale_;
+    force_groups_ = o.force_groups_;
+    moment_groups_ = o.moment_groups_;
     return *this;
   }
 

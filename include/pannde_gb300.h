@@ -340,6 +340,29 @@ int pn_solver_synchronize(pn_solver *s);
 int pn_solver_enable_kernel_timing(pn_solver *s, int32_t enable);
 int pn_solver_kernel_times(pn_solver *s, double *ms /* [3] */, int64_t *launches /* [3] */);
 
+/* ---- batches ------------------------------------------------------------
+   A batch advances many solvers together: each step is one launch per half
+   step (table form) or one fused launch (grid form) covering every member,
+   with work tiles spread over the GPU whatever the members' sizes.  Members
+   are ordinary solvers (same precision and form) that keep their own state,
+   sources, sensors, time and dt; they can join and leave between steps, and
+   a member's results do not depend on the other members.  No counterpart in
+   the reference, which runs one model per process. */
+typedef struct pn_batch pn_batch;
+
+int pn_batch_create(pn_batch **out);
+/* Add / remove a member (the batch does not own it; destroy members after
+   removing them or destroying the batch). */
+int pn_batch_add(pn_batch *b, pn_solver *member);
+int pn_batch_remove(pn_batch *b, pn_solver *member);
+int pn_batch_size(pn_batch *b, int32_t *n_members);
+/* Work on this stream (void* cudaStream_t; NULL = legacy default stream). */
+int pn_batch_set_stream(pn_batch *b, void *cuda_stream);
+/* Advance every member nsteps steps (their own signals, sensors, time). */
+int pn_batch_solve(pn_batch *b, int32_t nsteps);
+int pn_batch_synchronize(pn_batch *b);
+int pn_batch_destroy(pn_batch *b);
+
 /* Free all device memory of the solver. */
 int pn_solver_destroy(pn_solver *s);
 

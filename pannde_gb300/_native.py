@@ -127,6 +127,14 @@ SIGNATURES = {
     "pn_solver_enable_kernel_timing": (c_int, [c_void_p, c_int32]),
     "pn_solver_kernel_times": (c_int, [c_void_p, P_double, POINTER(c_int64)]),
     "pn_solver_destroy": (c_int, [c_void_p]),
+    "pn_batch_create": (c_int, [POINTER(c_void_p)]),
+    "pn_batch_add": (c_int, [c_void_p, c_void_p]),
+    "pn_batch_remove": (c_int, [c_void_p, c_void_p]),
+    "pn_batch_size": (c_int, [c_void_p, P_int32]),
+    "pn_batch_set_stream": (c_int, [c_void_p, c_void_p]),
+    "pn_batch_solve": (c_int, [c_void_p, c_int32]),
+    "pn_batch_synchronize": (c_int, [c_void_p]),
+    "pn_batch_destroy": (c_int, [c_void_p]),
 }
 
 

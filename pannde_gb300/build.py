@@ -8,6 +8,7 @@ Sources (``pannde_gb300/csrc``):
   pn_table.cpp  table form (any hex mesh)     g++
   pn_grid.cpp   grid form (voxel meshes)      g++
   pn_capi.cpp   C ABI                         g++
+  pn_batch.cpp  batches of solvers            g++
 Translation units compile in parallel; the link uses nvcc (static cudart).
 Output: ``pannde_gb300/_build/libpannde_gb300.so``.
 """
@@ -54,6 +55,7 @@ def _jobs() -> list[tuple[list[str], Path]]:
         (common_cc + ["-c", str(CSRC / "pn_table.cpp")], OUT / "pn_table.o"),
         (common_cc + ["-c", str(CSRC / "pn_grid.cpp")], OUT / "pn_grid.o"),
         (common_cc + ["-c", str(CSRC / "pn_capi.cpp")], OUT / "pn_capi.o"),
+        (common_cc + ["-c", str(CSRC / "pn_batch.cpp")], OUT / "pn_batch.o"),
     ]
     return [(cmd + ["-o", str(obj)], obj) for cmd, obj in jobs]
 

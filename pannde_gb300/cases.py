@@ -357,3 +357,102 @@ def holed_plate_case(nx=1024, ny=1024, nz=24, h=0.1e-3, nsteps=4000, n_holes=12,
     case = al_plate_case(nx, ny, nz, h, nsteps, 1e6, 2e-3, n_sensors, seed, holes, name)
     case.meta["holes"] = holes
     return case
+
+
+# ---- angle brackets (L-sections) --------------------------------------------
+
+WATER = dict(rho=1000.0, c=1480.0)
+
+
+def fluid_stiffness(rho: float, c: float) -> np.ndarray:
+    """Acoustic fluid through the 21 Cij: C11=C22=C33=C12=C13=C23=rho c^2, no shear."""
+    k = rho * c * c
+    out = np.zeros((6, 6))
+    out[:3, :3] = k
+    return out
+
+
+def disconnect_face(mesh: HexMesh, cells_above: np.ndarray, node_mask: np.ndarray) -> HexMesh:
+    """Split the mesh along a face: the nodes in node_mask get a duplicate that
+    the cells in cells_above use instead, so the two sides share no node there
+    (a zero-thickness crack; the reference then sees a missing incident cell on
+    each side, RightHex.hpp:225-231)."""
+    dup = np.flatnonzero(node_mask)
+    new_id = np.full(mesh.n_nodes, -1, dtype=np.int64)
+    new_id[dup] = mesh.n_nodes + np.arange(dup.size)
+    hexes = mesh.hexes.copy()
+    sub = hexes[cells_above]
+    repl = new_id[sub]
+    sub[repl >= 0] = repl[repl >= 0]
+    hexes[cells_above] = sub
+    x = np.concatenate([mesh.x, mesh.x[dup]])
+    y = np.concatenate([mesh.y, mesh.y[dup]])
+    z = np.concatenate([mesh.z, mesh.z[dup]])
+    ijk = np.concatenate([mesh.node_ijk, mesh.node_ijk[dup]]) if mesh.node_ijk is not None else None
+    return HexMesh(x, y, z, hexes.astype(np.int32), node_ijk=ijk, cell_ijk=mesh.cell_ijk)
+
+
+def bracket_case(seed: int, h=0.1e-3, nsteps=3000, water_column=False, n_sensors=8,
+                 scale=1.0, name="bracket") -> Case:
+    """Aluminium L-section angle bracket with a seeded planar crack at the inner fillet.
+
+    Cross-section in (y, z): a vertical leg (y < t) and a horizontal leg (z < t),
+    extruded along x (the voxel construction of AL_Angle_Bracket_Water_Column_Case_Maker.py:
+    geometry[:, :t, :] = geometry[:, :, :t] = 1).  Leg lengths 60-220 cells, thickness
+    12-30 cells, depth 40-160 cells, drawn from the seed (scale shrinks them for tests).
+    The crack lies in the plane z = t under the vertical leg, opening at the inner
+    face y = t, 1-6 mm long along x, as disconnected faces.  With water_column, a
+    cylinder of fluid cells (rho 1000, c 1480 m/s) stands on the horizontal leg's top
+    face and the excitation is a pressure (xx, yy, zz moment) window at its top;
+    otherwise a z-force transducer acts on the horizontal leg's outer face."""
+    rng = np.random.default_rng(seed)
+    ly = max(4, int(round(rng.integers(60, 221) * scale)))
+    lz = max(4, int(round(rng.integers(60, 221) * scale)))
+    t = max(2, int(round(rng.integers(12, 31) * scale)))
+    d = max(4, int(round(rng.integers(40, 161) * scale)))
+    ly, lz = max(ly, t + 2), max(lz, t + 2)
+    col_r = max(1, int(round(rng.integers(5, 16) * scale)))
+    col_h = max(1, int(round(rng.integers(10, 31) * scale)))
+    nz_box = max(lz, t + col_h) if water_column else lz
+    solid = np.zeros((d, ly, nz_box), dtype=bool)
+    solid[:, :t, :lz] = True
+    solid[:, :, :t] = True
+    fluid = np.zeros_like(solid)
+    yc = (t + ly) / 2.0
+    if water_column:
+        ii, jj = np.meshgrid(np.arange(d) + 0.5, np.arange(ly) + 0.5, indexing="ij")
+        disk = ((ii - d / 2.0) ** 2 + (jj - yc) ** 2 < col_r ** 2) & (jj >= t)
+        for k in range(t, t + col_h):
+            fluid[:, :, k] |= disk
+        fluid &= ~solid
+        solid |= fluid
+    mesh = voxel_mesh(solid, h)
+    ci, cj, ck = mesh.cell_ijk[:, 0], mesh.cell_ijk[:, 1], mesh.cell_ijk[:, 2]
+    cell_material = fluid[ci, cj, ck].astype(np.int32)
+    # crack: plane z = t, x in (x0, x0 + c), y in (t - cw, t], under the vertical leg
+    c_len = max(2, int(round(rng.uniform(1e-3, 6e-3) / h * min(1.0, scale * 2))))
+    c_len = min(c_len, d - 2)
+    cw = max(1, min(t - 1, int(round(rng.uniform(0.2, 0.6) * t))))
+    x0 = int(rng.integers(1, max(2, d - c_len)))
+    ni, nj, nk = mesh.node_ijk[:, 0], mesh.node_ijk[:, 1], mesh.node_ijk[:, 2]
+    on_face = (nk == t) & (ni > x0) & (ni < x0 + c_len) & (nj > t - cw) & (nj <= t)
+    above = np.flatnonzero((ck >= t) & (cj < t) & (cell_material == 0))
+    mesh = disconnect_face(mesh, above, on_face)
+    c_al = isotropic(ALUMINIUM["E"], ALUMINIUM["nu"])
+    rho_al = ALUMINIUM["rho"]
+    c_w = fluid_stiffness(WATER["rho"], WATER["c"])
+    dt = cfl_dt(h, max_wave_speed(c_al, rho_al))
+    freq = float(rng.uniform(0.5e6, 2e6))
+    tt, vv = tone_burst(freq, 5, dt)
+    if water_column:
+        ztop = (t + col_h) * h
+        src = [WindowSource(N.PN_SOURCE_MOMENT, 0, comp, (d * h / 2, yc * h, ztop), col_r * h * 0.9, h, tt, -vv)
+               for comp in (0, 1, 2)]
+    else:
+        src = [transducer_z((d * h / 2, yc * h, 0.0), max(2, col_r) * h, h, tt, vv)]
+    outer = np.flatnonzero((mesh.z == 0.0) | (mesh.y == 0.0))
+    sens = np.sort(rng.choice(outer, size=min(n_sensors, outer.size), replace=False)).astype(np.int32)
+    return Case(f"{name}-{seed}", mesh, np.array([rho_al, WATER["rho"]]),
+                np.stack([c21_from_6x6(c_al), c21_from_6x6(c_w)]), cell_material, dt, src, sens, nsteps,
+                dict(ly=ly, lz=lz, t=t, d=d, crack=(x0, c_len, cw), water_column=water_column, h=h,
+                     freq=freq))

@@ -1,0 +1,299 @@
+// pn_batch.cpp -- batches of solvers advanced by shared launches.
+//
+// Members keep everything of their own (state, tables, sources, sensors,
+// time, dt); a batch solve writes their argument blocks into one device array
+// and launches, per step, one kernel per half step (table form) or one fused
+// kernel (grid form) whose blocks walk the work tiles of all members.  The
+// arithmetic of a member does not depend on the others, so a member's result
+// is the same alone and in any batch.  pn_batch_solve returns when the steps
+// are done (it waits for the GPU at the end of every signal-table chunk).
+#include <cstring>
+#include <type_traits>
+
+#include "pn_solver.hpp"
+
+struct pn_batch {
+  std::vector<pn_solver *> members;
+  cudaStream_t stream = nullptr;
+  // device staging of argument blocks and prefix tables
+  void *d_args[2] = {nullptr, nullptr};  // table: vel / stress; grid: even / odd step parity
+  int *d_start[2] = {nullptr, nullptr};
+  size_t cap_args = 0, cap_start = 0;
+
+  ~pn_batch() {
+    for (int k = 0; k < 2; k++) {
+      if (d_args[k]) cudaFree(d_args[k]);
+      if (d_start[k]) cudaFree(d_start[k]);
+    }
+  }
+};
+
+namespace {
+
+int berr(int code, const std::string &m) { return pn::set_last_error(code, m); }
+
+template <typename F>
+int bguard(F &&f) {
+  pn::set_last_error(PN_OK, "");
+  try {
+    return f();
+  } catch (const pn::SetupError &e) {
+    return berr(e.code, e.msg);
+  } catch (const pn::CudaError &e) {
+    (void)cudaGetLastError();
+    return berr(PN_ERR_CUDA, std::string(e.what) + ": " + cudaGetErrorString(e.e));
+  } catch (const std::exception &e) {
+    return berr(PN_ERR_RUNTIME, e.what());
+  }
+}
+
+void ensure_capacity(pn_batch *b, size_t args_bytes, size_t start_ints) {
+  if (args_bytes > b->cap_args) {
+    for (int k = 0; k < 2; k++) {
+      if (b->d_args[k]) cudaFree(b->d_args[k]);
+      b->d_args[k] = nullptr;
+      pn::ck(cudaMalloc(&b->d_args[k], args_bytes), "batch args");
+    }
+    b->cap_args = args_bytes;
+  }
+  if (start_ints > b->cap_start) {
+    for (int k = 0; k < 2; k++) {
+      if (b->d_start[k]) cudaFree(b->d_start[k]);
+      b->d_start[k] = nullptr;
+      pn::ck(cudaMalloc(&b->d_start[k], start_ints * sizeof(int)), "batch tiles");
+    }
+    b->cap_start = start_ints;
+  }
+}
+
+// steps all members can take with their current signal tables
+int32_t common_chunk(pn_batch *b, int32_t want) {
+  int32_t chunk = want;
+  for (pn_solver *s : b->members) {
+    pn::ensure_signal_rows(s, chunk);
+    if (!s->src.empty() && !s->sig_hold)
+      chunk = (int32_t)std::min<int64_t>(chunk, s->sig_step0 + s->sig_rows - s->step);
+  }
+  return std::max<int32_t>(chunk, 1);
+}
+
+// per-member bookkeeping after `chunk` steps (time accumulated step by step,
+// as solve() does)
+void advance(pn_batch *b, int32_t chunk) {
+  for (pn_solver *s : b->members) {
+    for (int32_t k = 0; k < chunk; k++) s->time += s->dt;
+    if (s->form == PN_FORM_GRID && (chunk & 1)) s->cur ^= 1;
+    s->step += chunk;
+    s->rec_count += chunk;
+  }
+}
+
+template <typename T>
+void solve_table(pn_batch *b, int32_t nsteps, int precision) {
+  const int n = (int)b->members.size();
+  std::vector<pn::VelArgs<T>> va(n);
+  std::vector<pn::StressArgs<T>> sa(n);
+  std::vector<int> vs(n + 1, 0), ss(n + 1, 0);
+  int32_t done = 0;
+  while (done < nsteps) {
+    const int32_t chunk = common_chunk(b, nsteps - done);
+    for (int m = 0; m < n; m++) {
+      pn_solver *s = b->members[m];
+      pn::table_args<T>(s, va[m], sa[m]);
+      const int64_t nsig = (int64_t)s->src.size();
+      if (nsig > 0) {
+        const int64_t row0 = pn::sig_row(s, 0);
+        va[m].sigval = (const T *)s->d_sig + row0 * nsig;
+        va[m].sig_stride = (int32_t)nsig;
+        va[m].sig_rows = (int32_t)(s->sig_rows - row0);
+        sa[m].sigval = va[m].sigval;
+        sa[m].sig_stride = va[m].sig_stride;
+        sa[m].sig_rows = va[m].sig_rows;
+      }
+      va[m].rec_base = s->rec_count;
+      vs[m + 1] = vs[m] + (s->mesh.n_nodes + pn::kTile - 1) / pn::kTile;
+      ss[m + 1] = ss[m] + (s->mesh.n_cells + pn::kTile - 1) / pn::kTile;
+    }
+    ensure_capacity(b, std::max(sizeof(pn::VelArgs<T>), sizeof(pn::StressArgs<T>)) * n, n + 1);
+    pn::ck(cudaMemcpyAsync(b->d_args[0], va.data(), sizeof(pn::VelArgs<T>) * n, cudaMemcpyHostToDevice,
+                           b->stream), "batch args");
+    pn::ck(cudaMemcpyAsync(b->d_args[1], sa.data(), sizeof(pn::StressArgs<T>) * n, cudaMemcpyHostToDevice,
+                           b->stream), "batch args");
+    pn::ck(cudaMemcpyAsync(b->d_start[0], vs.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, b->stream),
+           "batch tiles");
+    pn::ck(cudaMemcpyAsync(b->d_start[1], ss.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, b->stream),
+           "batch tiles");
+    int dev = 0, sms = 1;
+    pn::ck(cudaGetDevice(&dev), "device");
+    pn::ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "sm count");
+    pn::BatchLaunch L;
+    L.n_members = n;
+    L.vel_args = b->d_args[0];
+    L.str_args = b->d_args[1];
+    L.vel_start = b->d_start[0];
+    L.str_start = b->d_start[1];
+    L.vel_tiles = vs[n];
+    L.str_tiles = ss[n];
+    // blocks walk the tiles: enough resident blocks for the GPU, never more than tiles
+    L.blocks_vel = std::min(vs[n], sms * 8);
+    L.blocks_str = std::min(ss[n], sms * 8);
+    for (int32_t k = 0; k < chunk; k++) pn::ck(pn::launch_table_batch(L, precision, k, b->stream), "batch step");
+    pn::ck(cudaStreamSynchronize(b->stream), "batch chunk");  // staging is reused next chunk
+    advance(b, chunk);
+    done += chunk;
+  }
+}
+
+template <typename T>
+void solve_grid(pn_batch *b, int32_t nsteps, int precision) {
+  const int n = (int)b->members.size();
+  std::vector<pn::GridArgs<T>> ga[2] = {std::vector<pn::GridArgs<T>>(n), std::vector<pn::GridArgs<T>>(n)};
+  std::vector<int> bs(n + 1, 0);
+  const int tx = pn::grid_tile_x(), ty = pn::grid_tile_y();
+  int sym = 2;
+  int32_t done = 0;
+  while (done < nsteps) {
+    const int32_t chunk = common_chunk(b, nsteps - done);
+    for (int m = 0; m < n; m++) {
+      pn_solver *s = b->members[m];
+      pn::GridArgs<T> a;
+      pn::grid_args<T>(s, a);
+      const int64_t nsig = (int64_t)s->src.size();
+      if (nsig > 0) {
+        const int64_t row0 = pn::sig_row(s, 0);
+        a.sigval = (const T *)s->d_sig + row0 * nsig;
+        a.sig_stride = (int32_t)nsig;
+        a.sig_rows = (int32_t)(s->sig_rows - row0);
+      }
+      a.rec = s->rec_count;
+      a.kchunk = pn::grid_chunk_layers(precision, a.nx, a.ny, a.nz);
+      for (int p = 0; p < 2; p++) {  // step parity: buffers swap every step
+        pn::GridArgs<T> q = a;
+        const int in = s->cur ^ p, out = in ^ 1;
+        for (int c = 0; c < 3; c++) {
+          q.V_in[c] = (const T *)s->V[in][c];
+          q.V_out[c] = (T *)s->V[out][c];
+        }
+        for (int c = 0; c < 6; c++) {
+          q.S_in[c] = (const T *)s->S[in][c];
+          q.S_out[c] = (T *)s->S[out][c];
+        }
+        ga[p][m] = q;
+      }
+      const int64_t blocks = (int64_t)(a.nx / (tx - 1) + 1) * (a.ny / (ty - 1) + 1) *
+                             ((a.nz + a.kchunk - 1) / a.kchunk);
+      bs[m + 1] = (int)(bs[m] + blocks);
+      sym = std::min(sym, s->sym);
+    }
+    ensure_capacity(b, sizeof(pn::GridArgs<T>) * n, n + 1);
+    for (int p = 0; p < 2; p++)
+      pn::ck(cudaMemcpyAsync(b->d_args[p], ga[p].data(), sizeof(pn::GridArgs<T>) * n, cudaMemcpyHostToDevice,
+                             b->stream), "batch args");
+    pn::ck(cudaMemcpyAsync(b->d_start[0], bs.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, b->stream),
+           "batch blocks");
+    for (int32_t k = 0; k < chunk; k++) {
+      pn::GridBatchLaunch L;
+      L.n_members = n;
+      L.args = b->d_args[k & 1];
+      L.block_start = b->d_start[0];
+      L.total_blocks = bs[n];
+      L.sym = sym;
+      pn::ck(pn::launch_grid_batch(L, precision, k, b->stream), "batch step");
+    }
+    pn::ck(cudaStreamSynchronize(b->stream), "batch chunk");
+    advance(b, chunk);
+    done += chunk;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int pn_batch_create(pn_batch **out) {
+  return bguard([&]() -> int {
+    if (!out) return berr(PN_ERR_INVALID, "null output handle");
+    *out = new pn_batch();
+    return PN_OK;
+  });
+}
+
+int pn_batch_add(pn_batch *b, pn_solver *m) {
+  if (!b || !m) return berr(PN_ERR_INVALID, "null argument");
+  for (pn_solver *x : b->members)
+    if (x == m) return berr(PN_ERR_INVALID, "solver already in the batch");
+  if (!b->members.empty()) {
+    pn_solver *f = b->members.front();
+    if (f->precision != m->precision || f->form != m->form)
+      return berr(PN_ERR_INVALID, "batch members need one precision and one form");
+  }
+  if (m->precision == PN_PREC_F64_EXACT) return berr(PN_ERR_INVALID, "the exact FP64 form is not batched");
+  if (m->has_mask_sources()) return berr(PN_ERR_INVALID, "window-mask sources need pn_solver_solve_signals");
+  b->members.push_back(m);
+  return PN_OK;
+}
+
+int pn_batch_remove(pn_batch *b, pn_solver *m) {
+  if (!b || !m) return berr(PN_ERR_INVALID, "null argument");
+  auto it = std::find(b->members.begin(), b->members.end(), m);
+  if (it == b->members.end()) return berr(PN_ERR_INVALID, "solver not in the batch");
+  b->members.erase(it);
+  return PN_OK;
+}
+
+int pn_batch_size(pn_batch *b, int32_t *n) {
+  if (!b || !n) return berr(PN_ERR_INVALID, "null argument");
+  *n = (int32_t)b->members.size();
+  return PN_OK;
+}
+
+int pn_batch_set_stream(pn_batch *b, void *stream) {
+  return bguard([&]() -> int {
+    if (!b) return berr(PN_ERR_INVALID, "null batch");
+    pn::ck(cudaStreamSynchronize(b->stream), "stream switch");
+    b->stream = (cudaStream_t)stream;
+    return PN_OK;
+  });
+}
+
+int pn_batch_solve(pn_batch *b, int32_t nsteps) {
+  return bguard([&]() -> int {
+    if (!b) return berr(PN_ERR_INVALID, "null batch");
+    if (nsteps < 0) return berr(PN_ERR_INVALID, "negative step count");
+    if (b->members.empty() || nsteps == 0) return PN_OK;
+    for (pn_solver *s : b->members) {
+      if (s->has_mask_sources()) return berr(PN_ERR_INVALID, "window-mask sources need pn_solver_solve_signals");
+      pn::ck(cudaStreamSynchronize(s->stream), "member sync");  // members' own work first
+      pn::refresh_sources(s);
+    }
+    const pn_solver *f = b->members.front();
+    if (f->form == PN_FORM_GRID) {
+      if (f->is_df64()) solve_grid<float2>(b, nsteps, f->precision);
+      else if (f->esz == 8) solve_grid<double>(b, nsteps, f->precision);
+      else solve_grid<float>(b, nsteps, f->precision);
+    } else {
+      if (f->is_df64()) solve_table<float2>(b, nsteps, f->precision);
+      else if (f->esz == 8) solve_table<double>(b, nsteps, f->precision);
+      else solve_table<float>(b, nsteps, f->precision);
+    }
+    return PN_OK;
+  });
+}
+
+int pn_batch_synchronize(pn_batch *b) {
+  return bguard([&]() -> int {
+    if (!b) return berr(PN_ERR_INVALID, "null batch");
+    pn::ck(cudaStreamSynchronize(b->stream), "batch sync");
+    pn::ck(cudaGetLastError(), "device error");
+    return PN_OK;
+  });
+}
+
+int pn_batch_destroy(pn_batch *b) {
+  if (!b) return PN_OK;
+  cudaStreamSynchronize(b->stream);
+  delete b;
+  return PN_OK;
+}
+
+}  // extern "C"

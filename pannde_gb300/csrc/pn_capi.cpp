@@ -374,20 +374,30 @@ int pn_solver_set_sensors(pn_solver *s, const int32_t *nodes, int32_t n, int32_t
   });
 }
 
-namespace {
+}  // extern "C"
+
+namespace pn {
+int set_last_error(int code, const std::string &msg) { return set_err(code, msg); }
+
 void refresh_sources(pn_solver *s) {
   if (!s->src_dirty) return;
-  if (s->form == PN_FORM_GRID) pn::grid_sources(s);
-  else pn::table_sources(s);
+  if (s->form == PN_FORM_GRID) grid_sources(s);
+  else table_sources(s);
   s->src_dirty = false;
   s->sig_valid = false;
 }
+}  // namespace pn
+
+namespace {
+using pn::refresh_sources;
 
 void run_any(pn_solver *s, int32_t nsteps) {
   if (s->form == PN_FORM_GRID) pn::grid_run(s, nsteps);
   else pn::table_run(s, nsteps);
 }
 }  // namespace
+
+extern "C" {
 
 int pn_solver_solve(pn_solver *s, int32_t nsteps, double *time_out) {
   return guarded([&]() -> int {

@@ -272,12 +272,9 @@ void grid_sensors(pn_solver *s, const std::vector<std::pair<int32_t, int32_t>> &
   s->upload_raw(s->d_sidx, idx.data(), idx.size() * 4);
 }
 
-namespace {
-
 template <typename T>
-void run(pn_solver *s, int32_t nsteps) {
+void grid_args(pn_solver *s, GridArgs<T> &a) {
   const GridMap &g = s->grid;
-  GridArgs<T> a;
   std::memset(&a, 0, sizeof(a));
   a.nx = g.nx;
   a.ny = g.ny;
@@ -296,6 +293,23 @@ void run(pn_solver *s, int32_t nsteps) {
   }
   a.n_sens = s->n_sens;
   a.traces = s->d_traces;
+  a.rec_cap = s->rec_cap;
+  a.s_rng = s->n_sens > 0 ? s->d_srng : nullptr;
+  a.s_key = s->d_skey;
+  a.s_idx = s->d_sidx;
+  a.sig_stride = 0;
+  a.sig_rows = 1;
+}
+template void grid_args<double>(pn_solver *, GridArgs<double> &);
+template void grid_args<float>(pn_solver *, GridArgs<float> &);
+template void grid_args<float2>(pn_solver *, GridArgs<float2> &);
+
+namespace {
+
+template <typename T>
+void run(pn_solver *s, int32_t nsteps) {
+  GridArgs<T> a;
+  grid_args<T>(s, a);
   const int64_t nsig = (int64_t)s->src.size();
   int32_t done = 0;
   while (done < nsteps) {
@@ -314,11 +328,7 @@ void run(pn_solver *s, int32_t nsteps) {
         a.S_out[c] = (T *)s->S[out][c];
       }
       a.sigval = nsig > 0 ? (const T *)s->d_sig + sig_row(s, k) * nsig : nullptr;
-      a.rec = s->rec_count + k;
-      const bool rec_on = s->n_sens > 0 && a.rec < s->rec_cap;
-      a.s_rng = rec_on ? s->d_srng : nullptr;
-      a.s_key = s->d_skey;
-      a.s_idx = s->d_sidx;
+      a.rec = s->rec_count + k;  // sigval points at this step's row (stride 0)
       pn_solver::Mark m{};
       if (s->timing) {
         ck(cudaEventCreate(&m.a), "event");

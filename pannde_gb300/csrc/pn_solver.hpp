@@ -243,4 +243,15 @@ void grid_get_state(pn_solver *s, double *const *V, double *const *S);
 // algorithmic HBM bytes of one step in the solver's form
 int64_t step_bytes(const pn_solver *s);
 
+// argument blocks of one solver (pointers, tables, constants; the per-step
+// fields -- signal row, record, buffers -- are the caller's to set)
+template <typename T> void table_args(pn_solver *s, VelArgs<T> &va, StressArgs<T> &sa);
+template <typename T> void grid_args(pn_solver *s, GridArgs<T> &a);
+
+// rebuild the source lists after sources changed (pn_capi.cpp)
+void refresh_sources(pn_solver *s);
+
+// the calling thread's message for pn_last_error(); returns code (pn_capi.cpp)
+int set_last_error(int code, const std::string &msg);
+
 }  // namespace pn

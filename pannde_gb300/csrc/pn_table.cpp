@@ -127,10 +127,8 @@ void table_sensors(pn_solver *s, const std::vector<std::pair<int32_t, int32_t>> 
   s->upload_raw(s->d_sidx, ix.data(), ix.size() * 4);
 }
 
-namespace {
-
 template <typename T>
-void fill_launch_args(pn_solver *s, VelArgs<T> &va, StressArgs<T> &sa) {
+void table_args(pn_solver *s, VelArgs<T> &va, StressArgs<T> &sa) {
   std::memset(&va, 0, sizeof(va));
   std::memset(&sa, 0, sizeof(sa));
   va.n_nodes = s->mesh.n_nodes;
@@ -149,6 +147,8 @@ void fill_launch_args(pn_solver *s, VelArgs<T> &va, StressArgs<T> &sa) {
     va.src_w = (const T *)s->d_fw;
   }
   va.n_sig = (int32_t)s->src.size();
+  va.sig_stride = 0;  // single launches point sigval at the step's row
+  va.sig_rows = 1;
   if (s->n_sens > 0) {
     va.tile_sens = s->d_stile; va.sens_node = s->d_snode; va.sens_idx = s->d_sidx;
     va.traces = s->d_traces; va.n_sens = s->n_sens; va.rec_cap = s->rec_cap;
@@ -167,14 +167,21 @@ void fill_launch_args(pn_solver *s, VelArgs<T> &va, StressArgs<T> &sa) {
     sa.src_w = (const T *)s->d_mw;
   }
   sa.n_sig = va.n_sig;
+  sa.sig_stride = 0;
+  sa.sig_rows = 1;
   sa.has_moments = s->has_moments ? 1 : 0;
 }
+template void table_args<double>(pn_solver *, VelArgs<double> &, StressArgs<double> &);
+template void table_args<float>(pn_solver *, VelArgs<float> &, StressArgs<float> &);
+template void table_args<float2>(pn_solver *, VelArgs<float2> &, StressArgs<float2> &);
+
+namespace {
 
 template <typename T>
 void run(pn_solver *s, int32_t nsteps) {
   VelArgs<T> va;
   StressArgs<T> sa;
-  fill_launch_args<T>(s, va, sa);
+  table_args<T>(s, va, sa);
   const int64_t nsig = (int64_t)s->src.size();
   int32_t done = 0;
   while (done < nsteps) {

@@ -44,8 +44,10 @@ struct VelArgs {
   const int32_t *__restrict__ src_elem;
   const int32_t *__restrict__ src_code;  // dir | (signal << 2)
   const T *__restrict__ src_w;
-  const T *__restrict__ sigval;  // [steps][n_sig] signal values of this solve() call
+  const T *__restrict__ sigval;  // signal values: row min(step, sig_rows-1) at stride sig_stride
   int32_t n_sig;
+  int32_t sig_stride;            // 0 when sigval already points at this step's row
+  int32_t sig_rows;
   // sensors
   const int2 *__restrict__ tile_sens;  // [n_tiles] or null
   const int32_t *__restrict__ sens_node;
@@ -81,8 +83,18 @@ struct StressArgs {
   const T *__restrict__ src_w;
   const T *__restrict__ sigval;
   int32_t n_sig;
+  int32_t sig_stride;
+  int32_t sig_rows;
   int32_t has_moments;
 };
+
+#ifdef __CUDACC__
+// signal row of a step: sigval + min(step, sig_rows-1) * sig_stride
+template <typename T>
+__device__ __forceinline__ const T *signal_row(const T *sigval, int step, int stride, int rows) {
+  return sigval + (int64_t)min(step, rows - 1) * stride;
+}
+#endif
 
 // Launchers (defined in rsg_fast.cu / rsg_exact.cu).  step = index of this
 // step inside the current solve() call (selects the signal row).
@@ -92,6 +104,20 @@ cudaError_t launch_velocity_f32(const VelArgs<float> &a, int step, bool uniform,
 cudaError_t launch_stress_f32(const StressArgs<float> &a, int step, bool uniform, cudaStream_t st);
 cudaError_t launch_velocity_df64(const VelArgs<float2> &a, int step, bool uniform, cudaStream_t st);
 cudaError_t launch_stress_df64(const StressArgs<float2> &a, int step, bool uniform, cudaStream_t st);
+// a batch of table-form members: device arrays of their argument blocks and
+// the prefix sums of their tile counts (members own consecutive tiles)
+struct BatchLaunch {
+  int n_members;
+  const void *vel_args;   // VelArgs<S>[n_members]
+  const void *str_args;   // StressArgs<S>[n_members]
+  const int *vel_start;   // [n_members + 1]
+  const int *str_start;   // [n_members + 1]
+  int vel_tiles, str_tiles;
+  int blocks_vel, blocks_str;  // grid sizes (blocks walk the tiles)
+};
+// precision: PN_PREC_F64 (1), PN_PREC_F32 (2), PN_PREC_DF64 (3)
+cudaError_t launch_table_batch(const BatchLaunch &b, int precision, int step, cudaStream_t st);
+
 cudaError_t launch_velocity_exact(const VelArgs<double> &a, int step, cudaStream_t st);
 cudaError_t launch_stress_exact(const StressArgs<double> &a, int step, cudaStream_t st);
 

@@ -81,11 +81,11 @@ __device__ __forceinline__ void gather_nodes(const typename Num<R>::S *__restric
   for (int k = 0; k < 8; k++) out[k] = Num<R>::ld(f, s[k]);
 }
 
+// velocity update of node n (tile = n / kTile, step within the call)
 template <typename R, bool UNIFORM>
-__global__ void __launch_bounds__(kTile) k_velocity(const VelArgs<typename Num<R>::S> a, int step) {
+__device__ __forceinline__ void velocity_node(const VelArgs<typename Num<R>::S> &a, int n, int tile,
+                                              int step) {
   using N = Num<R>;
-  const int n = blockIdx.x * kTile + threadIdx.x;
-  if (n >= a.n_nodes) return;
   const R cf = N::get(a.coef, n);
   R v0 = N::get(a.V0, n), v1 = N::get(a.V1, n), v2 = N::get(a.V2, n);
   if (!(cf == R())) {  // a zero coefficient marks a node owned by another partition
@@ -114,11 +114,12 @@ __global__ void __launch_bounds__(kTile) k_velocity(const VelArgs<typename Num<R
     gather_slots<R>(a.S2, s, f); diff3(f, dx, dy, dz);
     az = az + gz * dz;
     if (a.tile_src) {
-      const int2 r = a.tile_src[blockIdx.x];
+      const int2 r = a.tile_src[tile];
+      const typename N::S *sig = signal_row(a.sigval, step, a.sig_stride, a.sig_rows);
       for (int i = r.x; i < r.y; i++) {
         if (a.src_elem[i] != n) continue;
         const int code = a.src_code[i];
-        const R v = N::get(a.src_w, i) * N::get(a.sigval, code >> 2);
+        const R v = N::get(a.src_w, i) * N::get(sig, code >> 2);
         const int d = code & 3;
         if (d == 0) ax = ax + v;
         else if (d == 1) ay = ay + v;
@@ -133,7 +134,7 @@ __global__ void __launch_bounds__(kTile) k_velocity(const VelArgs<typename Num<R
     N::put(a.V2, n, v2);
   }
   if (a.tile_sens) {  // V after this step at the sensors of this tile
-    const int2 r = a.tile_sens[blockIdx.x];
+    const int2 r = a.tile_sens[tile];
     const int64_t rec = a.rec_base + step;
     if (rec < a.rec_cap) {
       for (int i = r.x; i < r.y; i++) {
@@ -147,11 +148,11 @@ __global__ void __launch_bounds__(kTile) k_velocity(const VelArgs<typename Num<R
   }
 }
 
+// stress update of cell c
 template <typename R, bool UNIFORM>
-__global__ void __launch_bounds__(kTile) k_stress(const StressArgs<typename Num<R>::S> a, int step) {
+__device__ __forceinline__ void stress_cell(const StressArgs<typename Num<R>::S> &a, int c, int tile,
+                                            int step) {
   using N = Num<R>;
-  const int c = blockIdx.x * kTile + threadIdx.x;
-  if (c >= a.n_cells) return;
   const int4 lo = a.hex[2 * c], hi = a.hex[2 * c + 1];
   const int s[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
   R gx = N::val(a.gx), gy = N::val(a.gy), gz = N::val(a.gz);
@@ -178,11 +179,12 @@ __global__ void __launch_bounds__(kTile) k_stress(const StressArgs<typename Num<
 #pragma unroll
   for (int q = 0; q < 6; q++) m[q] = R();
   if (a.tile_src) {
-    const int2 r = a.tile_src[blockIdx.x];
+    const int2 r = a.tile_src[tile];
+    const typename N::S *sig = signal_row(a.sigval, step, a.sig_stride, a.sig_rows);
     for (int i = r.x; i < r.y; i++) {
       if (a.src_elem[i] != c) continue;
       const int code = a.src_code[i];
-      const R v = N::get(a.src_w, i) * N::get(a.sigval, code >> 3);
+      const R v = N::get(a.src_w, i) * N::get(sig, code >> 3);
       const int k = code & 7;
 #pragma unroll
       for (int q = 0; q < 6; q++)
@@ -196,6 +198,62 @@ __global__ void __launch_bounds__(kTile) k_stress(const StressArgs<typename Num<
 #pragma unroll
     for (int j = 0; j < 6; j++) acc = acc + N::ld(C, 6 * k + j) * e[j];
     N::put(S[k], c, acc);
+  }
+}
+
+template <typename R, bool UNIFORM>
+__global__ void __launch_bounds__(kTile) k_velocity(const VelArgs<typename Num<R>::S> a, int step) {
+  const int n = blockIdx.x * kTile + threadIdx.x;
+  if (n < a.n_nodes) velocity_node<R, UNIFORM>(a, n, blockIdx.x, step);
+}
+
+template <typename R, bool UNIFORM>
+__global__ void __launch_bounds__(kTile) k_stress(const StressArgs<typename Num<R>::S> a, int step) {
+  const int c = blockIdx.x * kTile + threadIdx.x;
+  if (c < a.n_cells) stress_cell<R, UNIFORM>(a, c, blockIdx.x, step);
+}
+
+// member owning work tile t: tile_start is the members' prefix of tile counts
+__device__ __forceinline__ int member_of(const int *__restrict__ tile_start, int n_members, int t) {
+  int lo = 0, hi = n_members;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(tile_start + mid) <= t) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// batches: blocks walk the tiles of all members (grid-stride)
+template <typename R>
+__global__ void __launch_bounds__(kTile) k_velocity_batch(const VelArgs<typename Num<R>::S> *__restrict__ args,
+                                                          const int *__restrict__ tile_start, int n_members,
+                                                          int step) {
+  const int total = __ldg(tile_start + n_members);
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int m = member_of(tile_start, n_members, t);
+    const VelArgs<typename Num<R>::S> a = args[m];
+    const int tl = t - __ldg(tile_start + m);
+    const int n = tl * kTile + threadIdx.x;
+    if (n >= a.n_nodes) continue;
+    if (a.gnode) velocity_node<R, false>(a, n, tl, step);
+    else velocity_node<R, true>(a, n, tl, step);
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kTile) k_stress_batch(const StressArgs<typename Num<R>::S> *__restrict__ args,
+                                                        const int *__restrict__ tile_start, int n_members,
+                                                        int step) {
+  const int total = __ldg(tile_start + n_members);
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int m = member_of(tile_start, n_members, t);
+    const StressArgs<typename Num<R>::S> a = args[m];
+    const int tl = t - __ldg(tile_start + m);
+    const int c = tl * kTile + threadIdx.x;
+    if (c >= a.n_cells) continue;
+    if (a.gcell) stress_cell<R, false>(a, c, tl, step);
+    else stress_cell<R, true>(a, c, tl, step);
   }
 }
 
@@ -214,6 +272,18 @@ cudaError_t launch_str(const StressArgs<typename Num<R>::S> &a, int step, bool u
   const unsigned grid = (unsigned)((a.n_cells + kTile - 1) / kTile);
   if (uniform) k_stress<R, true><<<grid, kTile, 0, st>>>(a, step);
   else k_stress<R, false><<<grid, kTile, 0, st>>>(a, step);
+  return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_batch(const BatchLaunch &b, int step, cudaStream_t st) {
+  using S = typename Num<R>::S;
+  if (b.vel_tiles > 0)
+    k_velocity_batch<R><<<b.blocks_vel, kTile, 0, st>>>((const VelArgs<S> *)b.vel_args, b.vel_start,
+                                                         b.n_members, step);
+  if (b.str_tiles > 0)
+    k_stress_batch<R><<<b.blocks_str, kTile, 0, st>>>((const StressArgs<S> *)b.str_args, b.str_start,
+                                                       b.n_members, step);
   return cudaGetLastError();
 }
 
@@ -236,6 +306,11 @@ cudaError_t launch_velocity_df64(const VelArgs<float2> &a, int step, bool unifor
 }
 cudaError_t launch_stress_df64(const StressArgs<float2> &a, int step, bool uniform, cudaStream_t st) {
   return launch_str<df64>(a, step, uniform, st);
+}
+cudaError_t launch_table_batch(const BatchLaunch &b, int precision, int step, cudaStream_t st) {
+  if (precision == 2) return launch_batch<float>(b, step, st);
+  if (precision == 3) return launch_batch<df64>(b, step, st);
+  return launch_batch<double>(b, step, st);
 }
 
 }  // namespace pn

@@ -8,8 +8,11 @@
 // neighbouring tiles never see a half-updated step.
 //
 // A block owns a (TX-1) x (TY-1) column of cells and the same column of
-// nodes; its TX x TY threads are the nodes of the column plus a one-node
-// apron on the +x / +y side.  For each node layer k = 0..nz:
+// nodes over a chunk of cell layers [k0, k1) (blockIdx.z; chunks give the
+// GPU enough blocks on thin plates); its TX x TY threads are the nodes of the
+// column plus a one-node apron on the +x / +y side.  For each node layer
+// k = k0-1 .. k1 (layer k0-1 only seeds the partial sums, layer k1 is
+// recomputed for the stress of cell layer k1-1 and written by the next chunk):
 //   A  stage cell layer k of S_in (a (TX+1) x (TY+1) tile with a one-cell
 //      apron on the -x / -y side) in shared memory; issue the loads of layer
 //      k+1 into registers (software pipelining)
@@ -23,6 +26,7 @@
 //      partial sums over the corner velocities of node layers k-1 and k.
 // The apron node row/column is computed by both neighbouring tiles
 // (identical inputs, identical result) and written only by its owner.
+#include <algorithm>
 #include <cstdint>
 
 #include "df64.cuh"
@@ -71,8 +75,10 @@ __host__ __device__ constexpr bool c_used(int sym, int k, int j) {
                      (k == 3 && j == 4) || (k == 4 && j == 3));
 }
 
+// one block's work: tile (bx, by) of a grid with gxc tiles along x, z chunk bz
 template <typename R, int TX, int TY, int SYM>
-__global__ void __launch_bounds__(TX *TY) k_grid_step(const GridArgs<typename GNum<R>::S> a) {
+__device__ __forceinline__ void grid_block(const GridArgs<typename GNum<R>::S> &a, int bx, int by, int bz,
+                                           int gxc, int step) {
   using N = GNum<R>;
   using St = typename N::S;
   constexpr int NT = TX * TY;
@@ -84,8 +90,8 @@ __global__ void __launch_bounds__(TX *TY) k_grid_step(const GridArgs<typename GN
 
   const int t = threadIdx.x;
   const int tx = t % TX, ty = t / TX;
-  const int i0 = blockIdx.x * (TX - 1), j0 = blockIdx.y * (TY - 1);
-  const int blk = blockIdx.y * gridDim.x + blockIdx.x;
+  const int i0 = bx * (TX - 1), j0 = by * (TY - 1);
+  const int blk = by * gxc + bx;
   const int nx = a.nx, ny = a.ny, nz = a.nz;
   const int i = i0 + tx, j = j0 + ty;
   const bool node_in = (i <= nx) && (j <= ny);
@@ -95,6 +101,8 @@ __global__ void __launch_bounds__(TX *TY) k_grid_step(const GridArgs<typename GN
   const int64_t nidx0 = (int64_t)j * (nx + 1) + i;  // node index in its layer
   const int64_t cidx0 = (int64_t)j * nx + i;        // cell index in its layer
   const R gx = N::val(a.g[0]), gy = N::val(a.g[1]), gz = N::val(a.g[2]);
+  const St *sigrow = a.sigval ? a.sigval + (int64_t)min(step, a.sig_rows - 1) * a.sig_stride : nullptr;
+  const int64_t rec = a.rec + step;
 
   // staged cells of this thread: tile position and validity per layer
   int pf_off[PF];
@@ -111,13 +119,19 @@ __global__ void __launch_bounds__(TX *TY) k_grid_step(const GridArgs<typename GN
   auto issue = [&](int kc) {  // loads of cell layer kc (zeros outside)
 #pragma unroll
     for (int p = 0; p < PF; p++) {
-      const bool ok = pf_ok[p] && kc < nz;
+      const bool ok = pf_ok[p] && kc >= 0 && kc < nz;
       const int64_t g = ok ? (int64_t)kc * cplane + pf_off[p] : 0;  // in bounds either way
 #pragma unroll
       for (int f = 0; f < 6; f++) pf[p][f] = ok ? N::ld(a.S_in[f], g) : R();
     }
   };
-  issue(0);
+  // this block's chunk of the column: cell layers [k0, k1), node layers [k0, k1)
+  // (and node layer nz in the last chunk).  The march starts one cell layer
+  // below (its partial sums only) and recomputes node layer k1, which the next
+  // chunk owns, for the stress of cell layer k1-1.
+  const int k0 = bz * a.kchunk, k1 = min(nz, k0 + a.kchunk);
+  const bool last_chunk = k1 == nz;
+  issue(k0 - 1);
 
   // layer k-1 partial sums: velocity (per stress field) and stress (per V comp)
   R vpx0 = R(), vpx4 = R(), vpx5 = R(), vpy1 = R(), vpy3 = R(), vpy5 = R(), vs2 = R(), vs3 = R(),
@@ -126,8 +140,10 @@ __global__ void __launch_bounds__(TX *TY) k_grid_step(const GridArgs<typename GN
 #pragma unroll
   for (int c = 0; c < 3; c++) spx[c] = spy[c] = ss[c] = R();
 
-  for (int k = 0; k <= nz; k++) {
+  for (int k = k0 - 1; k <= k1; k++) {
     const int slot = (k + 1) % 3;  // cell layer k; layer -1 uses slot 0
+    const bool do_vel = k >= k0;                        // node layer k is computed
+    const bool own_layer = do_vel && (k < k1 || last_chunk);  // ... and written here
     St *Sk = sS + slot * 6 * CT;
     // ---- A: stage cell layer k, prefetch layer k+1
 #pragma unroll
@@ -138,9 +154,9 @@ __global__ void __launch_bounds__(TX *TY) k_grid_step(const GridArgs<typename GN
         for (int f = 0; f < 6; f++) Sk[f * CT + q] = N::sto(pf[p][f]);
       }
     }
-    if (k < nz) issue(k + 1);
+    if (k < k1) issue(k + 1);
     R vold[3], cf = R();
-    if (node_in) {
+    if (node_in && do_vel) {
       const int64_t n = (int64_t)k * nplane + nidx0;
       cf = N::ld(a.coef, n);
 #pragma unroll
@@ -175,12 +191,13 @@ __global__ void __launch_bounds__(TX *TY) k_grid_step(const GridArgs<typename GN
       R az = gx * (vpx4 + px4) + gy * (vpy3 + py3) + gz * (s2 - vs2);
       vpx0 = px0; vpx4 = px4; vpx5 = px5; vpy1 = py1; vpy3 = py3; vpy5 = py5;
       vs2 = s2; vs3 = s3; vs4 = s4;
+      if (do_vel) {
       if (a.f_rng) {  // force sources of this block and layer
         const int2 r = a.f_rng[(int64_t)blk * (nz + 1) + k];
         for (int e = r.x; e < r.y; e++) {
           const int key = a.f_key[e];
           if ((key & 0xffff) != t) continue;
-          const R v = N::val(a.f_w[e]) * N::val(a.sigval[a.f_sig[e]]);
+          const R v = N::val(a.f_w[e]) * N::val(sigrow[a.f_sig[e]]);
           const int d = key >> 16;
           if (d == 0) ax = ax + v;
           else if (d == 1) ay = ay + v;
@@ -195,26 +212,27 @@ __global__ void __launch_bounds__(TX *TY) k_grid_step(const GridArgs<typename GN
       }
 #pragma unroll
       for (int c = 0; c < 3; c++) Vk[c * NT + t] = N::sto(vn[c]);
-      if (node_own) {
+      if (node_own && own_layer) {
         const int64_t n = (int64_t)k * nplane + nidx0;
 #pragma unroll
         for (int c = 0; c < 3; c++) N::st(a.V_out[c], n, vn[c]);
-        if (a.s_rng) {  // sensor traces
+        if (a.s_rng && rec < a.rec_cap) {  // sensor traces
           const int2 r = a.s_rng[(int64_t)blk * (nz + 1) + k];
           for (int e = r.x; e < r.y; e++) {
             if (a.s_key[e] != t) continue;
-            double *tr = a.traces + ((int64_t)a.rec * a.n_sens + a.s_idx[e]) * 3;
+            double *tr = a.traces + (rec * a.n_sens + a.s_idx[e]) * 3;
             tr[0] = N::dbl(vn[0]);
             tr[1] = N::dbl(vn[1]);
             tr[2] = N::dbl(vn[2]);
           }
         }
       }
+      }  // do_vel
     }
     __syncthreads();
 
-    // ---- C: stress of cell layer k-1 (partial sums of node layer k always)
-    if (tx < TX - 1 && ty < TY - 1) {
+    // ---- C: stress of cell layer k-1 (partial sums of node layer k first)
+    if (do_vel && tx < TX - 1 && ty < TY - 1) {
       const int ia = t, ib = t + 1, ic = t + TX + 1, id = t + TX;
       R px[3], py[3], s[3];
 #pragma unroll
@@ -226,7 +244,7 @@ __global__ void __launch_bounds__(TX *TY) k_grid_step(const GridArgs<typename GN
         py[c] = cd - ab;
         s[c] = ab + cd;
       }
-      if (k >= 1 && cell_own) {
+      if (k > k0 && cell_own) {
         // d_ij = d/dx_i V_j over the cell of layer k-1
         const R d00 = spx[0] + px[0], d10 = spy[0] + py[0], d20 = s[0] - ss[0];
         const R d01 = spx[1] + px[1], d11 = spy[1] + py[1], d21 = s[1] - ss[1];
@@ -251,7 +269,7 @@ __global__ void __launch_bounds__(TX *TY) k_grid_step(const GridArgs<typename GN
           for (int ee = r.x; ee < r.y; ee++) {
             const int key = a.m_key[ee];
             if ((key & 0xffff) != t) continue;
-            const R v = N::val(a.m_w[ee]) * N::val(a.sigval[a.m_sig[ee]]);
+            const R v = N::val(a.m_w[ee]) * N::val(sigrow[a.m_sig[ee]]);
             const int kk = key >> 16;
 #pragma unroll
             for (int f = 0; f < 6; f++)
@@ -277,23 +295,93 @@ __global__ void __launch_bounds__(TX *TY) k_grid_step(const GridArgs<typename GN
 }
 
 template <typename R, int TX, int TY, int SYM>
-cudaError_t launch_t(const GridArgs<typename GNum<R>::S> &a, cudaStream_t st) {
-  using St = typename GNum<R>::S;
-  constexpr int CT = (TX + 1) * (TY + 1);
-  const size_t smem = sizeof(St) * (3 * 6 * CT + 2 * 3 * TX * TY);
-  static unsigned long long opted = 0;  // one opt-in per instantiation and device (< 64)
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  const unsigned long long bit = 1ull << (dev & 63);
-  if (!(opted & bit)) {
-    e = cudaFuncSetAttribute(k_grid_step<R, TX, TY, SYM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-    if (e != cudaSuccess) return e;
-    opted |= bit;
+__global__ void __launch_bounds__(TX *TY) k_grid_step(const GridArgs<typename GNum<R>::S> a, int step) {
+  grid_block<R, TX, TY, SYM>(a, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x, step);
+}
+
+// a batch of grid-form members: flat block ids over all members' (x, y, z)
+// block grids; block_start is the prefix of the members' block counts
+template <typename R, int TX, int TY, int SYM>
+__global__ void __launch_bounds__(TX *TY) k_grid_batch(const GridArgs<typename GNum<R>::S> *__restrict__ args,
+                                                       const int *__restrict__ block_start, int n_members,
+                                                       int step) {
+  const int id = blockIdx.x;
+  int lo = 0, hi = n_members;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(block_start + mid) <= id) lo = mid;
+    else hi = mid;
   }
-  const dim3 grid((unsigned)(a.nx / (TX - 1) + 1), (unsigned)(a.ny / (TY - 1) + 1));
-  k_grid_step<R, TX, TY, SYM><<<grid, TX * TY, smem, st>>>(a);
+  const GridArgs<typename GNum<R>::S> a = args[lo];
+  const int local = id - __ldg(block_start + lo);
+  const int gxc = a.nx / (TX - 1) + 1, gyc = a.ny / (TY - 1) + 1;
+  grid_block<R, TX, TY, SYM>(a, local % gxc, (local / gxc) % gyc, local / (gxc * gyc), gxc, step);
+}
+
+// per-instantiation, per-device set-up: shared-memory opt-in for the single
+// and batch kernels, SM count and resident blocks per SM
+template <typename R, int TX, int TY, int SYM>
+struct Setup {
+  using St = typename GNum<R>::S;
+  static constexpr int CT = (TX + 1) * (TY + 1);
+  static constexpr size_t smem = sizeof(St) * (3 * 6 * CT + 2 * 3 * TX * TY);
+  static cudaError_t ensure(int &sms, int &per_sm) {
+    static unsigned long long done = 0;
+    static int s_sms[64] = {0}, s_per[64] = {0};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const int d = dev & 63;
+    if (!(done & (1ull << d))) {
+      e = cudaFuncSetAttribute(k_grid_step<R, TX, TY, SYM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem);
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_grid_batch<R, TX, TY, SYM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+      if (e == cudaSuccess) e = cudaDeviceGetAttribute(&s_sms[d], cudaDevAttrMultiProcessorCount, dev);
+      if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s_per[d], k_grid_step<R, TX, TY, SYM>, TX * TY, smem);
+      if (e != cudaSuccess) return e;
+      s_per[d] = s_per[d] > 0 ? s_per[d] : 1;
+      done |= 1ull << d;
+    }
+    sms = s_sms[d];
+    per_sm = s_per[d];
+    return cudaSuccess;
+  }
+};
+
+// cell layers per z chunk: about four waves of blocks, at least four layers
+inline int chunk_layers(int nz, long long xy_blocks, int sms, int per_sm) {
+  const long long want = 4LL * sms * per_sm;
+  long long chunks = (want + xy_blocks - 1) / xy_blocks;
+  chunks = std::max(1LL, std::min(chunks, (long long)std::max(1, nz / 4)));
+  return (int)((nz + chunks - 1) / chunks);
+}
+
+template <typename R, int TX, int TY, int SYM>
+cudaError_t launch_t(const GridArgs<typename GNum<R>::S> &a, cudaStream_t st) {
+  using S = Setup<R, TX, TY, SYM>;
+  int sms = 0, per_sm = 0;
+  cudaError_t e = S::ensure(sms, per_sm);
+  if (e != cudaSuccess) return e;
+  GridArgs<typename GNum<R>::S> b = a;
+  const unsigned gx = (unsigned)(a.nx / (TX - 1) + 1), gy = (unsigned)(a.ny / (TY - 1) + 1);
+  if (b.kchunk <= 0) b.kchunk = chunk_layers(a.nz, (long long)gx * gy, sms, per_sm);
+  const dim3 grid(gx, gy, (unsigned)((a.nz + b.kchunk - 1) / b.kchunk));
+  k_grid_step<R, TX, TY, SYM><<<grid, TX * TY, S::smem, st>>>(b, 0);
+  return cudaGetLastError();
+}
+
+template <typename R, int TX, int TY, int SYM>
+cudaError_t launch_batch_t(const GridBatchLaunch &b, int step, cudaStream_t st) {
+  using S = Setup<R, TX, TY, SYM>;
+  int sms = 0, per_sm = 0;
+  cudaError_t e = S::ensure(sms, per_sm);
+  if (e != cudaSuccess) return e;
+  if (b.total_blocks <= 0) return cudaSuccess;
+  k_grid_batch<R, TX, TY, SYM><<<b.total_blocks, TX * TY, S::smem, st>>>(
+      (const GridArgs<typename GNum<R>::S> *)b.args, b.block_start, b.n_members, step);
   return cudaGetLastError();
 }
 
@@ -305,10 +393,27 @@ cudaError_t launch_sym(const GridArgs<typename GNum<R>::S> &a, int sym, cudaStre
   return launch_t<R, 32, 8, 0>(a, st);
 }
 
+template <typename R>
+cudaError_t launch_batch_sym(const GridBatchLaunch &b, int step, cudaStream_t st) {
+  if (b.sym == 2) return launch_batch_t<R, 32, 8, 2>(b, step, st);
+  if (b.sym == 1) return launch_batch_t<R, 32, 8, 1>(b, step, st);
+  return launch_batch_t<R, 32, 8, 0>(b, step, st);
+}
+
 }  // namespace
 
 int grid_tile_x() { return 32; }
 int grid_tile_y() { return 8; }
+
+int grid_chunk_layers(int precision, int nx, int ny, int nz) {
+  int sms = 0, per_sm = 0;
+  cudaError_t e = precision == 2 ? Setup<float, 32, 8, 0>::ensure(sms, per_sm)
+                : precision == 3 ? Setup<df64, 32, 8, 0>::ensure(sms, per_sm)
+                                 : Setup<double, 32, 8, 0>::ensure(sms, per_sm);
+  if (e != cudaSuccess || nz <= 0) return nz > 0 ? nz : 1;
+  const long long xy = (long long)(nx / 31 + 1) * (ny / 7 + 1);
+  return chunk_layers(nz, xy, sms, per_sm);
+}
 
 cudaError_t launch_grid_f32(const GridArgs<float> &a, int sym, cudaStream_t st) {
   return launch_sym<float>(a, sym, st);
@@ -318,6 +423,11 @@ cudaError_t launch_grid_f64(const GridArgs<double> &a, int sym, cudaStream_t st)
 }
 cudaError_t launch_grid_df64(const GridArgs<float2> &a, int sym, cudaStream_t st) {
   return launch_sym<df64>(a, sym, st);
+}
+cudaError_t launch_grid_batch(const GridBatchLaunch &b, int precision, int step, cudaStream_t st) {
+  if (precision == 2) return launch_batch_sym<float>(b, step, st);
+  if (precision == 3) return launch_batch_sym<df64>(b, step, st);
+  return launch_batch_sym<double>(b, step, st);
 }
 
 }  // namespace pn

@@ -15,6 +15,7 @@ namespace pn {
 template <typename T>
 struct GridArgs {
   int32_t nx, ny, nz;  // cells per axis
+  int32_t kchunk;      // cell layers per block along z (set by the launcher when 0)
   const T *V_in[3];
   T *V_out[3];
   const T *S_in[6];
@@ -33,18 +34,34 @@ struct GridArgs {
   const int32_t *m_key;  // local cell | Voigt component << 16
   const int32_t *m_sig;
   const T *m_w;          // weights carry dt
-  const T *sigval;       // signal values of this step
+  const T *sigval;       // signal rows: row min(step, sig_rows-1) at stride sig_stride
+  int32_t sig_stride;    // 0 when sigval already points at the step's row
+  int32_t sig_rows;
   // sensors, ranges per (block, node layer)
   const int2 *s_rng;
   const int32_t *s_key;  // local node
   const int32_t *s_idx;  // sensor number
   double *traces;        // [records][n_sens][3]
   int32_t n_sens;
-  int64_t rec;           // record written by this step
+  int64_t rec;           // record written by step 0 of the launch (rec + step later)
+  int64_t rec_cap;       // records beyond this are not written
 };
 
 int grid_tile_x();
 int grid_tile_y();
+// cell layers per z chunk the launcher picks for this lattice and precision
+int grid_chunk_layers(int precision, int nx, int ny, int nz);
+
+// a batch of grid-form members: argument blocks (kchunk set) and the prefix
+// of their block counts ((nx/(TX-1)+1) * (ny/(TY-1)+1) * chunks each)
+struct GridBatchLaunch {
+  int n_members;
+  const void *args;        // GridArgs<S>[n_members]
+  const int *block_start;  // [n_members + 1]
+  int total_blocks;
+  int sym;                 // most general symmetry class among the members
+};
+cudaError_t launch_grid_batch(const GridBatchLaunch &b, int precision, int step, cudaStream_t st);
 cudaError_t launch_grid_f32(const GridArgs<float> &a, int sym, cudaStream_t st);
 cudaError_t launch_grid_f64(const GridArgs<double> &a, int sym, cudaStream_t st);
 cudaError_t launch_grid_df64(const GridArgs<float2> &a, int sym, cudaStream_t st);

@@ -179,3 +179,50 @@ class Solver:
 
     def synchronize(self):
         N.check(self._lib.pn_solver_synchronize(self._h))
+
+
+class Batch:
+    """Solvers advanced together by shared launches (pn_batch_*).
+
+    Members keep their own state, sources, sensors and time; a member's
+    results are the same alone and in the batch.  The batch does not own its
+    members."""
+
+    def __init__(self):
+        self._lib = N.load()
+        h = c_void_p()
+        N.check(self._lib.pn_batch_create(ctypes.byref(h)))
+        self._h = h
+        self.members = []
+
+    def add(self, solver: Solver):
+        N.check(self._lib.pn_batch_add(self._h, solver._h))
+        self.members.append(solver)
+
+    def remove(self, solver: Solver):
+        N.check(self._lib.pn_batch_remove(self._h, solver._h))
+        self.members.remove(solver)
+
+    def set_stream(self, stream):
+        handle = getattr(stream, "cuda_stream", stream)
+        N.check(self._lib.pn_batch_set_stream(self._h, c_void_p(handle or 0)))
+
+    def solve(self, nsteps: int):
+        N.check(self._lib.pn_batch_solve(self._h, int(nsteps)))
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.pn_batch_destroy(self._h)
+            self._h = c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -31,6 +31,28 @@ def build_and_run(tmp_path):
     return r.stdout
 
 
+def test_runner_statements_compile_unchanged_with_standins(tmp_path):
+    """The runners' model-building lines, verbatim, build the device solver when
+    include/standin precedes the HostSolver headers."""
+    if not (REF / "modules" / "HostSolver" / "include" / "HostRSGTDUT.hpp").exists():
+        pytest.skip("reference headers not present")
+    exe = tmp_path / "standin_check"
+    inc = ["-I", str(ROOT / "include" / "standin"), "-I", str(ROOT / "include")]
+    for m in ("PanNDE", "HostData", "Stubs", "HostSolver"):
+        inc += ["-I", str(REF / "modules" / m / "include")]
+    cmd = ["g++", "-std=c++14", "-O1", "-w", *inc, str(ROOT / "tests" / "cxx" / "standin_check.cpp"),
+           "-L", str(LIB), "-lpannde_gb300", f"-Wl,-rpath,{LIB}", "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    tag = r.stdout.split()[0]
+    assert tag in ("no-device", "ran"), r.stdout
+    if tag == "ran":
+        f = r.stdout.split()
+        assert int(f[1]) == int(f[2]) and float(f[3]) != 0.0 and float(f[4]) != 0.0
+
+
 def test_adapter_builds_against_reference_and_runs(tmp_path):
     out = build_and_run(tmp_path)
     lines = out.strip().splitlines()
