@@ -62,6 +62,12 @@ def parse():
     p.add_argument("--no-fp32", action="store_true")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--no-batch", action="store_true", help="skip the batched-brackets leg")
+    p.add_argument("--batch-members", type=int, default=96)
+    p.add_argument("--batch-sample-steps", type=int, default=300)
+    p.add_argument("--no-serving", action="store_true", help="skip the serving leg")
+    p.add_argument("--serving-requests", type=int, default=12)
+    p.add_argument("--serving-rate", type=float, default=1.0, help="Poisson arrivals per second")
     return p.parse_args()
 
 
@@ -259,6 +265,84 @@ def e2e_run(case, prec, steps, torch):
     return (t1 - t0), h2d, d2h
 
 
+def batch_leg(n_members, sample_steps, torch, steps_total=3000):
+    """Batched sims/hour: n_members seeded L-brackets (legs 60-220 cells, 12-30
+    thick, 40-160 deep, 0.1 mm voxels, a 1-6 mm crack at the inner fillet as
+    disconnected faces; every sixth with an acoustic-fluid column and a
+    pressure source, the others a z-force transducer), FP32, 3000 steps each,
+    advanced together by pn_batch_solve (one launch per kernel per step for
+    all members).  A sample of the steps is timed with CUDA events on the
+    batch's stream; the per-step cost does not change along the run."""
+    from pannde_gb300 import cases
+    from pannde_gb300.solver import Batch, Solver
+    warm = 5
+    t0 = time.perf_counter()
+    cs = [cases.bracket_case(1000 + i, nsteps=steps_total, water_column=(i % 6 == 0)) for i in range(n_members)]
+    solvers = [Solver.from_case(c, precision="f32", capacity=warm + sample_steps) for c in cs]
+    setup_s = time.perf_counter() - t0
+    cells = sum(c.mesh.n_cells for c in cs)
+    forms = sorted({s.info()["form_name"] for s in solvers})
+    with Batch() as b:
+        for s in solvers:
+            b.add(s)
+        stream = torch.cuda.Stream()
+        b.set_stream(stream)
+        b.solve(warm)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.solve(sample_steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+    for s in solvers:
+        s.close()
+    per_step_s = ms * 1e-3 / sample_steps
+    return {"sims_per_hour": round(n_members / (per_step_s * steps_total) * 3600.0, 1),
+            "gcell_steps_per_s": round(cells / per_step_s / 1e9, 4),
+            "members": n_members, "cells_total": cells, "steps_per_sim": steps_total,
+            "timed_steps": sample_steps, "ms_per_batch_step": round(ms / sample_steps, 4),
+            "dtype": "f32", "form": ",".join(forms), "setup_s": round(setup_s, 1),
+            "workload": f"{n_members} seeded L-brackets with a disconnected-face crack, every sixth with a "
+                        "water column (pressure source), FP32, one pn_batch_solve over all members"}
+
+
+def serving_leg(n_requests, rate, torch, seed=7):
+    """Serving: Poisson arrivals (rate per second, seeded); each request an
+    aluminium or laminate plate, cells log-uniform 0.2 M - 20 M, transducer
+    position, 0.25-2 MHz, +-5% stiffness, 1000-8000 steps.  Continuous
+    batching in FP32 (pannde_gb300.serving.Server) against the same requests
+    solved one after another (no batching); every fourth request re-solved in
+    the double-float FP64-class form as a spot check of the FP32 traces."""
+    from pannde_gb300 import serving
+    from pannde_gb300.solver import Solver
+    t0 = time.perf_counter()
+    reqs = serving.poisson_requests(n_requests, rate, seed)
+    gen_s = time.perf_counter() - t0
+    free, _ = torch.cuda.mem_get_info()
+    srv = serving.Server(hbm_budget_bytes=int(0.7 * free), precision="f32", quantum=250)
+    res, st = srv.run(reqs)
+    seq, sst = serving.run_sequential(reqs, precision="f32")
+    errs = []
+    for r in res[::4]:
+        q = reqs[r.rid]
+        with Solver.from_case(q.case, precision="df64", capacity=q.nsteps) as s:
+            s.solve(q.nsteps)
+            ref = s.traces()
+        d = np.linalg.norm(ref)
+        errs.append(float(np.linalg.norm(r.traces - ref) / (d if d > 0 else 1.0)))
+    return {"sims_per_hour": round(st["sims_per_hour"], 1), "p50_s": round(st["p50_s"], 3),
+            "p99_s": round(st["p99_s"], 3), "gcell_steps_per_s": round(st["gcell_steps_per_s"], 3),
+            "max_in_flight": st["max_active"], "requests": st["requests"], "rate_per_s": rate,
+            "sequential": {"sims_per_hour": round(sst["sims_per_hour"], 1), "p50_s": round(sst["p50_s"], 3),
+                           "p99_s": round(sst["p99_s"], 3)},
+            "fp32_vs_double_float_trace_rel_l2_max": max(errs) if errs else None,
+            "spot_checks": len(errs), "request_generation_s": round(gen_s, 1),
+            "workload": "Poisson arrivals; Al or laminate plates 0.2-20 M cells (log-uniform), "
+                        "1000-8000 steps, 0.25-2 MHz; FP32 continuous batching, latency = arrival to traces"}
+
+
 def cpu_reference(case, budget_s):
     """The CPU implementation on a bounded sample of the workload (all threads)."""
     import oracle
@@ -364,6 +448,10 @@ def main():
                        "d2h_bytes_per_step": int(d2h / args.steps),
                        "how": "pn_solver_set_state from pinned host, one pn_solver_solve per step, "
                               "pn_solver_get_traces + pn_solver_get_state to pinned host; wall clock"}
+        if ws == 1 and not args.no_batch:
+            line["batch"] = batch_leg(args.batch_members, args.batch_sample_steps, torch)
+        if ws == 1 and not args.no_serving:
+            line["serving"] = serving_leg(args.serving_requests, args.serving_rate, torch)
         if ws == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_reference(case, args.cpu_seconds)
         print(json.dumps(line))

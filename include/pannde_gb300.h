@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define PN_ABI_VERSION 1
+#define PN_ABI_VERSION 2
 
 /* ---- status codes ------------------------------------------------------ */
 enum pn_status {
@@ -197,6 +197,7 @@ typedef struct pn_solver_info {
   double time;
   int32_t form;              /* PN_FORM_TABLE or PN_FORM_GRID */
   int32_t grid[3];           /* grid form: cells per axis */
+  int32_t grid_kernel;       /* grid form: 1 classic (register prefetch), 2 tensor-copy staging; 0 table */
 } pn_solver_info;
 
 /* What pn_solver_create would build, computed on the host only. */

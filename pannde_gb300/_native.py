@@ -12,6 +12,7 @@ from pathlib import Path
 import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "_build" / "libpannde_gb300.so"
+ABI_VERSION = 2  # PN_ABI_VERSION of include/pannde_gb300.h these declarations follow
 
 # status codes (enum pn_status)
 PN_OK = 0
@@ -87,7 +88,8 @@ class PnSolverInfo(ctypes.Structure):
                 ("n_materials", c_int32), ("uniform_spacing", c_int32),
                 ("n_source_nodes", c_int32), ("n_source_cells", c_int32), ("n_sensors", c_int32),
                 ("algorithmic_bytes_per_step", c_int64), ("device_bytes", c_int64),
-                ("dt", c_double), ("time", c_double), ("form", c_int32), ("grid", c_int32 * 3)]
+                ("dt", c_double), ("time", c_double), ("form", c_int32), ("grid", c_int32 * 3),
+                ("grid_kernel", c_int32)]
 
 
 class PnPlan(ctypes.Structure):
@@ -169,6 +171,8 @@ def load(path: Path | None = None):
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
+    if lib.pn_abi_version() != ABI_VERSION:
+        raise ExtensionMissing(f"{p} has ABI {lib.pn_abi_version()}, expected {ABI_VERSION}: rebuild it")
     if path is None:
         _lib = lib
     return lib

@@ -393,7 +393,7 @@ def disconnect_face(mesh: HexMesh, cells_above: np.ndarray, node_mask: np.ndarra
 
 
 def bracket_case(seed: int, h=0.1e-3, nsteps=3000, water_column=False, n_sensors=8,
-                 scale=1.0, name="bracket") -> Case:
+                 scale=1.0, name="bracket", crack="faces") -> Case:
     """Aluminium L-section angle bracket with a seeded planar crack at the inner fillet.
 
     Cross-section in (y, z): a vertical leg (y < t) and a horizontal leg (z < t),
@@ -401,7 +401,10 @@ def bracket_case(seed: int, h=0.1e-3, nsteps=3000, water_column=False, n_sensors
     geometry[:, :t, :] = geometry[:, :, :t] = 1).  Leg lengths 60-220 cells, thickness
     12-30 cells, depth 40-160 cells, drawn from the seed (scale shrinks them for tests).
     The crack lies in the plane z = t under the vertical leg, opening at the inner
-    face y = t, 1-6 mm long along x, as disconnected faces.  With water_column, a
+    face y = t, 1-6 mm long along x: crack="faces" makes it disconnected faces
+    (duplicated nodes), crack="slab" removes a 150 um slab of cells there instead
+    (the construction of Bracket_Crack...py:52-66; the mesh stays a voxel
+    lattice).  With water_column, a
     cylinder of fluid cells (rho 1000, c 1480 m/s) stands on the horizontal leg's top
     face and the excitation is a pressure (xx, yy, zz moment) window at its top;
     otherwise a z-force transducer acts on the horizontal leg's outer face."""
@@ -426,18 +429,24 @@ def bracket_case(seed: int, h=0.1e-3, nsteps=3000, water_column=False, n_sensors
             fluid[:, :, k] |= disk
         fluid &= ~solid
         solid |= fluid
-    mesh = voxel_mesh(solid, h)
-    ci, cj, ck = mesh.cell_ijk[:, 0], mesh.cell_ijk[:, 1], mesh.cell_ijk[:, 2]
-    cell_material = fluid[ci, cj, ck].astype(np.int32)
     # crack: plane z = t, x in (x0, x0 + c), y in (t - cw, t], under the vertical leg
     c_len = max(2, int(round(rng.uniform(1e-3, 6e-3) / h * min(1.0, scale * 2))))
     c_len = min(c_len, d - 2)
     cw = max(1, min(t - 1, int(round(rng.uniform(0.2, 0.6) * t))))
     x0 = int(rng.integers(1, max(2, d - c_len)))
-    ni, nj, nk = mesh.node_ijk[:, 0], mesh.node_ijk[:, 1], mesh.node_ijk[:, 2]
-    on_face = (nk == t) & (ni > x0) & (ni < x0 + c_len) & (nj > t - cw) & (nj <= t)
-    above = np.flatnonzero((ck >= t) & (cj < t) & (cell_material == 0))
-    mesh = disconnect_face(mesh, above, on_face)
+    if crack == "slab":
+        slab = max(1, int(round(150e-6 / h)))
+        solid[x0:x0 + c_len, t - cw:t, t:min(t + slab, lz)] = False
+    mesh = voxel_mesh(solid, h)
+    ci, cj, ck = mesh.cell_ijk[:, 0], mesh.cell_ijk[:, 1], mesh.cell_ijk[:, 2]
+    cell_material = fluid[ci, cj, ck].astype(np.int32)
+    if crack == "faces":
+        ni, nj, nk = mesh.node_ijk[:, 0], mesh.node_ijk[:, 1], mesh.node_ijk[:, 2]
+        on_face = (nk == t) & (ni > x0) & (ni < x0 + c_len) & (nj > t - cw) & (nj <= t)
+        above = np.flatnonzero((ck >= t) & (cj < t) & (cell_material == 0))
+        mesh = disconnect_face(mesh, above, on_face)
+    elif crack != "slab":
+        raise ValueError(f"crack must be 'faces' or 'slab', not {crack!r}")
     c_al = isotropic(ALUMINIUM["E"], ALUMINIUM["nu"])
     rho_al = ALUMINIUM["rho"]
     c_w = fluid_stiffness(WATER["rho"], WATER["c"])
@@ -454,5 +463,5 @@ def bracket_case(seed: int, h=0.1e-3, nsteps=3000, water_column=False, n_sensors
     sens = np.sort(rng.choice(outer, size=min(n_sensors, outer.size), replace=False)).astype(np.int32)
     return Case(f"{name}-{seed}", mesh, np.array([rho_al, WATER["rho"]]),
                 np.stack([c21_from_6x6(c_al), c21_from_6x6(c_w)]), cell_material, dt, src, sens, nsteps,
-                dict(ly=ly, lz=lz, t=t, d=d, crack=(x0, c_len, cw), water_column=water_column, h=h,
-                     freq=freq))
+                dict(ly=ly, lz=lz, t=t, d=d, crack=(x0, c_len, cw), crack_kind=crack,
+                     water_column=water_column, h=h, freq=freq))

@@ -151,6 +151,8 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision) {
   std::vector<int> bs(n + 1, 0);
   const int tx = pn::grid_tile_x(), ty = pn::grid_tile_y();
   int sym = 2;
+  bool tma = true;  // the tensor-copy kernel when every member has its maps
+  for (pn_solver *s : b->members) tma = tma && s->d_tmaps != nullptr;
   int32_t done = 0;
   while (done < nsteps) {
     const int32_t chunk = common_chunk(b, nsteps - done);
@@ -166,10 +168,11 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision) {
         a.sig_rows = (int32_t)(s->sig_rows - row0);
       }
       a.rec = s->rec_count;
-      a.kchunk = pn::grid_chunk_layers(precision, a.nx, a.ny, a.nz);
+      a.kchunk = pn::grid_chunk_layers(precision, a.nx, a.ny, a.nz, tma);
       for (int p = 0; p < 2; p++) {  // step parity: buffers swap every step
         pn::GridArgs<T> q = a;
         const int in = s->cur ^ p, out = in ^ 1;
+        q.tmaps = tma ? pn::grid_maps_for(s, in) : nullptr;
         for (int c = 0; c < 3; c++) {
           q.V_in[c] = (const T *)s->V[in][c];
           q.V_out[c] = (T *)s->V[out][c];
@@ -198,7 +201,9 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision) {
       L.block_start = b->d_start[0];
       L.total_blocks = bs[n];
       L.sym = sym;
-      pn::ck(pn::launch_grid_batch(L, precision, k, b->stream), "batch step");
+      pn::ck(tma ? pn::launch_grid_tma_batch(L, precision, k, b->stream)
+                 : pn::launch_grid_batch(L, precision, k, b->stream),
+             "batch step");
     }
     pn::ck(cudaStreamSynchronize(b->stream), "batch chunk");
     advance(b, chunk);
@@ -285,6 +290,8 @@ int pn_batch_synchronize(pn_batch *b) {
     if (!b) return berr(PN_ERR_INVALID, "null batch");
     pn::ck(cudaStreamSynchronize(b->stream), "batch sync");
     pn::ck(cudaGetLastError(), "device error");
+    for (pn_solver *m : b->members)
+      if (const int rc = pn::device_check(m)) return rc;
     return PN_OK;
   });
 }

@@ -379,6 +379,16 @@ int pn_solver_set_sensors(pn_solver *s, const int32_t *nodes, int32_t n, int32_t
 namespace pn {
 int set_last_error(int code, const std::string &msg) { return set_err(code, msg); }
 
+int device_check(pn_solver *s) {
+  if (!s->d_err) return PN_OK;
+  int32_t v = 0;
+  ck(cudaMemcpy(&v, s->d_err, sizeof(v), cudaMemcpyDeviceToHost), "error word");
+  if (v == 0) return PN_OK;
+  ck(cudaMemset(s->d_err, 0, sizeof(v)), "error word");
+  return set_err(PN_ERR_DEVICE_CHECK,
+                 "grid step: a wait for staged tiles gave up after 1 s; the state of this solver is invalid");
+}
+
 void refresh_sources(pn_solver *s) {
   if (!s->src_dirty) return;
   if (s->form == PN_FORM_GRID) grid_sources(s);
@@ -454,6 +464,7 @@ int pn_solver_get_state(pn_solver *s, double *const *V, double *const *S) {
   return guarded([&]() -> int {
     if (!s) return set_err(PN_ERR_INVALID, "null solver");
     pn::ck(cudaStreamSynchronize(s->stream), "get_state sync");
+    if (const int rc = pn::device_check(s)) return rc;
     if (s->form == PN_FORM_GRID) pn::grid_get_state(s, V, S);
     else pn::table_get_state(s, V, S);
     return PN_OK;
@@ -465,6 +476,7 @@ int pn_solver_get_traces(pn_solver *s, double *out, int64_t max_records, int64_t
     if (!s) return set_err(PN_ERR_INVALID, "null solver");
     if (max_records < 0 || (max_records > 0 && !out)) return set_err(PN_ERR_INVALID, "trace buffer");
     pn::ck(cudaStreamSynchronize(s->stream), "get_traces sync");
+    if (const int rc = pn::device_check(s)) return rc;
     const int64_t have = std::min(s->rec_count, s->rec_cap);
     const int64_t n = std::min(have, max_records);
     if (n > 0 && s->n_sens > 0)
@@ -506,6 +518,7 @@ int pn_solver_get_info(pn_solver *s, pn_solver_info *info) {
     info->grid[0] = s->grid.nx;
     info->grid[1] = s->grid.ny;
     info->grid[2] = s->grid.nz;
+    info->grid_kernel = s->d_tmaps ? 2 : 1;
   }
   return PN_OK;
 }
@@ -522,7 +535,7 @@ int pn_solver_synchronize(pn_solver *s) {
     if (!s) return set_err(PN_ERR_INVALID, "null solver");
     pn::ck(cudaStreamSynchronize(s->stream), "synchronize");
     pn::ck(cudaGetLastError(), "device error");
-    return PN_OK;
+    return pn::device_check(s);
   });
 }
 

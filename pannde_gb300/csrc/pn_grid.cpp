@@ -3,6 +3,7 @@
 // double-buffered state.  Host arrays stay in the caller's numbering; the
 // device holds the lattice numbering (x fastest) and this file maps between.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <type_traits>
@@ -56,16 +57,16 @@ Tiles tiles_of(const GridMap &g) {
 }
 
 void node_ijk(const GridMap &g, int64_t q, int64_t &i, int64_t &j, int64_t &k) {
-  const int64_t w = g.nx + 1, h = g.ny + 1;
+  const int64_t w = g.pnx, h = g.ny + 1;
   i = q % w;
   j = (q / w) % h;
   k = q / (w * h);
 }
 
 void cell_ijk(const GridMap &g, int64_t q, int64_t &i, int64_t &j, int64_t &k) {
-  i = q % g.nx;
-  j = (q / g.nx) % g.ny;
-  k = q / ((int64_t)g.nx * g.ny);
+  i = q % g.pcx;
+  j = (q / g.pcx) % g.ny;
+  k = q / ((int64_t)g.pcx * g.ny);
 }
 
 // 2: only the C11..C33 block and the shear diagonal; 1: monoclinic about z;
@@ -116,13 +117,24 @@ bool grid_eligible(const MeshTables &m, const MaterialTables &mt, int precision,
 
 int64_t grid_footprint(const GridMap &g, const MaterialTables &mt, int precision) {
   const int64_t e = precision == PN_PREC_F32 ? 4 : 8;
-  const int64_t gn = g.grid_nodes(), gc = g.grid_cells();
-  return 2 * (3 * gn + 6 * gc) * e + gn * e + gc + (int64_t)(mt.n_mat + 1) * 36 * e;
+  const int64_t gn = g.node_sites(), gc = g.cell_sites();
+  return 2 * (3 * gn + 6 * gc) * e + gn * e + gc + (int64_t)(mt.n_mat + 1) * 36 * e +
+         2 * (int64_t)grid_tma_maps_bytes() + 16;
+}
+
+// The tensor-copy kernel (rsg_grid_tma.cu) runs when the stiffness table fits
+// its shared-memory rows and every buffer meets the copy rules; otherwise the
+// classic kernel (rsg_grid.cu).  PN_GRID_KERNEL=classic selects the classic
+// kernel for comparisons.
+static bool want_tma(const pn_solver *s) {
+  const char *v = std::getenv("PN_GRID_KERNEL");
+  if (v && std::strcmp(v, "classic") == 0) return false;
+  return s->mat.n_mat + 1 <= kGridTmaRowsMax;
 }
 
 void grid_create(pn_solver *s) {
   const GridMap &g = s->grid;
-  const int64_t gn = g.grid_nodes(), gc = g.grid_cells();
+  const int64_t gn = g.node_sites(), gc = g.cell_sites();
   const size_t e = s->esz;
   for (int b = 0; b < 2; b++) {
     for (int k = 0; k < 3; k++) {
@@ -148,44 +160,62 @@ void grid_create(pn_solver *s) {
   s->upload_real(s->d_ctab, ct.data(), ct.size());
   s->sym = symmetry_class(s->mat);
   s->cur = 0;
+  s->d_err = s->alloc<int32_t>(16);
+  ck(cudaMemsetAsync(s->d_err, 0, 16, s->stream), "memset");
+  if (want_tma(s)) {
+    const size_t mb = grid_tma_maps_bytes();
+    std::vector<unsigned char> maps(2 * mb);
+    bool ok = true;
+    for (int p = 0; p < 2 && ok; p++) {
+      const void *V[3] = {s->V[p][0], s->V[p][1], s->V[p][2]};
+      const void *S[6] = {s->S[p][0], s->S[p][1], s->S[p][2], s->S[p][3], s->S[p][4], s->S[p][5]};
+      ok = grid_tma_encode(s->precision, g.nx, g.ny, g.nz, g.pnx, g.pcx, V, S, s->d_coef, s->d_gmat,
+                           maps.data() + p * mb);
+    }
+    if (ok) {
+      s->d_tmaps = s->alloc<void>(2 * mb);
+      s->upload_raw(s->d_tmaps, maps.data(), 2 * mb);
+    }
+  }
   ck(cudaStreamSynchronize(s->stream), "create sync");
 }
 
+// node / cell -> lattice position maps on the device (first transfer)
+static void ensure_grid_maps(pn_solver *s) {
+  const GridMap &g = s->grid;
+  if (!s->d_nmap) {
+    s->d_nmap = s->alloc<int64_t>(g.node_grid.size() * sizeof(int64_t));
+    s->upload_raw(s->d_nmap, g.node_grid.data(), g.node_grid.size() * sizeof(int64_t));
+  }
+  if (!s->d_cmap) {
+    s->d_cmap = s->alloc<int64_t>(g.cell_grid.size() * sizeof(int64_t));
+    s->upload_raw(s->d_cmap, g.cell_grid.data(), g.cell_grid.size() * sizeof(int64_t));
+  }
+}
+
+// The lattice buffers are cleared (void sites stay zero) and the caller's
+// fields scattered to their lattice positions on the device (rsg_state.cu).
 void grid_put_state(pn_solver *s, const double *const *V, const double *const *S) {
   const GridMap &g = s->grid;
-  const int64_t gn = g.grid_nodes(), gc = g.grid_cells();
-  std::vector<double> buf;
+  const int64_t gn = g.node_sites(), gc = g.cell_sites();
+  ensure_grid_maps(s);
   for (int k = 0; k < 3; k++) {
-    buf.assign((size_t)gn, 0.0);
-    if (V && V[k])
-      for (int32_t u = 0; u < s->mesh.n_nodes; u++) buf[g.node_grid[u]] = V[k][u];
-    s->upload_real(s->V[s->cur][k], buf.data(), buf.size());
-    ck(cudaStreamSynchronize(s->stream), "put_state");
+    ck(cudaMemsetAsync(s->V[s->cur][k], 0, (size_t)gn * s->esz, s->stream), "memset");
+    if (V && V[k]) s->put_field(s->V[s->cur][k], V[k], (size_t)s->mesh.n_nodes, s->d_nmap);
   }
   for (int k = 0; k < 6; k++) {
-    buf.assign((size_t)gc, 0.0);
-    if (S && S[k])
-      for (int32_t c = 0; c < s->mesh.n_cells; c++) buf[g.cell_grid[c]] = S[k][c];
-    s->upload_real(s->S[s->cur][k], buf.data(), buf.size());
-    ck(cudaStreamSynchronize(s->stream), "put_state");
+    ck(cudaMemsetAsync(s->S[s->cur][k], 0, (size_t)gc * s->esz, s->stream), "memset");
+    if (S && S[k]) s->put_field(s->S[s->cur][k], S[k], (size_t)s->mesh.n_cells, s->d_cmap);
   }
 }
 
 void grid_get_state(pn_solver *s, double *const *V, double *const *S) {
-  const GridMap &g = s->grid;
-  std::vector<double> buf;
-  for (int k = 0; k < 3; k++) {
-    if (!V || !V[k]) continue;
-    buf.resize((size_t)g.grid_nodes());
-    s->download_real(buf.data(), s->V[s->cur][k], buf.size());
-    for (int32_t u = 0; u < s->mesh.n_nodes; u++) V[k][u] = buf[g.node_grid[u]];
-  }
-  for (int k = 0; k < 6; k++) {
-    if (!S || !S[k]) continue;
-    buf.resize((size_t)g.grid_cells());
-    s->download_real(buf.data(), s->S[s->cur][k], buf.size());
-    for (int32_t c = 0; c < s->mesh.n_cells; c++) S[k][c] = buf[g.cell_grid[c]];
-  }
+  ensure_grid_maps(s);
+  for (int k = 0; k < 3; k++)
+    if (V && V[k]) s->get_field(V[k], s->V[s->cur][k], (size_t)s->mesh.n_nodes, s->d_nmap);
+  for (int k = 0; k < 6; k++)
+    if (S && S[k]) s->get_field(S[k], s->S[s->cur][k], (size_t)s->mesh.n_cells, s->d_cmap);
+  ck(cudaStreamSynchronize(s->stream), "get_state");
 }
 
 void grid_sources(pn_solver *s) {
@@ -279,6 +309,8 @@ void grid_args(pn_solver *s, GridArgs<T> &a) {
   a.nx = g.nx;
   a.ny = g.ny;
   a.nz = g.nz;
+  a.pnx = g.pnx;
+  a.pcx = g.pcx;
   a.coef = (const T *)s->d_coef;
   a.mat = s->d_gmat;
   a.ctab = (const T *)s->d_ctab;
@@ -299,6 +331,13 @@ void grid_args(pn_solver *s, GridArgs<T> &a) {
   a.s_idx = s->d_sidx;
   a.sig_stride = 0;
   a.sig_rows = 1;
+  a.err = s->d_err;
+  a.n_rows = s->mat.n_mat + 1;
+}
+
+const void *grid_maps_for(const pn_solver *s, int in) {
+  return s->d_tmaps ? (const void *)((const unsigned char *)s->d_tmaps + (size_t)in * grid_tma_maps_bytes())
+                    : nullptr;
 }
 template void grid_args<double>(pn_solver *, GridArgs<double> &);
 template void grid_args<float>(pn_solver *, GridArgs<float> &);
@@ -327,6 +366,7 @@ void run(pn_solver *s, int32_t nsteps) {
         a.S_in[c] = (const T *)s->S[in][c];
         a.S_out[c] = (T *)s->S[out][c];
       }
+      a.tmaps = grid_maps_for(s, in);
       a.sigval = nsig > 0 ? (const T *)s->d_sig + sig_row(s, k) * nsig : nullptr;
       a.rec = s->rec_count + k;  // sigval points at this step's row (stride 0)
       pn_solver::Mark m{};
@@ -337,7 +377,8 @@ void run(pn_solver *s, int32_t nsteps) {
         ck(cudaEventRecord(m.a, s->stream), "event");
       }
       cudaError_t e;
-      if constexpr (std::is_same<T, float2>::value) e = launch_grid_df64(a, s->sym, s->stream);
+      if (a.tmaps) e = launch_grid_tma(&a, s->precision, s->sym, s->stream);
+      else if constexpr (std::is_same<T, float2>::value) e = launch_grid_df64(a, s->sym, s->stream);
       else if constexpr (std::is_same<T, double>::value) e = launch_grid_f64(a, s->sym, s->stream);
       else e = launch_grid_f32(a, s->sym, s->stream);
       if (s->timing) {

@@ -423,7 +423,8 @@ void detect_grid(const MeshTables &t, GridMap &g, double max_void_fraction) {
   }
   const int64_t nx = mi, ny = mj, nz = mk;
   const int64_t gnodes = (nx + 1) * (ny + 1) * (nz + 1), gcells = nx * ny * nz;
-  if (gnodes >= (int64_t(1) << 31) - 1) {
+  const int64_t pnx = GridMap::node_pitch(nx), pcx = GridMap::cell_pitch(nx);
+  if (pnx * (ny + 1) * (nz + 1) >= (int64_t(1) << 31) - 1) {
     g.why = "lattice too large for 32-bit indices";
     return;
   }
@@ -434,10 +435,12 @@ void detect_grid(const MeshTables &t, GridMap &g, double max_void_fraction) {
   g.nx = (int32_t)nx;
   g.ny = (int32_t)ny;
   g.nz = (int32_t)nz;
+  g.pnx = (int32_t)pnx;
+  g.pcx = (int32_t)pcx;
   g.node_grid.resize(t.n_nodes);
-  std::vector<uint8_t> taken((size_t)gnodes, 0);
+  std::vector<uint8_t> taken((size_t)g.node_sites(), 0);
   for (int32_t n = 0; n < t.n_nodes; n++) {
-    const int64_t q = (gk[n] * (ny + 1) + gj[n]) * (nx + 1) + gi[n];
+    const int64_t q = g.node_at(gi[n], gj[n], gk[n]);
     if (taken[q]) {
       g.why = "two nodes on one lattice site";
       return;
@@ -448,7 +451,7 @@ void detect_grid(const MeshTables &t, GridMap &g, double max_void_fraction) {
   static const int bx[8] = {0, 1, 1, 0, 0, 1, 1, 0}, by[8] = {0, 0, 1, 1, 0, 0, 1, 1},
                    bz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
   g.cell_grid.resize(t.n_cells);
-  std::vector<uint8_t> ctaken((size_t)gcells, 0);
+  std::vector<uint8_t> ctaken((size_t)g.cell_sites(), 0);
   for (int32_t c = 0; c < t.n_cells; c++) {
     const int32_t *h = &t.hex[(size_t)c * 8];
     const int64_t i0 = gi[h[0]], j0 = gj[h[0]], k0 = gk[h[0]];
@@ -458,7 +461,7 @@ void detect_grid(const MeshTables &t, GridMap &g, double max_void_fraction) {
         return;
       }
     }
-    const int64_t q = (k0 * ny + j0) * nx + i0;
+    const int64_t q = g.cell_at(i0, j0, k0);
     if (ctaken[q]) {
       g.why = "two cells on one lattice site";
       return;

@@ -96,17 +96,29 @@ void build_source_entries(const MeshTables &t, const std::vector<pn_window_sourc
 // in the reference's corner order, no two nodes or cells on one lattice site.
 // Lattice sites without a mesh node / cell are "void": their velocity and
 // stress stay zero, which is what a missing (-1) slot contributes in the
-// reference (RightHex.hpp:225-231).  Internal numbering is x fastest:
-//   grid node (i,j,k) -> (k*(ny+1) + j)*(nx+1) + i
-//   grid cell (i,j,k) -> (k*ny + j)*nx + i
+// reference (RightHex.hpp:225-231).  Internal numbering is x fastest with
+// padded rows, so that every row starts on a 16-byte boundary (a tensor-copy
+// requirement on row strides):
+//   grid node (i,j,k) -> (k*(ny+1) + j)*pnx + i,  pnx = (nx+1) rounded up to 4
+//   grid cell (i,j,k) -> (k*ny + j)*pcx + i,      pcx = nx rounded up to 16
+// Padding sites are void.
 struct GridMap {
   bool ok = false;
   std::string why;               // reason when not a grid
   int32_t nx = 0, ny = 0, nz = 0;  // cells per axis
+  int32_t pnx = 0, pcx = 0;        // row pitch (sites) of node / cell buffers
   std::vector<int64_t> node_grid;  // mesh node -> grid node
   std::vector<int64_t> cell_grid;  // mesh cell -> grid cell
+  // lattice sites (the box, without padding)
   int64_t grid_nodes() const { return (int64_t)(nx + 1) * (ny + 1) * (nz + 1); }
   int64_t grid_cells() const { return (int64_t)nx * ny * nz; }
+  // buffer lengths (with padding)
+  int64_t node_sites() const { return (int64_t)pnx * (ny + 1) * (nz + 1); }
+  int64_t cell_sites() const { return (int64_t)pcx * ny * nz; }
+  int64_t node_at(int64_t i, int64_t j, int64_t k) const { return (k * (ny + 1) + j) * pnx + i; }
+  int64_t cell_at(int64_t i, int64_t j, int64_t k) const { return (k * ny + j) * pcx + i; }
+  static int32_t node_pitch(int64_t nx) { return (int32_t)((nx + 1 + 3) / 4 * 4); }
+  static int32_t cell_pitch(int64_t nx) { return (int32_t)((nx + 15) / 16 * 16); }
 };
 
 // Detects the voxel-grid structure of a uniformly spaced mesh; gives up

@@ -18,6 +18,7 @@
 #include "pn_setup.hpp"
 #include "rsg_common.cuh"
 #include "rsg_grid.cuh"
+#include "rsg_state.cuh"
 
 namespace pn {
 
@@ -83,6 +84,8 @@ struct pn_solver {
   pn::GridMap grid;
   int sym = 0;             // material symmetry class of the stiffness table
   uint8_t *d_gmat = nullptr;
+  void *d_tmaps = nullptr;   // tensor maps [2 input parities] (null: classic kernel)
+  int32_t *d_err = nullptr;  // device error word of the grid kernels
 
   // sources (both forms)
   std::vector<pn_window_source> src;
@@ -200,6 +203,32 @@ struct pn_solver {
     pn::ck(cudaMemcpyAsync(dst, src_, bytes, cudaMemcpyHostToDevice, stream), "upload");
   }
 
+  // State transfer through the device: one FP64 field is copied to a staging
+  // buffer and converted / permuted there by rsg_state.cu.  The staging buffer
+  // (8 B per node or cell, whichever is more) and the grid form's index maps
+  // are allocated on the first transfer and counted in dev_bytes from then.
+  double *d_stage = nullptr;
+  int64_t *d_nmap = nullptr, *d_cmap = nullptr;
+
+  double *stage() {
+    if (!d_stage) d_stage = alloc<double>(8 * (size_t)std::max(mesh.n_nodes, mesh.n_cells));
+    return d_stage;
+  }
+  // host FP64 field[n] -> dst[map[i]] in the storage type (map null: dst[i])
+  void put_field(void *dst, const double *host, size_t n, const int64_t *map) {
+    if (n == 0) return;
+    double *st = stage();
+    pn::ck(cudaMemcpyAsync(st, host, n * 8, cudaMemcpyHostToDevice, stream), "put_field copy");
+    pn::ck(pn::launch_state_store(precision, st, (int64_t)n, map, dst, stream), "put_field kernel");
+  }
+  // src[map[i]] (or src[i]) in the storage type -> host FP64 field[n]
+  void get_field(double *host, const void *src, size_t n, const int64_t *map) {
+    if (n == 0 || !host) return;
+    double *st = stage();
+    pn::ck(pn::launch_state_load(precision, src, (int64_t)n, map, st, stream), "get_field kernel");
+    pn::ck(cudaMemcpyAsync(host, st, n * 8, cudaMemcpyDeviceToHost, stream), "get_field copy");
+  }
+
   void clear_marks() {
     for (auto &m : marks) {
       cudaEventDestroy(m.a);
@@ -247,11 +276,17 @@ int64_t step_bytes(const pn_solver *s);
 // fields -- signal row, record, buffers -- are the caller's to set)
 template <typename T> void table_args(pn_solver *s, VelArgs<T> &va, StressArgs<T> &sa);
 template <typename T> void grid_args(pn_solver *s, GridArgs<T> &a);
+// tensor maps of input buffer `in` (0/1) for the tensor-copy kernel, or null
+const void *grid_maps_for(const pn_solver *s, int in);
 
 // rebuild the source lists after sources changed (pn_capi.cpp)
 void refresh_sources(pn_solver *s);
 
 // the calling thread's message for pn_last_error(); returns code (pn_capi.cpp)
 int set_last_error(int code, const std::string &msg);
+
+// PN_ERR_DEVICE_CHECK (and the word cleared) when a kernel recorded an error
+// in the solver's device error word; the stream must be synchronised
+int device_check(pn_solver *s);
 
 }  // namespace pn

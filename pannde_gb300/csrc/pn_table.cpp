@@ -56,22 +56,29 @@ void table_create(pn_solver *s) {
 }
 
 void table_put_state(pn_solver *s, const double *const *V, const double *const *S) {
+  // FP64 storage takes the caller's array as is; FP32 and double-float
+  // storage convert on the device (rsg_state.cu)
   const int32_t nn = s->mesh.n_nodes, nc = s->mesh.n_cells;
-  for (int k = 0; k < 3; k++) {
-    if (V && V[k]) s->upload_real(s->V[0][k], V[k], nn);
-    else ck(cudaMemsetAsync(s->V[0][k], 0, (size_t)nn * s->esz, s->stream), "memset");
-  }
-  for (int k = 0; k < 6; k++) {
-    if (S && S[k]) s->upload_real(s->S[0][k], S[k], nc);
-    else ck(cudaMemsetAsync(s->S[0][k], 0, (size_t)nc * s->esz, s->stream), "memset");
-  }
+  const bool raw = s->esz == 8 && !s->is_df64();
+  auto put = [&](void *dst, const double *src, int32_t n) {
+    if (!src) ck(cudaMemsetAsync(dst, 0, (size_t)n * s->esz, s->stream), "memset");
+    else if (raw) s->upload_raw(dst, src, (size_t)n * 8);
+    else s->put_field(dst, src, (size_t)n, nullptr);
+  };
+  for (int k = 0; k < 3; k++) put(s->V[0][k], V ? V[k] : nullptr, nn);
+  for (int k = 0; k < 6; k++) put(s->S[0][k], S ? S[k] : nullptr, nc);
 }
 
 void table_get_state(pn_solver *s, double *const *V, double *const *S) {
-  for (int k = 0; k < 3; k++)
-    if (V) s->download_real(V[k], s->V[0][k], (size_t)s->mesh.n_nodes);
-  for (int k = 0; k < 6; k++)
-    if (S) s->download_real(S[k], s->S[0][k], (size_t)s->mesh.n_cells);
+  const bool raw = s->esz == 8 && !s->is_df64();
+  auto get = [&](double *dst, const void *src, int32_t n) {
+    if (!dst || n == 0) return;
+    if (raw) ck(cudaMemcpyAsync(dst, src, (size_t)n * 8, cudaMemcpyDeviceToHost, s->stream), "download");
+    else s->get_field(dst, src, (size_t)n, nullptr);
+  };
+  for (int k = 0; k < 3; k++) get(V ? V[k] : nullptr, s->V[0][k], s->mesh.n_nodes);
+  for (int k = 0; k < 6; k++) get(S ? S[k] : nullptr, s->S[0][k], s->mesh.n_cells);
+  ck(cudaStreamSynchronize(s->stream), "get_state");
 }
 
 void table_sources(pn_solver *s) {

@@ -97,9 +97,9 @@ __device__ __forceinline__ void grid_block(const GridArgs<typename GNum<R>::S> &
   const bool node_in = (i <= nx) && (j <= ny);
   const bool node_own = node_in && tx < TX - 1 && ty < TY - 1;
   const bool cell_own = tx < TX - 1 && ty < TY - 1 && i < nx && j < ny;
-  const int64_t nplane = (int64_t)(nx + 1) * (ny + 1), cplane = (int64_t)nx * ny;
-  const int64_t nidx0 = (int64_t)j * (nx + 1) + i;  // node index in its layer
-  const int64_t cidx0 = (int64_t)j * nx + i;        // cell index in its layer
+  const int64_t nplane = (int64_t)a.pnx * (ny + 1), cplane = (int64_t)a.pcx * ny;
+  const int64_t nidx0 = (int64_t)j * a.pnx + i;  // node index in its layer
+  const int64_t cidx0 = (int64_t)j * a.pcx + i;  // cell index in its layer
   const R gx = N::val(a.g[0]), gy = N::val(a.g[1]), gz = N::val(a.g[2]);
   const St *sigrow = a.sigval ? a.sigval + (int64_t)min(step, a.sig_rows - 1) * a.sig_stride : nullptr;
   const int64_t rec = a.rec + step;
@@ -113,7 +113,7 @@ __device__ __forceinline__ void grid_block(const GridArgs<typename GNum<R>::S> &
     const int cx = q % CW, cy = q / CW;
     const int ci = i0 - 1 + cx, cj = j0 - 1 + cy;
     pf_ok[p] = q < CT && ci >= 0 && ci < nx && cj >= 0 && cj < ny;
-    pf_off[p] = pf_ok[p] ? cj * nx + ci : 0;
+    pf_off[p] = pf_ok[p] ? cj * a.pcx + ci : 0;
   }
   R pf[PF][6];
   auto issue = [&](int kc) {  // loads of cell layer kc (zeros outside)
@@ -351,14 +351,6 @@ struct Setup {
   }
 };
 
-// cell layers per z chunk: about four waves of blocks, at least four layers
-inline int chunk_layers(int nz, long long xy_blocks, int sms, int per_sm) {
-  const long long want = 4LL * sms * per_sm;
-  long long chunks = (want + xy_blocks - 1) / xy_blocks;
-  chunks = std::max(1LL, std::min(chunks, (long long)std::max(1, nz / 4)));
-  return (int)((nz + chunks - 1) / chunks);
-}
-
 template <typename R, int TX, int TY, int SYM>
 cudaError_t launch_t(const GridArgs<typename GNum<R>::S> &a, cudaStream_t st) {
   using S = Setup<R, TX, TY, SYM>;
@@ -367,7 +359,7 @@ cudaError_t launch_t(const GridArgs<typename GNum<R>::S> &a, cudaStream_t st) {
   if (e != cudaSuccess) return e;
   GridArgs<typename GNum<R>::S> b = a;
   const unsigned gx = (unsigned)(a.nx / (TX - 1) + 1), gy = (unsigned)(a.ny / (TY - 1) + 1);
-  if (b.kchunk <= 0) b.kchunk = chunk_layers(a.nz, (long long)gx * gy, sms, per_sm);
+  if (b.kchunk <= 0) b.kchunk = grid_chunk_for(a.nz, (long long)gx * gy, sms, per_sm);
   const dim3 grid(gx, gy, (unsigned)((a.nz + b.kchunk - 1) / b.kchunk));
   k_grid_step<R, TX, TY, SYM><<<grid, TX * TY, S::smem, st>>>(b, 0);
   return cudaGetLastError();
@@ -405,14 +397,27 @@ cudaError_t launch_batch_sym(const GridBatchLaunch &b, int step, cudaStream_t st
 int grid_tile_x() { return 32; }
 int grid_tile_y() { return 8; }
 
-int grid_chunk_layers(int precision, int nx, int ny, int nz) {
+int grid_chunk_for(int nz, long long xy_blocks, int sms, int per_sm) {
+  if (nz <= 0) return 1;
+  const long long want = 4LL * sms * per_sm;
+  long long chunks = (want + xy_blocks - 1) / xy_blocks;
+  chunks = std::max(1LL, std::min(chunks, (long long)std::max(1, nz / 4)));
+  chunks = std::max(chunks, (long long)((nz + kGridChunkMax - 1) / kGridChunkMax));
+  return (int)((nz + chunks - 1) / chunks);
+}
+
+int grid_chunk_layers(int precision, int nx, int ny, int nz, bool tma) {
   int sms = 0, per_sm = 0;
   cudaError_t e = precision == 2 ? Setup<float, 32, 8, 0>::ensure(sms, per_sm)
                 : precision == 3 ? Setup<df64, 32, 8, 0>::ensure(sms, per_sm)
                                  : Setup<double, 32, 8, 0>::ensure(sms, per_sm);
-  if (e != cudaSuccess || nz <= 0) return nz > 0 ? nz : 1;
+  if (e != cudaSuccess || nz <= 0) return std::min(std::max(nz, 1), kGridChunkMax);
+  if (tma) {
+    const int p = grid_tma_blocks_per_sm(precision);
+    if (p > 0) per_sm = p;
+  }
   const long long xy = (long long)(nx / 31 + 1) * (ny / 7 + 1);
-  return chunk_layers(nz, xy, sms, per_sm);
+  return grid_chunk_for(nz, xy, sms, per_sm);
 }
 
 cudaError_t launch_grid_f32(const GridArgs<float> &a, int sym, cudaStream_t st) {

@@ -1,7 +1,8 @@
 // rsg_grid.cuh -- arguments of the fused voxel-grid step kernel (rsg_grid.cu).
 //
-// Layout (x fastest): grid node (i,j,k) at (k*(ny+1)+j)*(nx+1)+i, grid cell
-// (i,j,k) at (k*ny+j)*nx+i.  Block (bx,by) owns node and cell columns
+// Layout (x fastest, padded rows): grid node (i,j,k) at (k*(ny+1)+j)*pnx+i,
+// grid cell (i,j,k) at (k*ny+j)*pcx+i; pnx*sizeof(T) and pcx are multiples of
+// 16 bytes (row strides a tensor copy accepts).  Block (bx,by) owns node and cell columns
 // i in [bx*(TX-1), bx*(TX-1)+TX-1), j likewise with TY; its local index of the
 // node / cell (i,j) is (i-i0) + TX*(j-j0).  Sparse sources and sensors are
 // sorted by (block, layer, local index) with one [begin,end) range per
@@ -15,6 +16,7 @@ namespace pn {
 template <typename T>
 struct GridArgs {
   int32_t nx, ny, nz;  // cells per axis
+  int32_t pnx, pcx;    // row pitch (sites) of node / cell buffers
   int32_t kchunk;      // cell layers per block along z (set by the launcher when 0)
   const T *V_in[3];
   T *V_out[3];
@@ -45,12 +47,22 @@ struct GridArgs {
   int32_t n_sens;
   int64_t rec;           // record written by step 0 of the launch (rec + step later)
   int64_t rec_cap;       // records beyond this are not written
+  int32_t *err;          // device error word (bounded waits that gave up), or null
+  const void *tmaps;     // tensor maps of this step's input buffers (rsg_grid_tma.cu), or null
+  int32_t n_rows;        // rows of ctab (materials + the void row)
 };
+
+constexpr int kGridChunkMax = 64;     // cell layers per z chunk, at most
+constexpr int kGridTmaRowsMax = 32;   // stiffness rows the tensor-copy kernel stages
 
 int grid_tile_x();
 int grid_tile_y();
-// cell layers per z chunk the launcher picks for this lattice and precision
-int grid_chunk_layers(int precision, int nx, int ny, int nz);
+// cell layers per z chunk: about four waves of blocks, at least four layers,
+// at most kGridChunkMax
+int grid_chunk_for(int nz, long long xy_blocks, int sms, int per_sm);
+// cell layers per z chunk the launcher picks for this lattice, precision and
+// kernel (tma: the tensor-copy kernel of rsg_grid_tma.cu)
+int grid_chunk_layers(int precision, int nx, int ny, int nz, bool tma);
 
 // a batch of grid-form members: argument blocks (kchunk set) and the prefix
 // of their block counts ((nx/(TX-1)+1) * (ny/(TY-1)+1) * chunks each)
@@ -65,5 +77,16 @@ cudaError_t launch_grid_batch(const GridBatchLaunch &b, int precision, int step,
 cudaError_t launch_grid_f32(const GridArgs<float> &a, int sym, cudaStream_t st);
 cudaError_t launch_grid_f64(const GridArgs<double> &a, int sym, cudaStream_t st);
 cudaError_t launch_grid_df64(const GridArgs<float2> &a, int sym, cudaStream_t st);
+
+// tensor-copy kernel (rsg_grid_tma.cu): maps of one input parity occupy
+// grid_tma_maps_bytes(); encoding fails (false) when a buffer or pitch does not
+// meet the copy's alignment rules
+size_t grid_tma_maps_bytes();
+bool grid_tma_encode(int precision, int nx, int ny, int nz, int pnx, int pcx, const void *const V[3],
+                     const void *const S[6], const void *coef, const uint8_t *mat, void *out);
+int grid_tma_blocks_per_sm(int precision);
+cudaError_t launch_grid_tma(const void *args /* GridArgs<storage type> */, int precision, int sym,
+                            cudaStream_t st);
+cudaError_t launch_grid_tma_batch(const GridBatchLaunch &b, int precision, int step, cudaStream_t st);
 
 }  // namespace pn

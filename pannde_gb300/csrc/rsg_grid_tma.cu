@@ -1,0 +1,574 @@
+// rsg_grid_tma.cu -- the fused voxel-grid step with tensor-copy (TMA) staging.
+//
+// Same arithmetic and tiling as rsg_grid.cu (a block owns a 31 x 7 column of
+// nodes and cells over a chunk of layers; its 32 x 8 threads are the nodes
+// plus a one-node apron on +x / +y), but every per-layer input tile arrives in
+// shared memory by cp.async.bulk.tensor, issued by one thread one layer
+// ahead and completed on an mbarrier:
+//   slot ring (4 layers)    S_in[6] cell tile (33 x 9 used, x rounded down to
+//                           the 16-byte boundary), material tile (31 x 7 used)
+//   node ring (2 layers)    V_in[3] and coef node tiles (32 x 8 used)
+// No thread holds prefetched values in registers and the loads never stall an
+// instruction stream; out-of-lattice elements arrive as zeros (the tensor
+// copy's fill), which is the void-site value.
+//
+// One __syncthreads per layer: iteration k runs
+//   B(k)    velocity of node layer k from cell layers k-1 (partial sums in
+//           registers) and k (slot k), written to the computed-velocity tile
+//           k&1 and, for owned nodes, to V_out (HostRSGTDUT.hpp:338-362)
+//   C(k-2)  stress of cell layer k-2 from node layers k-2 (partial sums in
+//           registers) and k-1 (computed tile (k-1)&1, complete since the
+//           previous barrier) (HostRSGTDUT.hpp:278-293)
+// and thread 0 first issues the copies of layer k+1 into slot (k+1)&3, whose
+// previous layer k-3 was last read before the previous barrier.
+//
+// Every wait is bounded (about one second of %globaltimer); a wait that gives
+// up records an error word for the host, the block drains its own copies in
+// flight (again bounded) and returns.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+
+#include "df64.cuh"
+#include "rsg_common.cuh"
+#include "rsg_grid.cuh"
+
+namespace pn {
+namespace {
+
+constexpr int TX = 32, TY = 8, NT = TX * TY;
+constexpr int KC_MAX = kGridChunkMax;  // cell layers per chunk (source-range staging)
+constexpr int ROWS_MAX = kGridTmaRowsMax;
+constexpr int NSLOT = 4;
+
+struct GridMaps {
+  CUtensorMap S[6];
+  CUtensorMap V[3];
+  CUtensorMap coef;
+  CUtensorMap mat;
+};
+
+// shared-memory geometry for a storage element of ESZ bytes
+template <int ESZ>
+struct Geo {
+  static constexpr int A = 16 / ESZ;              // x alignment of a copy (elements)
+  static constexpr int BWC = ESZ == 4 ? 36 : 34;  // cell tile width: offset (< A) + 33
+  static constexpr int BWN = ESZ == 4 ? 36 : 34;  // node tile width: offset (< A) + 32
+  static constexpr int BWM = 48;                  // material tile width: offset (< 16) + 31
+  static constexpr int SBOX_BYTES = BWC * (TY + 1) * ESZ;
+  static constexpr int SBOX = (SBOX_BYTES + 127) / 128 * 128;
+  static constexpr int VBOX = BWN * TY * ESZ;
+  static constexpr int MBOX_BYTES = BWM * (TY - 1);
+  static constexpr int MBOX = (MBOX_BYTES + 127) / 128 * 128;
+  static constexpr int SLOT = 6 * SBOX + MBOX;
+  static constexpr int VSLOT = 4 * VBOX;
+  static constexpr uint32_t TX_BYTES = 6 * SBOX_BYTES + 4 * VBOX + MBOX_BYTES;
+  static constexpr int OFF_V = NSLOT * SLOT;
+  static constexpr int OFF_VT = OFF_V + 2 * VSLOT;             // computed velocity [2][3][NT]
+  static constexpr int OFF_C = OFF_VT + 2 * 3 * NT * ESZ;      // dt*C rows [ROWS_MAX][36]
+  static constexpr int OFF_R = OFF_C + ROWS_MAX * 36 * ESZ;    // ranges f, s [KC_MAX+2], m [KC_MAX]
+  static constexpr int OFF_B = OFF_R + (3 * KC_MAX + 4) * 8;   // mbarriers [NSLOT]
+  static constexpr int BYTES = OFF_B + NSLOT * 8;
+  static constexpr size_t SMEM = BYTES + 128;                  // + base alignment
+  static_assert(SLOT % 128 == 0 && VBOX % 128 == 0 && OFF_V % 128 == 0 && OFF_B % 8 == 0, "alignment");
+  static_assert(SBOX % ESZ == 0 && VBOX % ESZ == 0, "element size");
+};
+
+template <typename R> struct GNum;
+template <> struct GNum<float> {
+  using S = float;
+  static __device__ __forceinline__ float val(float v) { return v; }
+  static __device__ __forceinline__ float sto(float v) { return v; }
+  static __device__ __forceinline__ void st(float *p, int64_t i, float v) { p[i] = v; }
+  static __device__ __forceinline__ double dbl(float v) { return (double)v; }
+};
+template <> struct GNum<double> {
+  using S = double;
+  static __device__ __forceinline__ double val(double v) { return v; }
+  static __device__ __forceinline__ double sto(double v) { return v; }
+  static __device__ __forceinline__ void st(double *p, int64_t i, double v) { p[i] = v; }
+  static __device__ __forceinline__ double dbl(double v) { return v; }
+};
+template <> struct GNum<df64> {
+  using S = float2;
+  static __device__ __forceinline__ df64 val(float2 v) { return df64(v.x, v.y); }
+  static __device__ __forceinline__ float2 sto(df64 v) { return make_float2(v.hi, v.lo); }
+  static __device__ __forceinline__ void st(float2 *p, int64_t i, df64 v) { p[i] = make_float2(v.hi, v.lo); }
+  static __device__ __forceinline__ double dbl(df64 v) { return (double)v.hi + (double)v.lo; }
+};
+
+__host__ __device__ constexpr bool c_used(int sym, int k, int j) {
+  return sym == 0 ? true
+       : sym == 2 ? ((k < 3 && j < 3) || k == j)
+                  : ((k < 3 && j < 3) || k == j || (k == 5 && j < 3) || (j == 5 && k < 3) ||
+                     (k == 3 && j == 4) || (k == 4 && j == 3));
+}
+
+// ---- PTX wrappers: mbarrier, tensor copy, timer -------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// wait for phase `parity` of the barrier; false after about one second
+__device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (uint32_t n = 1;; n++) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((n & 63) == 0 && global_ns() - t0 > 1000000000ull) return false;
+  }
+}
+__device__ __forceinline__ void proxy_fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void tma_prefetch_map(const void *map) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(map) : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const void *map, int x, int y, int z, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ int floor_to(int v, int m) {  // largest multiple of m <= v (m > 0)
+  return v >= 0 ? v / m * m : -((-v + m - 1) / m) * m;
+}
+
+// error word codes
+constexpr int32_t kErrWait = 1;
+
+template <typename R, int SYM>
+__device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::S> &a, const GridMaps *M,
+                                               int bx, int by, int bz, int gxc, int step) {
+  using N = GNum<R>;
+  using St = typename N::S;
+  using G = Geo<(int)sizeof(St)>;
+  constexpr int SB = G::SBOX / (int)sizeof(St);  // field stride in a slot (elements)
+  constexpr int VB = G::VBOX / (int)sizeof(St);
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *base = (unsigned char *)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
+  St *sVt = reinterpret_cast<St *>(base + G::OFF_VT);
+  St *sC = reinterpret_cast<St *>(base + G::OFF_C);
+  int2 *sRf = reinterpret_cast<int2 *>(base + G::OFF_R);
+  int2 *sRs = sRf + (KC_MAX + 2);
+  int2 *sRm = sRs + (KC_MAX + 2);
+  const uint32_t bars = smem_u32(base + G::OFF_B);
+
+  const int t = threadIdx.x;
+  const int tx = t % TX, ty = t / TX;
+  const int i0 = bx * (TX - 1), j0 = by * (TY - 1);
+  const int blk = by * gxc + bx;
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+  const int i = i0 + tx, j = j0 + ty;
+  const bool node_own = (i <= nx) && (j <= ny) && tx < TX - 1 && ty < TY - 1;
+  const bool cell_own = tx < TX - 1 && ty < TY - 1 && i < nx && j < ny;
+  const int64_t nplane = (int64_t)a.pnx * (ny + 1), cplane = (int64_t)a.pcx * ny;
+  const int64_t nidx0 = (int64_t)j * a.pnx + i;
+  const int64_t cidx0 = (int64_t)j * a.pcx + i;
+  const R gx = N::val(a.g[0]), gy = N::val(a.g[1]), gz = N::val(a.g[2]);
+  const St *sigrow = a.sigval ? a.sigval + (int64_t)min(step, a.sig_rows - 1) * a.sig_stride : nullptr;
+  const int64_t rec = a.rec + step;
+  const int k0 = bz * a.kchunk, k1 = min(nz, k0 + a.kchunk);
+  const bool last_chunk = k1 == nz;
+
+  // tile origins of the copies (x on the 16-byte boundary) and offsets in them
+  const int xs_c = floor_to(i0 - 1, G::A), oc = i0 - 1 - xs_c;
+  const int xs_n = floor_to(i0, G::A), on = i0 - xs_n;
+  const int xs_m = floor_to(i0, 16), om = i0 - xs_m;
+
+  auto issue = [&](int L) {  // thread 0: copies of layer L into slot L&3, node slot L&1
+    const uint32_t bar = bars + 8u * (uint32_t)(L & 3);
+    unsigned char *sl = base + (L & 3) * G::SLOT;
+    unsigned char *vl = base + G::OFF_V + (L & 1) * G::VSLOT;
+    mbar_expect_tx(bar, G::TX_BYTES);
+#pragma unroll
+    for (int f = 0; f < 6; f++) tma_load_3d(smem_u32(sl + f * G::SBOX), &M->S[f], xs_c, j0 - 1, L, bar);
+    tma_load_3d(smem_u32(sl + 6 * G::SBOX), &M->mat, xs_m, j0, L, bar);
+#pragma unroll
+    for (int c = 0; c < 3; c++) tma_load_3d(smem_u32(vl + c * G::VBOX), &M->V[c], xs_n, j0, L, bar);
+    tma_load_3d(smem_u32(vl + 3 * G::VBOX), &M->coef, xs_n, j0, L, bar);
+  };
+  auto parity = [&](int L) { return (uint32_t)(((L - k0 + 1) >> 2) & 1); };
+
+  if (t == 0) {
+#pragma unroll
+    for (int s = 0; s < NSLOT; s++) mbar_init(bars + 8u * s, 1);
+    mbar_init_fence();
+  }
+  // per-chunk tables: stiffness rows, source and sensor ranges
+  for (int q = t; q < a.n_rows * 36; q += NT) sC[q] = a.ctab[q];
+  const int nL = k1 - k0 + 2;  // node layers k0-1 .. k1
+  for (int q = t; q < nL; q += NT) {
+    const int k = k0 - 1 + q;
+    const bool ok = k >= 0 && k <= nz;
+    sRf[q] = (a.f_rng && ok) ? a.f_rng[(int64_t)blk * (nz + 1) + k] : make_int2(0, 0);
+    sRs[q] = (a.s_rng && ok) ? a.s_rng[(int64_t)blk * (nz + 1) + k] : make_int2(0, 0);
+  }
+  for (int q = t; q < k1 - k0; q += NT) sRm[q] = a.m_rng ? a.m_rng[(int64_t)blk * nz + k0 + q] : make_int2(0, 0);
+  __syncthreads();
+  if (t == 0) {
+    issue(k0 - 1);
+    issue(k0);
+  }
+
+  R vpx0 = R(), vpx4 = R(), vpx5 = R(), vpy1 = R(), vpy3 = R(), vpy5 = R(), vs2 = R(), vs3 = R(),
+    vs4 = R();
+  R spx[3], spy[3], ss[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) spx[c] = spy[c] = ss[c] = R();
+  const int ra = ty * G::BWC + oc + tx;  // cell (i-1, j-1) in the cell tile
+  const int rv = ty * G::BWN + on + tx;  // node (i, j) in the node tile
+  int waited = k0 - 2;                   // last layer this thread has waited for
+  bool fail = false;
+
+  for (int k = k0 - 1; k <= k1 + 1; k++) {
+    if (t == 0 && k >= k0 && k + 1 <= k1) {
+      proxy_fence_async_smem();
+      issue(k + 1);
+    }
+    // ---- B: velocity of node layer k
+    if (k <= k1) {
+      if (mbar_wait(bars + 8u * (uint32_t)(k & 3), parity(k))) waited = k;
+      else fail = true;
+      const St *Sk = reinterpret_cast<const St *>(base + (k & 3) * G::SLOT);
+      auto cellv = [&](int f, int q) { return N::val(Sk[f * SB + q]); };
+      const int ib = ra + 1, id = ra + G::BWC, ic = id + 1;
+      R A, B, C, D;
+      A = cellv(0, ra); B = cellv(0, ib); C = cellv(0, ic); D = cellv(0, id);
+      const R px0 = (B + C) - (A + D);
+      A = cellv(1, ra); B = cellv(1, ib); C = cellv(1, ic); D = cellv(1, id);
+      const R py1 = (C + D) - (A + B);
+      A = cellv(2, ra); B = cellv(2, ib); C = cellv(2, ic); D = cellv(2, id);
+      const R s2 = (A + B) + (C + D);
+      A = cellv(3, ra); B = cellv(3, ib); C = cellv(3, ic); D = cellv(3, id);
+      R ab = A + B, cd = C + D;
+      const R py3 = cd - ab, s3 = ab + cd;
+      A = cellv(4, ra); B = cellv(4, ib); C = cellv(4, ic); D = cellv(4, id);
+      R bc = B + C, ad = A + D;
+      const R px4 = bc - ad, s4 = bc + ad;
+      A = cellv(5, ra); B = cellv(5, ib); C = cellv(5, ic); D = cellv(5, id);
+      const R px5 = (B + C) - (A + D), py5 = (C + D) - (A + B);
+      if (k >= k0) {
+        R ax = gx * (vpx0 + px0) + gy * (vpy5 + py5) + gz * (s4 - vs4);
+        R ay = gx * (vpx5 + px5) + gy * (vpy1 + py1) + gz * (s3 - vs3);
+        R az = gx * (vpx4 + px4) + gy * (vpy3 + py3) + gz * (s2 - vs2);
+        const int2 fr = sRf[k - k0 + 1];
+        for (int e = fr.x; e < fr.y; e++) {  // force sources of this block and layer
+          const int key = __ldg(a.f_key + e);
+          if ((key & 0xffff) != t) continue;
+          const R v = N::val(a.f_w[e]) * N::val(sigrow[__ldg(a.f_sig + e)]);
+          const int d = key >> 16;
+          if (d == 0) ax = ax + v;
+          else if (d == 1) ay = ay + v;
+          else az = az + v;
+        }
+        const St *Vk = reinterpret_cast<const St *>(base + G::OFF_V + (k & 1) * G::VSLOT);
+        R vn[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) vn[c] = N::val(Vk[c * VB + rv]);
+        const R cf = N::val(Vk[3 * VB + rv]);
+        if (!(cf == R())) {
+          vn[0] = vn[0] + cf * ax;
+          vn[1] = vn[1] + cf * ay;
+          vn[2] = vn[2] + cf * az;
+        }
+        St *Vt = sVt + (k & 1) * 3 * NT;
+#pragma unroll
+        for (int c = 0; c < 3; c++) Vt[c * NT + t] = N::sto(vn[c]);
+        if (node_own && (k < k1 || last_chunk)) {
+          const int64_t n = (int64_t)k * nplane + nidx0;
+#pragma unroll
+          for (int c = 0; c < 3; c++) N::st(a.V_out[c], n, vn[c]);
+          const int2 sr = sRs[k - k0 + 1];
+          if (rec < a.rec_cap) {
+            for (int e = sr.x; e < sr.y; e++) {  // sensor traces
+              if (__ldg(a.s_key + e) != t) continue;
+              double *tr = a.traces + (rec * a.n_sens + __ldg(a.s_idx + e)) * 3;
+              tr[0] = N::dbl(vn[0]);
+              tr[1] = N::dbl(vn[1]);
+              tr[2] = N::dbl(vn[2]);
+            }
+          }
+        }
+      }
+      vpx0 = px0; vpx4 = px4; vpx5 = px5; vpy1 = py1; vpy3 = py3; vpy5 = py5;
+      vs2 = s2; vs3 = s3; vs4 = s4;
+    }
+
+    // ---- C: partial sums of node layer k-1, stress of cell layer k-2
+    if (k - 1 >= k0 && k - 1 <= k1 && tx < TX - 1 && ty < TY - 1) {
+      const St *Vt = sVt + ((k - 1) & 1) * 3 * NT;
+      const int ia = t, ib = t + 1, ic = t + TX + 1, id = t + TX;
+      R px[3], py[3], s[3];
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const R A = N::val(Vt[c * NT + ia]), B = N::val(Vt[c * NT + ib]);
+        const R C = N::val(Vt[c * NT + ic]), D = N::val(Vt[c * NT + id]);
+        const R ab = A + B, cd = C + D;
+        px[c] = (B + C) - (A + D);
+        py[c] = cd - ab;
+        s[c] = ab + cd;
+      }
+      const int kc = k - 2;
+      if (kc >= k0 && cell_own) {
+        const R d00 = spx[0] + px[0], d10 = spy[0] + py[0], d20 = s[0] - ss[0];
+        const R d01 = spx[1] + px[1], d11 = spy[1] + py[1], d21 = s[1] - ss[1];
+        const R d02 = spx[2] + px[2], d12 = spy[2] + py[2], d22 = s[2] - ss[2];
+        R e[6];
+        e[0] = gx * d00;
+        e[1] = gy * d11;
+        e[2] = gz * d22;
+        e[3] = gy * d12 + gz * d21;
+        e[4] = gx * d02 + gz * d20;
+        e[5] = gx * d01 + gy * d10;
+        const unsigned char *sl = base + (kc & 3) * G::SLOT;
+        const St *Sc = reinterpret_cast<const St *>(sl);
+        const int own = ra + G::BWC + 1;  // cell (i, j)
+        const int row = sl[6 * G::SBOX + ty * G::BWM + om + tx];
+        const St *Cm = sC + 36 * row;
+        R acc[6];
+#pragma unroll
+        for (int f = 0; f < 6; f++) acc[f] = N::val(Sc[f * SB + own]);
+        const int2 mr = sRm[kc - k0];
+        for (int ee = mr.x; ee < mr.y; ee++) {  // moment sources of this block and cell layer
+          const int key = __ldg(a.m_key + ee);
+          if ((key & 0xffff) != t) continue;
+          const R v = N::val(a.m_w[ee]) * N::val(sigrow[__ldg(a.m_sig + ee)]);
+          const int kk = key >> 16;
+#pragma unroll
+          for (int f = 0; f < 6; f++)
+            if (f == kk) acc[f] = acc[f] + v;
+        }
+        const int64_t cg = (int64_t)kc * cplane + cidx0;
+#pragma unroll
+        for (int kk = 0; kk < 6; kk++) {
+#pragma unroll
+          for (int jj = 0; jj < 6; jj++)
+            if (c_used(SYM, kk, jj)) acc[kk] = acc[kk] + N::val(Cm[6 * kk + jj]) * e[jj];
+          N::st(a.S_out[kk], cg, acc[kk]);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        spx[c] = px[c];
+        spy[c] = py[c];
+        ss[c] = s[c];
+      }
+    }
+    if (__syncthreads_or(fail)) {
+      // give up: record, drain this block's copies in flight, return
+      if (t == 0) {
+        if (a.err) atomicExch(a.err, kErrWait);
+        const int issued = min(k1, max(k + 1, k0));
+        for (int L = waited + 1; L <= issued; L++) (void)mbar_wait(bars + 8u * (uint32_t)(L & 3), parity(L));
+      }
+      return;
+    }
+  }
+}
+
+template <typename R, int SYM>
+__global__ void __launch_bounds__(NT) k_grid_tma(const GridArgs<typename GNum<R>::S> a, int step) {
+  const GridMaps *M = reinterpret_cast<const GridMaps *>(a.tmaps);
+  grid_block_tma<R, SYM>(a, M, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x, step);
+}
+
+template <typename R, int SYM>
+__global__ void __launch_bounds__(NT)
+    k_grid_tma_batch(const GridArgs<typename GNum<R>::S> *__restrict__ args, const int *__restrict__ block_start,
+                     int n_members, int step) {
+  const int id = blockIdx.x;
+  int lo = 0, hi = n_members;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(block_start + mid) <= id) lo = mid;
+    else hi = mid;
+  }
+  const GridArgs<typename GNum<R>::S> &a = args[lo];
+  const GridMaps *M = reinterpret_cast<const GridMaps *>(a.tmaps);
+  const int local = id - __ldg(block_start + lo);
+  const int gxc = a.nx / (TX - 1) + 1, gyc = a.ny / (TY - 1) + 1;
+  grid_block_tma<R, SYM>(a, M, local % gxc, (local / gxc) % gyc, local / (gxc * gyc), gxc, step);
+}
+
+template <typename R, int SYM>
+struct SetupT {
+  using St = typename GNum<R>::S;
+  static constexpr size_t smem = Geo<(int)sizeof(St)>::SMEM;
+  static cudaError_t ensure(int &sms, int &per_sm) {
+    static unsigned long long done = 0;
+    static int s_sms[64] = {0}, s_per[64] = {0};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const int d = dev & 63;
+    if (!(done & (1ull << d))) {
+      e = cudaFuncSetAttribute(k_grid_tma<R, SYM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_grid_tma_batch<R, SYM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e == cudaSuccess) e = cudaDeviceGetAttribute(&s_sms[d], cudaDevAttrMultiProcessorCount, dev);
+      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s_per[d], k_grid_tma<R, SYM>, NT, smem);
+      if (e != cudaSuccess) return e;
+      s_per[d] = s_per[d] > 0 ? s_per[d] : 1;
+      done |= 1ull << d;
+    }
+    sms = s_sms[d];
+    per_sm = s_per[d];
+    return cudaSuccess;
+  }
+};
+
+template <typename R, int SYM>
+cudaError_t launch_t(const GridArgs<typename GNum<R>::S> &a, cudaStream_t st) {
+  using S = SetupT<R, SYM>;
+  int sms = 0, per_sm = 0;
+  cudaError_t e = S::ensure(sms, per_sm);
+  if (e != cudaSuccess) return e;
+  GridArgs<typename GNum<R>::S> b = a;
+  const unsigned gx = (unsigned)(a.nx / (TX - 1) + 1), gy = (unsigned)(a.ny / (TY - 1) + 1);
+  if (b.kchunk <= 0) b.kchunk = grid_chunk_for(a.nz, (long long)gx * gy, sms, per_sm);
+  if (b.kchunk > KC_MAX) return cudaErrorInvalidValue;
+  const dim3 grid(gx, gy, (unsigned)((a.nz + b.kchunk - 1) / b.kchunk));
+  k_grid_tma<R, SYM><<<grid, NT, S::smem, st>>>(b, 0);
+  return cudaGetLastError();
+}
+
+template <typename R, int SYM>
+cudaError_t launch_batch_t(const GridBatchLaunch &b, int step, cudaStream_t st) {
+  using S = SetupT<R, SYM>;
+  int sms = 0, per_sm = 0;
+  cudaError_t e = S::ensure(sms, per_sm);
+  if (e != cudaSuccess) return e;
+  if (b.total_blocks <= 0) return cudaSuccess;
+  k_grid_tma_batch<R, SYM><<<b.total_blocks, NT, S::smem, st>>>(
+      (const GridArgs<typename GNum<R>::S> *)b.args, b.block_start, b.n_members, step);
+  return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_sym(const GridArgs<typename GNum<R>::S> &a, int sym, cudaStream_t st) {
+  if (a.nx <= 0 || a.ny <= 0 || a.nz <= 0) return cudaSuccess;
+  if (!a.tmaps || a.n_rows > ROWS_MAX) return cudaErrorInvalidValue;
+  if (sym == 2) return launch_t<R, 2>(a, st);
+  if (sym == 1) return launch_t<R, 1>(a, st);
+  return launch_t<R, 0>(a, st);
+}
+
+template <typename R>
+cudaError_t launch_batch_sym(const GridBatchLaunch &b, int step, cudaStream_t st) {
+  if (b.sym == 2) return launch_batch_t<R, 2>(b, step, st);
+  if (b.sym == 1) return launch_batch_t<R, 1>(b, step, st);
+  return launch_batch_t<R, 0>(b, step, st);
+}
+
+// ---- tensor-map encoding (driver entry point, no libcuda link) ------------------
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *,
+                                 CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                 CUtensorMapFloatOOBfill);
+
+EncodeTiled encoder() {
+  static const EncodeTiled fn = []() -> EncodeTiled {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return nullptr;
+    return reinterpret_cast<EncodeTiled>(p);
+  }();
+  return fn;
+}
+
+// 3-D tile map over a pitched lattice buffer: dims (d0, d1, d2) sites, rows of
+// `pitch` sites, box (b0, b1, 1)
+bool encode3(CUtensorMap *m, CUtensorMapDataType dt, int esz, const void *ptr, int64_t d0, int64_t d1,
+             int64_t d2, int64_t pitch, int b0, int b1) {
+  const EncodeTiled fn = encoder();
+  if (!fn || !ptr) return false;
+  if (((uintptr_t)ptr & 15) != 0 || (pitch * esz) % 16 != 0 || (b0 * esz) % 16 != 0) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)d0, (cuuint64_t)d1, (cuuint64_t)d2};
+  const cuuint64_t strides[2] = {(cuuint64_t)(pitch * esz), (cuuint64_t)(pitch * d1 * esz)};
+  const cuuint32_t box[3] = {(cuuint32_t)b0, (cuuint32_t)b1, 1};
+  const cuuint32_t es[3] = {1, 1, 1};
+  return fn(m, dt, 3, const_cast<void *>(ptr), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int ESZ>
+bool encode_all(int nx, int ny, int nz, int pnx, int pcx, const void *const V[3], const void *const S[6],
+                const void *coef, const uint8_t *mat, GridMaps &m) {
+  using G = Geo<ESZ>;
+  const CUtensorMapDataType dt = ESZ == 4 ? CU_TENSOR_MAP_DATA_TYPE_UINT32 : CU_TENSOR_MAP_DATA_TYPE_UINT64;
+  bool ok = true;
+  for (int f = 0; f < 6; f++) ok = ok && encode3(&m.S[f], dt, ESZ, S[f], nx, ny, nz, pcx, G::BWC, TY + 1);
+  for (int c = 0; c < 3; c++) ok = ok && encode3(&m.V[c], dt, ESZ, V[c], nx + 1, ny + 1, nz + 1, pnx, G::BWN, TY);
+  ok = ok && encode3(&m.coef, dt, ESZ, coef, nx + 1, ny + 1, nz + 1, pnx, G::BWN, TY);
+  ok = ok && encode3(&m.mat, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, mat, nx, ny, nz, pcx, G::BWM, TY - 1);
+  return ok;
+}
+
+}  // namespace
+
+size_t grid_tma_maps_bytes() { return sizeof(GridMaps); }
+
+bool grid_tma_encode(int precision, int nx, int ny, int nz, int pnx, int pcx, const void *const V[3],
+                     const void *const S[6], const void *coef, const uint8_t *mat, void *out) {
+  GridMaps m;
+  std::memset(&m, 0, sizeof(m));
+  const bool ok = precision == 2 ? encode_all<4>(nx, ny, nz, pnx, pcx, V, S, coef, mat, m)
+                                 : encode_all<8>(nx, ny, nz, pnx, pcx, V, S, coef, mat, m);
+  if (ok) std::memcpy(out, &m, sizeof(m));
+  return ok;
+}
+
+int grid_tma_blocks_per_sm(int precision) {
+  int sms = 0, per_sm = 0;
+  const cudaError_t e = precision == 2 ? SetupT<float, 0>::ensure(sms, per_sm)
+                      : precision == 3 ? SetupT<df64, 0>::ensure(sms, per_sm)
+                                       : SetupT<double, 0>::ensure(sms, per_sm);
+  return e == cudaSuccess ? per_sm : 0;
+}
+
+cudaError_t launch_grid_tma(const void *args, int precision, int sym, cudaStream_t st) {
+  if (precision == 2) return launch_sym<float>(*(const GridArgs<float> *)args, sym, st);
+  if (precision == 3) return launch_sym<df64>(*(const GridArgs<float2> *)args, sym, st);
+  return launch_sym<double>(*(const GridArgs<double> *)args, sym, st);
+}
+
+cudaError_t launch_grid_tma_batch(const GridBatchLaunch &b, int precision, int step, cudaStream_t st) {
+  if (precision == 2) return launch_batch_sym<float>(b, step, st);
+  if (precision == 3) return launch_batch_sym<df64>(b, step, st);
+  return launch_batch_sym<double>(b, step, st);
+}
+
+}  // namespace pn

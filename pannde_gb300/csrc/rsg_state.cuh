@@ -1,0 +1,19 @@
+// rsg_state.cuh -- launchers of the state transfer kernels (rsg_state.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace pn {
+
+// Convert n FP64 values at src (device) to the storage type of `precision`
+// and write them to dst[map[i]] (dst[i] when map is null).
+cudaError_t launch_state_store(int precision, const double *src, int64_t n, const int64_t *map,
+                               void *dst, cudaStream_t st);
+
+// Read src[map[i]] (src[i] when map is null) in the storage type of
+// `precision` and write it as FP64 to dst[i] (device), i < n.
+cudaError_t launch_state_load(int precision, const void *src, int64_t n, const int64_t *map,
+                              double *dst, cudaStream_t st);
+
+}  // namespace pn

@@ -159,6 +159,7 @@ class Solver:
         d = {k: getattr(inf, k) for k, _ in N.PnSolverInfo._fields_}
         d["grid"] = tuple(d["grid"])
         d["form_name"] = {N.PN_FORM_GRID: "grid", N.PN_FORM_TABLE: "table"}.get(d["form"], "?")
+        d["kernel_name"] = {1: "classic", 2: "tma"}.get(d["grid_kernel"], "table")
         return d
 
     def device_state(self):

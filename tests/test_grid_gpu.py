@@ -117,7 +117,7 @@ def test_grid_chunked_solve_is_deterministic(cuda_device):
     assert np.array_equal(a[2], b[2])
 
 
-@pytest.mark.parametrize("dims", [(1, 1, 1), (31, 7, 2), (32, 8, 3), (62, 14, 1), (5, 40, 3)])
+@pytest.mark.parametrize("dims", [(1, 1, 1), (31, 7, 2), (32, 8, 3), (62, 14, 1), (5, 40, 3), (12, 9, 70)])
 def test_grid_tile_edges(cuda_device, dims):
     """Lattices at, below and above the 31 x 7 owned-cell tile sizes."""
     m = cases.voxel_mesh(np.ones(dims, dtype=bool), 1e-4)
@@ -141,3 +141,43 @@ def test_grid_and_table_forms_agree(cuda_device):
     for k in range(3):
         np.testing.assert_allclose(Vg[k], Vt[k], rtol=0, atol=1e-12 * np.abs(Vt[k]).max())
     np.testing.assert_allclose(tg, tt, rtol=0, atol=1e-12 * np.abs(tt).max())
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_grid_kernels_agree(cuda_device, prec, monkeypatch):
+    """The tensor-copy (TMA) staged kernel and the classic register-prefetch
+    kernel compute the same step: same sums in the same order, so FP64 and
+    double-float agree to rounding noise and FP32 to 1e-5."""
+    c = cases.laminate_case(nx=70, ny=23, nz=9, nsteps=25, radius=0.5e-3, n_sensors=6)
+    V0, S0 = random_state(c.mesh, 2)
+    out = {}
+    for kern in ("tma", "classic"):
+        if kern == "classic":
+            monkeypatch.setenv("PN_GRID_KERNEL", "classic")
+        with Solver.from_case(c, precision=prec, form="grid") as s:
+            assert s.info()["kernel_name"] == kern
+            s.set_state(V0, S0)
+            s.solve(c.nsteps)
+            out[kern] = (s.get_state(), s.traces())
+        monkeypatch.delenv("PN_GRID_KERNEL", raising=False)
+    tol = 1e-5 if prec == "f32" else 1e-12
+    (Va, Sa), ta = out["tma"]
+    (Vb, Sb), tb = out["classic"]
+    for x, y in list(zip(Va, Vb)) + list(zip(Sa, Sb)) + [(ta, tb)]:
+        d = np.linalg.norm(y)
+        assert np.linalg.norm(x - y) <= tol * (d if d > 0 else 1.0)
+
+
+def test_grid_many_materials_use_classic_kernel(cuda_device):
+    """More stiffness rows than the staged table holds: the classic kernel."""
+    m = cases.voxel_mesh(np.ones((20, 9, 40), dtype=bool), 1e-4)
+    base = cases.c21_from_6x6(cases.isotropic(70e9, 0.33))
+    mats = np.stack([base * (1.0 + 0.01 * q) for q in range(40)])
+    cm = (m.cell_ijk[:, 2] % 40).astype(np.int32)
+    c = cases.Case("g", m, np.full(40, 2700.0), mats, cm, 5e-9)
+    V0, S0 = random_state(m, 6)
+    ref = oracle.run(m, c.material_fields(), c.dt, [], 9, None, V0=V0, S0=S0)
+    with Solver(m, c, c.dt, "df64", "grid") as s:
+        assert s.info()["kernel_name"] == "classic"
+    dev, _ = run_grid(m, c, c.dt, [], 9, None, "df64", V0=V0, S0=S0)
+    compare("df64", dev, ref)
