@@ -361,6 +361,31 @@ int pn_batch_size(pn_batch *b, int32_t *n_members);
 int pn_batch_set_stream(pn_batch *b, void *cuda_stream);
 /* Advance every member nsteps steps (their own signals, sensors, time). */
 int pn_batch_solve(pn_batch *b, int32_t nsteps);
+
+/* pn_batch_solve without any device allocation.  No counterpart in the
+   reference (replaces nothing there; an addition for callers that cannot
+   allocate device memory while they run: a serving loop that plans every
+   byte of HBM up front with pn_plan_solver and must not have a solve grow
+   buffers behind its back, or a host whose device memory is owned by a pool
+   that forbids driver allocations after start-up -- cudaMalloc and cudaFree
+   can also stall every stream of the device while they run).
+   pn_batch_solve stages the members' argument blocks in buffers it grows
+   with cudaMalloc; this call stages them in one fixed 256 KiB device array
+   compiled into the library (room for about 350 grid-form or 550
+   table-form members), looked up with
+   cudaGetSymbolAddress on the first call on each device -- make that first
+   call before any stream capture starts on the device.  Batches whose
+   staging does not fit return PN_ERR_INVALID with the sizes, and so do
+   members whose source tables or signal table have not been built yet (any
+   one pn_batch_solve or pn_solver_solve step builds them; signal rows are
+   then refilled in place, never grown).  Nothing in the scratch has to start
+   at zero: every launch reads only bytes its call wrote before it.  All
+   batches of a process share the scratch: overlapping calls (from several
+   host threads) would race on it, so the call holds a process-wide lock and
+   they run one after another; each call waits for its GPU work before it
+   returns, so the scratch is idle between calls.  Results are identical to
+   pn_batch_solve. */
+int pn_batch_solve_noalloc(pn_batch *b, int32_t nsteps);
 int pn_batch_synchronize(pn_batch *b);
 int pn_batch_destroy(pn_batch *b);
 

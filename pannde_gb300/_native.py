@@ -135,6 +135,7 @@ SIGNATURES = {
     "pn_batch_size": (c_int, [c_void_p, P_int32]),
     "pn_batch_set_stream": (c_int, [c_void_p, c_void_p]),
     "pn_batch_solve": (c_int, [c_void_p, c_int32]),
+    "pn_batch_solve_noalloc": (c_int, [c_void_p, c_int32]),
     "pn_batch_synchronize": (c_int, [c_void_p]),
     "pn_batch_destroy": (c_int, [c_void_p]),
 }

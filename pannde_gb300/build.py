@@ -6,6 +6,7 @@ Sources (``pannde_gb300/csrc``):
   rsg_grid.cu   fused voxel-grid step kernel  nvcc, sm_103a
   rsg_grid_tma.cu  grid step, tensor-copy staging  nvcc, sm_103a
   rsg_state.cu  state convert / permute       nvcc, sm_103a
+  pn_noalloc.cu fixed scratch of the allocation-free batch solve   nvcc
   pn_setup.cpp  host table construction       g++, -ffp-contract=off
   pn_table.cpp  table form (any hex mesh)     g++
   pn_grid.cpp   grid form (voxel meshes)      g++
@@ -55,6 +56,7 @@ def _jobs() -> list[tuple[list[str], Path]]:
         (common_cu + ["-c", str(CSRC / "rsg_grid.cu")], OUT / "rsg_grid.o"),
         (common_cu + ["-c", str(CSRC / "rsg_grid_tma.cu")], OUT / "rsg_grid_tma.o"),
         (common_cu + ["-c", str(CSRC / "rsg_state.cu")], OUT / "rsg_state.o"),
+        (common_cu + ["-c", str(CSRC / "pn_noalloc.cu")], OUT / "pn_noalloc.o"),
         (common_cc + ["-c", str(CSRC / "pn_setup.cpp")], OUT / "pn_setup.o"),
         (common_cc + ["-c", str(CSRC / "pn_table.cpp")], OUT / "pn_table.o"),
         (common_cc + ["-c", str(CSRC / "pn_grid.cpp")], OUT / "pn_grid.o"),

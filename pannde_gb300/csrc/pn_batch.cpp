@@ -8,8 +8,11 @@
 // is the same alone and in any batch.  pn_batch_solve returns when the steps
 // are done (it waits for the GPU at the end of every signal-table chunk).
 #include <cstring>
+#include <mutex>
+#include <string>
 #include <type_traits>
 
+#include "pn_noalloc.hpp"
 #include "pn_solver.hpp"
 
 struct pn_batch {
@@ -66,11 +69,45 @@ void ensure_capacity(pn_batch *b, size_t args_bytes, size_t start_ints) {
   }
 }
 
-// steps all members can take with their current signal tables
-int32_t common_chunk(pn_batch *b, int32_t want) {
+// where one batch call stages the argument blocks and tile prefixes its
+// launches read: table form [0] velocity / [1] stress, grid form [0] even /
+// [1] odd step parity
+struct Staging {
+  void *args[2];
+  int *start[2];
+};
+
+// pn_batch_solve: the batch's own buffers, grown with cudaMalloc as needed
+struct GrownStaging {
+  pn_batch *b;
+  Staging operator()(size_t args_bytes, size_t start_ints) const {
+    ensure_capacity(b, args_bytes, start_ints);
+    return Staging{{b->d_args[0], b->d_args[1]}, {b->d_start[0], b->d_start[1]}};
+  }
+};
+
+// pn_batch_solve_noalloc: carved from the fixed device scratch (the caller
+// has checked that the call fits)
+struct ScratchStaging {
+  unsigned char *base;
+  static size_t round(size_t n) { return (n + 255) / 256 * 256; }
+  static size_t bytes(size_t args_bytes, size_t start_ints) {
+    return 2 * round(args_bytes) + 2 * round(start_ints * sizeof(int));
+  }
+  Staging operator()(size_t args_bytes, size_t start_ints) const {
+    const size_t a = round(args_bytes), st = round(start_ints * sizeof(int));
+    if (bytes(args_bytes, start_ints) > pn::kNoAllocScratchBytes)
+      throw pn::SetupError{PN_ERR_INVALID, "batch staging exceeds the fixed scratch"};
+    return Staging{{base, base + a}, {(int *)(base + 2 * a), (int *)(base + 2 * a + st)}};
+  }
+};
+
+// steps all members can take with their current signal tables (may_alloc
+// false: tables are refilled in place, never grown)
+int32_t common_chunk(pn_batch *b, int32_t want, bool may_alloc = true) {
   int32_t chunk = want;
   for (pn_solver *s : b->members) {
-    pn::ensure_signal_rows(s, chunk);
+    pn::ensure_signal_rows(s, chunk, may_alloc);
     if (!s->src.empty() && !s->sig_hold)
       chunk = (int32_t)std::min<int64_t>(chunk, s->sig_step0 + s->sig_rows - s->step);
   }
@@ -88,15 +125,15 @@ void advance(pn_batch *b, int32_t chunk) {
   }
 }
 
-template <typename T>
-void solve_table(pn_batch *b, int32_t nsteps, int precision) {
+template <typename T, typename Stage>
+void solve_table(pn_batch *b, int32_t nsteps, int precision, const Stage &stage, bool may_alloc) {
   const int n = (int)b->members.size();
   std::vector<pn::VelArgs<T>> va(n);
   std::vector<pn::StressArgs<T>> sa(n);
   std::vector<int> vs(n + 1, 0), ss(n + 1, 0);
   int32_t done = 0;
   while (done < nsteps) {
-    const int32_t chunk = common_chunk(b, nsteps - done);
+    const int32_t chunk = common_chunk(b, nsteps - done, may_alloc);
     for (int m = 0; m < n; m++) {
       pn_solver *s = b->members[m];
       pn::table_args<T>(s, va[m], sa[m]);
@@ -114,24 +151,24 @@ void solve_table(pn_batch *b, int32_t nsteps, int precision) {
       vs[m + 1] = vs[m] + (s->mesh.n_nodes + pn::kTile - 1) / pn::kTile;
       ss[m + 1] = ss[m] + (s->mesh.n_cells + pn::kTile - 1) / pn::kTile;
     }
-    ensure_capacity(b, std::max(sizeof(pn::VelArgs<T>), sizeof(pn::StressArgs<T>)) * n, n + 1);
-    pn::ck(cudaMemcpyAsync(b->d_args[0], va.data(), sizeof(pn::VelArgs<T>) * n, cudaMemcpyHostToDevice,
+    const Staging g = stage(std::max(sizeof(pn::VelArgs<T>), sizeof(pn::StressArgs<T>)) * n, n + 1);
+    pn::ck(cudaMemcpyAsync(g.args[0], va.data(), sizeof(pn::VelArgs<T>) * n, cudaMemcpyHostToDevice,
                            b->stream), "batch args");
-    pn::ck(cudaMemcpyAsync(b->d_args[1], sa.data(), sizeof(pn::StressArgs<T>) * n, cudaMemcpyHostToDevice,
+    pn::ck(cudaMemcpyAsync(g.args[1], sa.data(), sizeof(pn::StressArgs<T>) * n, cudaMemcpyHostToDevice,
                            b->stream), "batch args");
-    pn::ck(cudaMemcpyAsync(b->d_start[0], vs.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, b->stream),
+    pn::ck(cudaMemcpyAsync(g.start[0], vs.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, b->stream),
            "batch tiles");
-    pn::ck(cudaMemcpyAsync(b->d_start[1], ss.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, b->stream),
+    pn::ck(cudaMemcpyAsync(g.start[1], ss.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, b->stream),
            "batch tiles");
     int dev = 0, sms = 1;
     pn::ck(cudaGetDevice(&dev), "device");
     pn::ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "sm count");
     pn::BatchLaunch L;
     L.n_members = n;
-    L.vel_args = b->d_args[0];
-    L.str_args = b->d_args[1];
-    L.vel_start = b->d_start[0];
-    L.str_start = b->d_start[1];
+    L.vel_args = g.args[0];
+    L.str_args = g.args[1];
+    L.vel_start = g.start[0];
+    L.str_start = g.start[1];
     L.vel_tiles = vs[n];
     L.str_tiles = ss[n];
     // blocks walk the tiles: enough resident blocks for the GPU, never more than tiles
@@ -144,8 +181,8 @@ void solve_table(pn_batch *b, int32_t nsteps, int precision) {
   }
 }
 
-template <typename T>
-void solve_grid(pn_batch *b, int32_t nsteps, int precision) {
+template <typename T, typename Stage>
+void solve_grid(pn_batch *b, int32_t nsteps, int precision, const Stage &stage, bool may_alloc) {
   const int n = (int)b->members.size();
   std::vector<pn::GridArgs<T>> ga[2] = {std::vector<pn::GridArgs<T>>(n), std::vector<pn::GridArgs<T>>(n)};
   std::vector<int> bs(n + 1, 0);
@@ -155,7 +192,7 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision) {
   for (pn_solver *s : b->members) tma = tma && s->d_tmaps != nullptr;
   int32_t done = 0;
   while (done < nsteps) {
-    const int32_t chunk = common_chunk(b, nsteps - done);
+    const int32_t chunk = common_chunk(b, nsteps - done, may_alloc);
     for (int m = 0; m < n; m++) {
       pn_solver *s = b->members[m];
       pn::GridArgs<T> a;
@@ -188,17 +225,17 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision) {
       bs[m + 1] = (int)(bs[m] + blocks);
       sym = std::min(sym, s->sym);
     }
-    ensure_capacity(b, sizeof(pn::GridArgs<T>) * n, n + 1);
+    const Staging g = stage(sizeof(pn::GridArgs<T>) * n, n + 1);
     for (int p = 0; p < 2; p++)
-      pn::ck(cudaMemcpyAsync(b->d_args[p], ga[p].data(), sizeof(pn::GridArgs<T>) * n, cudaMemcpyHostToDevice,
+      pn::ck(cudaMemcpyAsync(g.args[p], ga[p].data(), sizeof(pn::GridArgs<T>) * n, cudaMemcpyHostToDevice,
                              b->stream), "batch args");
-    pn::ck(cudaMemcpyAsync(b->d_start[0], bs.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, b->stream),
+    pn::ck(cudaMemcpyAsync(g.start[0], bs.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, b->stream),
            "batch blocks");
     for (int32_t k = 0; k < chunk; k++) {
       pn::GridBatchLaunch L;
       L.n_members = n;
-      L.args = b->d_args[k & 1];
-      L.block_start = b->d_start[0];
+      L.args = g.args[k & 1];
+      L.block_start = g.start[0];
       L.total_blocks = bs[n];
       L.sym = sym;
       pn::ck(tma ? pn::launch_grid_tma_batch(L, precision, k, b->stream)
@@ -209,6 +246,35 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision) {
     advance(b, chunk);
     done += chunk;
   }
+}
+
+template <typename Stage>
+void solve_members(pn_batch *b, int32_t nsteps, const Stage &stage, bool may_alloc) {
+  const pn_solver *f = b->members.front();
+  if (f->form == PN_FORM_GRID) {
+    if (f->is_df64()) solve_grid<float2>(b, nsteps, f->precision, stage, may_alloc);
+    else if (f->esz == 8) solve_grid<double>(b, nsteps, f->precision, stage, may_alloc);
+    else solve_grid<float>(b, nsteps, f->precision, stage, may_alloc);
+  } else {
+    if (f->is_df64()) solve_table<float2>(b, nsteps, f->precision, stage, may_alloc);
+    else if (f->esz == 8) solve_table<double>(b, nsteps, f->precision, stage, may_alloc);
+    else solve_table<float>(b, nsteps, f->precision, stage, may_alloc);
+  }
+}
+
+// device bytes one batch call stages (ScratchStaging layout)
+size_t scratch_bytes(const pn_batch *b) {
+  const size_t n = b->members.size();
+  const pn_solver *f = b->members.front();
+  size_t args = 0;
+  if (f->form == PN_FORM_GRID)
+    args = f->is_df64() ? sizeof(pn::GridArgs<float2>) : f->esz == 8 ? sizeof(pn::GridArgs<double>)
+                                                                       : sizeof(pn::GridArgs<float>);
+  else
+    args = f->is_df64() ? std::max(sizeof(pn::VelArgs<float2>), sizeof(pn::StressArgs<float2>))
+         : f->esz == 8  ? std::max(sizeof(pn::VelArgs<double>), sizeof(pn::StressArgs<double>))
+                        : std::max(sizeof(pn::VelArgs<float>), sizeof(pn::StressArgs<float>));
+  return ScratchStaging::bytes(args * n, n + 1);
 }
 
 }  // namespace
@@ -271,16 +337,35 @@ int pn_batch_solve(pn_batch *b, int32_t nsteps) {
       pn::ck(cudaStreamSynchronize(s->stream), "member sync");  // members' own work first
       pn::refresh_sources(s);
     }
-    const pn_solver *f = b->members.front();
-    if (f->form == PN_FORM_GRID) {
-      if (f->is_df64()) solve_grid<float2>(b, nsteps, f->precision);
-      else if (f->esz == 8) solve_grid<double>(b, nsteps, f->precision);
-      else solve_grid<float>(b, nsteps, f->precision);
-    } else {
-      if (f->is_df64()) solve_table<float2>(b, nsteps, f->precision);
-      else if (f->esz == 8) solve_table<double>(b, nsteps, f->precision);
-      else solve_table<float>(b, nsteps, f->precision);
+    solve_members(b, nsteps, GrownStaging{b}, true);
+    return PN_OK;
+  });
+}
+
+int pn_batch_solve_noalloc(pn_batch *b, int32_t nsteps) {
+  return bguard([&]() -> int {
+    if (!b) return berr(PN_ERR_INVALID, "null batch");
+    if (nsteps < 0) return berr(PN_ERR_INVALID, "negative step count");
+    if (b->members.empty() || nsteps == 0) return PN_OK;
+    const size_t need = scratch_bytes(b);
+    if (need > pn::kNoAllocScratchBytes)
+      return berr(PN_ERR_INVALID, "pn_batch_solve_noalloc: " + std::to_string(b->members.size()) +
+                                      " members need " + std::to_string(need) + " bytes of argument scratch, more "
+                                      "than the fixed " + std::to_string(pn::kNoAllocScratchBytes) +
+                                      " bytes; use pn_batch_solve or a smaller batch");
+    for (size_t m = 0; m < b->members.size(); m++) {
+      pn_solver *s = b->members[m];
+      if (s->has_mask_sources()) return berr(PN_ERR_INVALID, "window-mask sources need pn_solver_solve_signals");
+      if (s->src_dirty || (!s->src.empty() && s->sig_alloc_rows == 0))
+        return berr(PN_ERR_INVALID, "pn_batch_solve_noalloc: member " + std::to_string(m) +
+                                        " has sources whose device tables are not built yet; one pn_batch_solve "
+                                        "or pn_solver_solve step builds them");
     }
+    std::lock_guard<std::mutex> lock(pn::noalloc_call_lock());
+    void *scratch = nullptr;
+    pn::ck(pn::noalloc_scratch(&scratch), "scratch symbol address");
+    for (pn_solver *s : b->members) pn::ck(cudaStreamSynchronize(s->stream), "member sync");
+    solve_members(b, nsteps, ScratchStaging{(unsigned char *)scratch}, false);
     return PN_OK;
   });
 }

@@ -15,7 +15,7 @@
 
 namespace pn {
 
-void ensure_signal_rows(pn_solver *s, int64_t nsteps) {
+void ensure_signal_rows(pn_solver *s, int64_t nsteps, bool may_alloc) {
   const int64_t nsig = (int64_t)s->src.size();
   if (nsig == 0 || s->caller_signals) return;  // caller rows cover the whole call
   const int64_t first = s->step, last = s->step + nsteps - 1;
@@ -23,8 +23,13 @@ void ensure_signal_rows(pn_solver *s, int64_t nsteps) {
     return;
   double tmax = -1e300;
   for (auto &sr : s->series) tmax = std::max(tmax, sr.last_time());
-  // rows for at least this call (capped), fewer once every signal holds
-  const int64_t want = std::min<int64_t>(std::max<int64_t>(nsteps, 1024), kSigRowsCap);
+  // rows for at least this call (capped), fewer once every signal holds;
+  // without allocation, at most the rows the table already has
+  int64_t want = std::min<int64_t>(std::max<int64_t>(nsteps, 1024), kSigRowsCap);
+  if (!may_alloc) {
+    if (s->sig_alloc_rows <= 0) throw SetupError{PN_ERR_INVALID, "signal table not resident"};
+    want = std::min<int64_t>(want, s->sig_alloc_rows);
+  }
   std::vector<double> rows;
   rows.reserve((size_t)want * nsig);
   double t = s->time;

@@ -247,7 +247,8 @@ struct pn_solver {
 namespace pn {
 
 // shared by both forms (pn_capi.cpp)
-void ensure_signal_rows(pn_solver *s, int64_t nsteps);
+// (may_alloc false: refill the resident table in place, never grow it)
+void ensure_signal_rows(pn_solver *s, int64_t nsteps, bool may_alloc = true);
 int64_t sig_row(const pn_solver *s, int64_t step_in_call);  // row of this step
 
 // table form (pn_table.cpp)

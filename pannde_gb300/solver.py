@@ -211,6 +211,11 @@ class Batch:
     def solve(self, nsteps: int):
         N.check(self._lib.pn_batch_solve(self._h, int(nsteps)))
 
+    def solve_noalloc(self, nsteps: int):
+        """pn_batch_solve_noalloc: the same steps staged in the library's fixed
+        device scratch, with no device allocation."""
+        N.check(self._lib.pn_batch_solve_noalloc(self._h, int(nsteps)))
+
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
             self._lib.pn_batch_destroy(self._h)
