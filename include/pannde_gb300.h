@@ -328,6 +328,16 @@ int pn_solver_get_info(pn_solver *s, pn_solver_info *info);
    form. */
 int pn_solver_device_state(pn_solver *s, void **V, void **S);
 
+/* Energy audit of the current state, formed and summed in FP64 whatever the
+   storage precision: kinetic = 1/2 sum_n m_n |V_n|^2 with the lumped nodal
+   mass m_n = rho_n dx_n dy_n dz_n (rho_n the reference's nodal density,
+   nodes of other partitions excluded); strain = 1/2 sum_c vol_c S_c . C_c+ S_c
+   with C_c+ the pseudo-inverse of the cell's Voigt stiffness (engineering
+   shear strain, so S . C+ S = sigma : epsilon; a fluid's missing shear
+   stiffness contributes nothing).  Synchronises.  No counterpart in the
+   reference: an audit the FP32 form reports beside its traces. */
+int pn_solver_energy(pn_solver *s, double *kinetic, double *strain);
+
 /* Block until all work enqueued by this solver is done; reports errors from
    the device-side checks. */
 int pn_solver_synchronize(pn_solver *s);

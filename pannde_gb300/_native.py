@@ -125,6 +125,7 @@ SIGNATURES = {
     "pn_solver_get_time": (c_int, [c_void_p, P_double]),
     "pn_solver_get_info": (c_int, [c_void_p, POINTER(PnSolverInfo)]),
     "pn_solver_device_state": (c_int, [c_void_p, POINTER(c_void_p), POINTER(c_void_p)]),
+    "pn_solver_energy": (c_int, [c_void_p, P_double, P_double]),
     "pn_solver_synchronize": (c_int, [c_void_p]),
     "pn_solver_enable_kernel_timing": (c_int, [c_void_p, c_int32]),
     "pn_solver_kernel_times": (c_int, [c_void_p, P_double, POINTER(c_int64)]),

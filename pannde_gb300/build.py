@@ -7,7 +7,9 @@ Sources (``pannde_gb300/csrc``):
   rsg_grid_tma.cu  grid step, tensor-copy staging  nvcc, sm_103a
   rsg_state.cu  state convert / permute       nvcc, sm_103a
   pn_noalloc.cu fixed scratch of the allocation-free batch solve   nvcc
-  pn_setup.cpp  host table construction       g++, -ffp-contract=off
+  rsg_energy.cu FP64 energy audit             nvcc, sm_103a
+  pn_energy.cpp energy audit tables           g++
+  pn_setup.cpp  host table construction       g++, -ffp-contract=off, OpenMP loops
   pn_table.cpp  table form (any hex mesh)     g++
   pn_grid.cpp   grid form (voxel meshes)      g++
   pn_capi.cpp   C ABI                         g++
@@ -48,7 +50,7 @@ def _jobs() -> list[tuple[list[str], Path]]:
     inc = ["-I", str(CSRC), "-I", str(HERE.parent / "include")]
     common_cu = [nvcc, "-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC", *inc]
     cxx = os.environ.get("CXX", "g++")
-    common_cc = [cxx, "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math",
+    common_cc = [cxx, "-std=c++17", "-O2", "-fPIC", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
                  "-I", str(cuda / "include"), *inc]
     jobs = [
         (common_cu + ["-c", str(CSRC / "rsg_fast.cu")], OUT / "rsg_fast.o"),
@@ -57,6 +59,8 @@ def _jobs() -> list[tuple[list[str], Path]]:
         (common_cu + ["-c", str(CSRC / "rsg_grid_tma.cu")], OUT / "rsg_grid_tma.o"),
         (common_cu + ["-c", str(CSRC / "rsg_state.cu")], OUT / "rsg_state.o"),
         (common_cu + ["-c", str(CSRC / "pn_noalloc.cu")], OUT / "pn_noalloc.o"),
+        (common_cu + ["-c", str(CSRC / "rsg_energy.cu")], OUT / "rsg_energy.o"),
+        (common_cc + ["-c", str(CSRC / "pn_energy.cpp")], OUT / "pn_energy.o"),
         (common_cc + ["-c", str(CSRC / "pn_setup.cpp")], OUT / "pn_setup.o"),
         (common_cc + ["-c", str(CSRC / "pn_table.cpp")], OUT / "pn_table.o"),
         (common_cc + ["-c", str(CSRC / "pn_grid.cpp")], OUT / "pn_grid.o"),
@@ -79,7 +83,7 @@ def build(verbose: bool = False) -> Path:
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         list(ex.map(lambda j: _run(j[0]), jobs))
     nvcc = str(_cuda_home() / "bin" / "nvcc")
-    link = [nvcc, "-shared", *ARCH, "-o", str(LIB)] + [str(o) for _, o in jobs]
+    link = [nvcc, "-shared", *ARCH, "-Xcompiler", "-fopenmp", "-o", str(LIB)] + [str(o) for _, o in jobs]
     _run(link)
     if verbose:
         print(f"built {LIB}", file=sys.stderr)

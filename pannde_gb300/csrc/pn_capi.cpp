@@ -535,6 +535,16 @@ int pn_solver_device_state(pn_solver *s, void **V, void **S) {
   return PN_OK;
 }
 
+int pn_solver_energy(pn_solver *s, double *kinetic, double *strain) {
+  return guarded([&]() -> int {
+    if (!s || !kinetic || !strain) return set_err(PN_ERR_INVALID, "null argument");
+    pn::ck(cudaStreamSynchronize(s->stream), "energy sync");
+    if (const int rc = pn::device_check(s)) return rc;
+    pn::energy(s, *kinetic, *strain);
+    return PN_OK;
+  });
+}
+
 int pn_solver_synchronize(pn_solver *s) {
   return guarded([&]() -> int {
     if (!s) return set_err(PN_ERR_INVALID, "null solver");

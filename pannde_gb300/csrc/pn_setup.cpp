@@ -17,10 +17,60 @@ namespace {
 bool near_equal(double a, double b) { return std::fabs(a - b) <= 1e-12 * std::fabs(b); }
 }  // namespace
 
+void pinv_sym6(const double *a, double *out) {
+  double m[6][6], v[6][6];
+  for (int i = 0; i < 6; i++)
+    for (int j = 0; j < 6; j++) {
+      m[i][j] = 0.5 * (a[i * 6 + j] + a[j * 6 + i]);
+      v[i][j] = i == j ? 1.0 : 0.0;
+    }
+  // cyclic Jacobi: rotate away each off-diagonal entry in turn until they vanish
+  for (int sweep = 0; sweep < 64; sweep++) {
+    double off = 0.0, diag = 0.0;
+    for (int i = 0; i < 6; i++) {
+      diag += m[i][i] * m[i][i];
+      for (int j = i + 1; j < 6; j++) off += m[i][j] * m[i][j];
+    }
+    if (off <= 1e-30 * diag || off == 0.0) break;
+    for (int p = 0; p < 6; p++)
+      for (int q = p + 1; q < 6; q++) {
+        if (m[p][q] == 0.0) continue;
+        const double theta = (m[q][q] - m[p][p]) / (2.0 * m[p][q]);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+        for (int k = 0; k < 6; k++) {  // columns p, q
+          const double mkp = m[k][p], mkq = m[k][q];
+          m[k][p] = c * mkp - sn * mkq;
+          m[k][q] = sn * mkp + c * mkq;
+        }
+        for (int k = 0; k < 6; k++) {  // rows p, q
+          const double mpk = m[p][k], mqk = m[q][k];
+          m[p][k] = c * mpk - sn * mqk;
+          m[q][k] = sn * mpk + c * mqk;
+        }
+        for (int k = 0; k < 6; k++) {
+          const double vkp = v[k][p], vkq = v[k][q];
+          v[k][p] = c * vkp - sn * vkq;
+          v[k][q] = sn * vkp + c * vkq;
+        }
+      }
+  }
+  double lmax = 0.0;
+  for (int i = 0; i < 6; i++) lmax = std::max(lmax, std::fabs(m[i][i]));
+  for (int i = 0; i < 6; i++)
+    for (int j = 0; j < 6; j++) {
+      double s = 0.0;
+      for (int k = 0; k < 6; k++)
+        if (std::fabs(m[k][k]) > 1e-12 * lmax) s += v[i][k] * v[j][k] / m[k][k];
+      out[i * 6 + j] = s;
+    }
+}
+
 bool all_finite(const double *p, int64_t n) {
-  for (int64_t i = 0; i < n; i++)
-    if (!std::isfinite(p[i])) return false;
-  return true;
+  bool ok = true;
+#pragma omp parallel for reduction(&& : ok) schedule(static)
+  for (int64_t i = 0; i < n; i++) ok = ok && std::isfinite(p[i]);
+  return ok;
 }
 
 void build_mesh_tables(const pn_mesh &m, MeshTables &t) {
@@ -36,11 +86,17 @@ void build_mesh_tables(const pn_mesh &m, MeshTables &t) {
   t.y.assign(m.y, m.y + nn);
   t.z.assign(m.z, m.z + nn);
   t.hex.assign(m.hexes, m.hexes + (size_t)nc * 8);
-  // HexMesh::setCell throws std::out_of_range for an invalid node id
-  for (size_t k = 0; k < t.hex.size(); k++) {
-    if (t.hex[k] < 0 || t.hex[k] >= nn)
+  // HexMesh::setCell throws std::out_of_range for an invalid node id (the
+  // first one in cell order is reported)
+  {
+    const int64_t nh = (int64_t)t.hex.size();
+    int64_t bad = nh;
+#pragma omp parallel for reduction(min : bad) schedule(static)
+    for (int64_t k = 0; k < nh; k++)
+      if (t.hex[(size_t)k] < 0 || t.hex[(size_t)k] >= nn) bad = std::min(bad, k);
+    if (bad < nh)
       fail(PN_ERR_RANGE, "invalid node id: Node count: " + std::to_string(nn) +
-                             ", provided index: " + std::to_string(t.hex[k]));
+                             ", provided index: " + std::to_string(t.hex[(size_t)bad]));
   }
   t.owned.assign(nn, 1);
   if (m.node_owner)
@@ -51,10 +107,34 @@ void build_mesh_tables(const pn_mesh &m, MeshTables &t) {
   for (int32_t c = 0; c < nc; c++)
     for (int k = 0; k < 8; k++) t.ncc[(size_t)t.hex[(size_t)c * 8 + k] * 8 + (k ^ 6)] = c;
 
-  // nodePrep (RightHex.hpp:272-309)
+  // nodePrep (RightHex.hpp:272-309): per axis, the extent of every corner of
+  // every incident cell around the node.  Min / max are exact, so taking them
+  // per cell first (the cell's corner box) and then over the node's cells
+  // gives the same numbers with 8 reads per node instead of 64.  Nodes are
+  // independent; the first node (in order) with a non-positive spacing
+  // decides the error, as in the reference's loop.
+  std::vector<double> box((size_t)nc * 6);
+#pragma omp parallel for schedule(static)
+  for (int32_t c = 0; c < nc; c++) {
+    double lo[3] = {1e308, 1e308, 1e308}, hi[3] = {-1e308, -1e308, -1e308};
+    for (int kbb = 0; kbb < 8; kbb++) {
+      const int32_t q = t.hex[(size_t)c * 8 + kbb];
+      const double pt[3] = {t.x[q], t.y[q], t.z[q]};
+      for (int kd = 0; kd < 3; kd++) {
+        lo[kd] = std::min(lo[kd], pt[kd]);
+        hi[kd] = std::max(hi[kd], pt[kd]);
+      }
+    }
+    for (int kd = 0; kd < 3; kd++) {
+      box[(size_t)c * 6 + kd] = lo[kd];
+      box[(size_t)c * 6 + 3 + kd] = hi[kd];
+    }
+  }
   t.dxn.resize(nn);
   t.dyn.resize(nn);
   t.dzn.resize(nn);
+  int64_t bad_node = nn;
+#pragma omp parallel for reduction(min : bad_node) schedule(static)
   for (int32_t n = 0; n < nn; n++) {
     const double node[3] = {t.x[n], t.y[n], t.z[n]};
     double lo[3] = {node[0], node[1], node[2]};
@@ -62,13 +142,9 @@ void build_mesh_tables(const pn_mesh &m, MeshTables &t) {
     for (int kb = 0; kb < 8; kb++) {
       const int32_t c = t.ncc[(size_t)n * 8 + kb];
       if (c == -1) continue;
-      for (int kbb = 0; kbb < 8; kbb++) {
-        const int32_t q = t.hex[(size_t)c * 8 + kbb];
-        const double pt[3] = {t.x[q], t.y[q], t.z[q]};
-        for (int kd = 0; kd < 3; kd++) {
-          lo[kd] = std::min(lo[kd], pt[kd]);
-          hi[kd] = std::max(hi[kd], pt[kd]);
-        }
+      for (int kd = 0; kd < 3; kd++) {
+        lo[kd] = std::min(lo[kd], box[(size_t)c * 6 + kd]);
+        hi[kd] = std::max(hi[kd], box[(size_t)c * 6 + 3 + kd]);
       }
     }
     for (int kd = 0; kd < 3; kd++) {
@@ -76,16 +152,19 @@ void build_mesh_tables(const pn_mesh &m, MeshTables &t) {
       if (hi[kd] == node[kd]) hi[kd] = 2. * node[kd] - lo[kd];
     }
     t.dxn[n] = 0.5 * (hi[0] - lo[0]);
-    if (0 >= t.dxn[n]) fail(PN_ERR_SPACING, "DX");
     t.dyn[n] = 0.5 * (hi[1] - lo[1]);
-    if (0 >= t.dyn[n]) fail(PN_ERR_SPACING, "DY");
     t.dzn[n] = 0.5 * (hi[2] - lo[2]);
-    if (0 >= t.dzn[n]) fail(PN_ERR_SPACING, "DZ");
+    if (0 >= t.dxn[n] || 0 >= t.dyn[n] || 0 >= t.dzn[n]) bad_node = std::min<int64_t>(bad_node, n);
+  }
+  if (bad_node < nn) {
+    const size_t n = (size_t)bad_node;
+    fail(PN_ERR_SPACING, 0 >= t.dxn[n] ? "DX" : 0 >= t.dyn[n] ? "DY" : "DZ");
   }
   // cellPrep (RightHex.hpp:253-264)
   t.dxc.resize(nc);
   t.dyc.resize(nc);
   t.dzc.resize(nc);
+#pragma omp parallel for schedule(static)
   for (int32_t c = 0; c < nc; c++) {
     const int32_t a = t.hex[(size_t)c * 8], b = t.hex[(size_t)c * 8 + 6];
     t.dxc[c] = t.x[b] - t.x[a];
@@ -98,10 +177,14 @@ void build_mesh_tables(const pn_mesh &m, MeshTables &t) {
     t.hx = t.dxc[0];
     t.hy = t.dyc[0];
     t.hz = t.dzc[0];
-    for (int32_t c = 0; c < nc && t.uniform; c++)
-      t.uniform = near_equal(t.dxc[c], t.hx) && near_equal(t.dyc[c], t.hy) && near_equal(t.dzc[c], t.hz);
-    for (int32_t n = 0; n < nn && t.uniform; n++)
-      t.uniform = near_equal(t.dxn[n], t.hx) && near_equal(t.dyn[n], t.hy) && near_equal(t.dzn[n], t.hz);
+    bool u = true;
+#pragma omp parallel for reduction(&& : u) schedule(static)
+    for (int32_t c = 0; c < nc; c++)
+      u = u && near_equal(t.dxc[c], t.hx) && near_equal(t.dyc[c], t.hy) && near_equal(t.dzc[c], t.hz);
+#pragma omp parallel for reduction(&& : u) schedule(static)
+    for (int32_t n = 0; n < nn; n++)
+      u = u && near_equal(t.dxn[n], t.hx) && near_equal(t.dyn[n], t.hy) && near_equal(t.dzn[n], t.hz);
+    t.uniform = u;
   }
 }
 
@@ -298,6 +381,7 @@ void build_source_entries(const MeshTables &t, const std::vector<pn_window_sourc
   if (ngf > 0) {
     // cell centres, HostRSGTDUT::cellcenter order (corner order, += 0.125*pt)
     std::vector<double> cc((size_t)t.n_cells * 3);
+#pragma omp parallel for schedule(static)
     for (int32_t c = 0; c < t.n_cells; c++) {
       double p[3] = {0., 0., 0.};
       for (int kb = 0; kb < 8; kb++) {
@@ -320,6 +404,7 @@ void build_source_entries(const MeshTables &t, const std::vector<pn_window_sourc
     const size_t nf = fsrc.size();
     std::vector<uint8_t> hit((size_t)t.n_cells * nf, 0);
     std::vector<uint8_t> any_cell(t.n_cells, 0);
+#pragma omp parallel for schedule(static)
     for (int32_t c = 0; c < t.n_cells; c++)
       for (size_t l = 0; l < nf; l++) {
         const int32_t i = fsrc[l];
@@ -395,6 +480,7 @@ void detect_grid(const MeshTables &t, GridMap &g, double max_void_fraction) {
     return;
   }
   double x0 = t.x[0], y0 = t.y[0], z0 = t.z[0];
+#pragma omp parallel for reduction(min : x0, y0, z0) schedule(static)
   for (int32_t n = 0; n < t.n_nodes; n++) {
     x0 = std::min(x0, t.x[n]);
     y0 = std::min(y0, t.y[n]);
@@ -407,15 +493,20 @@ void detect_grid(const MeshTables &t, GridMap &g, double max_void_fraction) {
     out = (int64_t)std::llround(f);
     return std::fabs(f - (double)out) <= 1e-6 && out >= 0 && out < (1 << 20);
   };
+  bool on = true;
+#pragma omp parallel for reduction(max : mi, mj, mk) reduction(&& : on) schedule(static)
   for (int32_t n = 0; n < t.n_nodes; n++) {
-    if (!lattice(t.x[n], x0, t.hx, gi[n]) || !lattice(t.y[n], y0, t.hy, gj[n]) ||
-        !lattice(t.z[n], z0, t.hz, gk[n])) {
-      g.why = "node off the lattice";
-      return;
-    }
+    const bool ok = lattice(t.x[n], x0, t.hx, gi[n]) && lattice(t.y[n], y0, t.hy, gj[n]) &&
+                    lattice(t.z[n], z0, t.hz, gk[n]);
+    on = on && ok;
+    if (!ok) continue;
     mi = std::max(mi, gi[n]);
     mj = std::max(mj, gj[n]);
     mk = std::max(mk, gk[n]);
+  }
+  if (!on) {
+    g.why = "node off the lattice";
+    return;
   }
   if (mi < 1 || mj < 1 || mk < 1) {
     g.why = "degenerate lattice";
@@ -438,36 +529,43 @@ void detect_grid(const MeshTables &t, GridMap &g, double max_void_fraction) {
   g.pnx = (int32_t)pnx;
   g.pcx = (int32_t)pcx;
   g.node_grid.resize(t.n_nodes);
+#pragma omp parallel for schedule(static)
+  for (int32_t n = 0; n < t.n_nodes; n++) g.node_grid[n] = g.node_at(gi[n], gj[n], gk[n]);
   std::vector<uint8_t> taken((size_t)g.node_sites(), 0);
   for (int32_t n = 0; n < t.n_nodes; n++) {
-    const int64_t q = g.node_at(gi[n], gj[n], gk[n]);
-    if (taken[q]) {
+    uint8_t &site = taken[(size_t)g.node_grid[n]];
+    if (site) {
       g.why = "two nodes on one lattice site";
       return;
     }
-    taken[q] = 1;
-    g.node_grid[n] = q;
+    site = 1;
   }
   static const int bx[8] = {0, 1, 1, 0, 0, 1, 1, 0}, by[8] = {0, 0, 1, 1, 0, 0, 1, 1},
                    bz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
   g.cell_grid.resize(t.n_cells);
-  std::vector<uint8_t> ctaken((size_t)g.cell_sites(), 0);
+  bool boxes = true;
+#pragma omp parallel for reduction(&& : boxes) schedule(static)
   for (int32_t c = 0; c < t.n_cells; c++) {
     const int32_t *h = &t.hex[(size_t)c * 8];
     const int64_t i0 = gi[h[0]], j0 = gj[h[0]], k0 = gk[h[0]];
-    for (int kb = 0; kb < 8; kb++) {
-      if (gi[h[kb]] != i0 + bx[kb] || gj[h[kb]] != j0 + by[kb] || gk[h[kb]] != k0 + bz[kb]) {
-        g.why = "cell is not a lattice box in corner order";
-        return;
-      }
-    }
-    const int64_t q = g.cell_at(i0, j0, k0);
-    if (ctaken[q]) {
+    bool box = true;
+    for (int kb = 0; kb < 8; kb++)
+      box = box && gi[h[kb]] == i0 + bx[kb] && gj[h[kb]] == j0 + by[kb] && gk[h[kb]] == k0 + bz[kb];
+    boxes = boxes && box;
+    g.cell_grid[c] = box ? g.cell_at(i0, j0, k0) : 0;
+  }
+  if (!boxes) {
+    g.why = "cell is not a lattice box in corner order";
+    return;
+  }
+  std::vector<uint8_t> ctaken((size_t)g.cell_sites(), 0);
+  for (int32_t c = 0; c < t.n_cells; c++) {
+    uint8_t &site = ctaken[(size_t)g.cell_grid[c]];
+    if (site) {
       g.why = "two cells on one lattice site";
       return;
     }
-    ctaken[q] = 1;
-    g.cell_grid[c] = q;
+    site = 1;
   }
   g.ok = true;
 }

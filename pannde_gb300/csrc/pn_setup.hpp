@@ -132,6 +132,11 @@ void tile_ranges(const std::vector<int32_t> &elems, int32_t n_elems, int tile,
 // NaN / Inf scan.
 bool all_finite(const double *p, int64_t n);
 
+// Moore-Penrose pseudo-inverse of a symmetric 6x6 matrix (row-major), by the
+// cyclic Jacobi eigenvalue method; eigenvalues below 1e-12 of the largest are
+// treated as zero (a fluid's stiffness has no shear part).
+void pinv_sym6(const double *a, double *out);
+
 // Split a double into the (hi, lo) float pair of the double-float form:
 // hi = the nearest float, lo = the nearest float to the remainder.
 inline void split_df(double d, float &hi, float &lo) {

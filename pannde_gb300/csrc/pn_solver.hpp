@@ -87,6 +87,10 @@ struct pn_solver {
   void *d_tmaps = nullptr;   // tensor maps [2 input parities] (null: classic kernel)
   int32_t *d_err = nullptr;  // device error word of the grid kernels
 
+  // energy audit tables (pn_energy.cpp; built on the first call)
+  double *d_emass = nullptr, *d_evol = nullptr, *d_ecomp = nullptr, *d_epart = nullptr;
+  int64_t e_nodes = 0, e_cells = 0;
+
   // sources (both forms)
   std::vector<pn_window_source> src;
   std::vector<std::vector<double>> src_t, src_v;  // owned copies of signal arrays
@@ -285,6 +289,9 @@ void refresh_sources(pn_solver *s);
 
 // the calling thread's message for pn_last_error(); returns code (pn_capi.cpp)
 int set_last_error(int code, const std::string &msg);
+
+// FP64 kinetic and strain energy of the current state (pn_energy.cpp)
+void energy(pn_solver *s, double &kinetic, double &strain);
 
 // PN_ERR_DEVICE_CHECK (and the word cleared) when a kernel recorded an error
 // in the solver's device error word; the stream must be synchronised

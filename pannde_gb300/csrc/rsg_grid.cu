@@ -27,6 +27,7 @@
 // The apron node row/column is computed by both neighbouring tiles
 // (identical inputs, identical result) and written only by its owner.
 #include <algorithm>
+#include <cstdlib>
 #include <cstdint>
 
 #include "df64.cuh"
@@ -399,7 +400,15 @@ int grid_tile_y() { return 8; }
 
 int grid_chunk_for(int nz, long long xy_blocks, int sms, int per_sm) {
   if (nz <= 0) return 1;
-  const long long want = 4LL * sms * per_sm;
+  // tuning override: PN_GRID_KCHUNK cell layers per chunk
+  if (const char *v = std::getenv("PN_GRID_KCHUNK")) {
+    const int k = std::atoi(v);
+    if (k > 0) return std::min(std::min(k, kGridChunkMax), nz);
+  }
+  // Each chunk re-marches two layers (the partial sums below it, the node
+  // layer above it), which costs more than a partly empty last wave: split
+  // columns only as far as one wave of resident blocks needs.
+  const long long want = (long long)sms * per_sm;
   long long chunks = (want + xy_blocks - 1) / xy_blocks;
   chunks = std::max(1LL, std::min(chunks, (long long)std::max(1, nz / 4)));
   chunks = std::max(chunks, (long long)((nz + kGridChunkMax - 1) / kGridChunkMax));

@@ -57,7 +57,7 @@ constexpr int kGridTmaRowsMax = 32;   // stiffness rows the tensor-copy kernel s
 
 int grid_tile_x();
 int grid_tile_y();
-// cell layers per z chunk: about four waves of blocks, at least four layers,
+// cell layers per z chunk: about one wave of blocks, at least four layers,
 // at most kGridChunkMax
 int grid_chunk_for(int nz, long long xy_blocks, int sms, int per_sm);
 // cell layers per z chunk the launcher picks for this lattice, precision and

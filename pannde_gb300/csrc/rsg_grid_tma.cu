@@ -30,6 +30,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 
 #include "df64.cuh"
@@ -508,6 +509,17 @@ EncodeTiled encoder() {
   return fn;
 }
 
+// L2 sector promotion of the tile copies (tuning override PN_TMA_L2_PROMOTION
+// = 0, 64, 128 or 256 bytes; default 128)
+CUtensorMapL2promotion l2_promotion() {
+  const char *v = std::getenv("PN_TMA_L2_PROMOTION");
+  const int b = v ? std::atoi(v) : 128;
+  return b == 0 ? CU_TENSOR_MAP_L2_PROMOTION_NONE
+       : b == 64 ? CU_TENSOR_MAP_L2_PROMOTION_L2_64B
+       : b == 256 ? CU_TENSOR_MAP_L2_PROMOTION_L2_256B
+                  : CU_TENSOR_MAP_L2_PROMOTION_L2_128B;
+}
+
 // 3-D tile map over a pitched lattice buffer: dims (d0, d1, d2) sites, rows of
 // `pitch` sites, box (b0, b1, 1)
 bool encode3(CUtensorMap *m, CUtensorMapDataType dt, int esz, const void *ptr, int64_t d0, int64_t d1,
@@ -520,8 +532,7 @@ bool encode3(CUtensorMap *m, CUtensorMapDataType dt, int esz, const void *ptr, i
   const cuuint32_t box[3] = {(cuuint32_t)b0, (cuuint32_t)b1, 1};
   const cuuint32_t es[3] = {1, 1, 1};
   return fn(m, dt, 3, const_cast<void *>(ptr), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+            CU_TENSOR_MAP_SWIZZLE_NONE, l2_promotion(), CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 template <int ESZ>

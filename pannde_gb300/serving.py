@@ -3,13 +3,14 @@
 Requests arrive over time; each is a plate solve with its own mesh size,
 material, transducer and step count.  The loop
 
-* admits an arrived request when its device footprint (pn_plan_solver, no
-  allocation) fits in the free part of the HBM budget, creating its solver
-  (fields stay resident on the device until it finishes);
-* advances every admitted request together (pn_batch_solve: one launch per
-  step covers all of them), in quanta that end exactly when the next request
-  finishes, so requests that arrive while others run join the batch at the
-  next quantum;
+* prepares an arrived request (its solver: host tables, device upload) on a
+  background thread when its device footprint (pn_plan_solver, no
+  allocation) fits in the free part of the HBM budget;
+* admits prepared requests into the running batch while the GPU is not
+  saturated, and advances every admitted request together (pn_batch_solve:
+  one launch per step covers all of them), in quanta that end exactly when
+  the next request finishes, so requests that arrive while others run join
+  the batch at the next quantum;
 * retires finished requests (downloads their sensor traces, frees their
   memory) and records their latency from arrival to completion.
 
@@ -69,53 +70,105 @@ def plan_bytes(case: cases.Case, precision: str, form: str = "auto") -> int:
 
 
 class Server:
-    """Continuous-batching request loop on the current CUDA device."""
+    """Continuous-batching request loop on the current CUDA device.
+
+    * ``prepare_threads`` preparation threads build the solvers of arrived
+      requests (host tables, device upload, sources, sensors) while the GPU
+      works on the admitted ones, each as soon as its footprint fits in the
+      free HBM budget (taken in arrival order); at most ``prepare_ahead``
+      prepared solvers wait for admission.
+    * The GPU loop admits prepared solvers while the admitted set holds fewer
+      than ``saturation_cells`` cells (one step launch over that many cells
+      keeps the GPU busy; sharing it further only delays everyone), then
+      advances the batch in quanta that end when the next request finishes.
+    * A finished request's traces are read back, its memory freed, and its
+      latency (arrival to traces) recorded.
+    """
 
     def __init__(self, hbm_budget_bytes: int, precision: str = "f32", quantum: int = 250,
+                 saturation_cells: int = 8_000_000, prepare_ahead: int = 2, prepare_threads: int = 2,
                  clock: Callable[[], float] = time.perf_counter):
         self.budget = int(hbm_budget_bytes)
         self.precision = precision
         self.quantum = int(quantum)
+        self.saturation = int(saturation_cells)
+        self.ahead = int(prepare_ahead)
+        self.threads = max(1, int(prepare_threads))
         self.clock = clock
 
     def run(self, requests: list[Request], on_admit=None) -> tuple[list[Result], dict]:
+        import queue
+        import threading
+
         pending = sorted(requests, key=lambda r: (r.arrival, r.rid))
-        results: list[Result] = []
-        active: dict[int, dict] = {}
-        used = 0
+        ready: "queue.Queue" = queue.Queue()
+        lock = threading.Condition()
+        state = dict(used=0, prepared=0, error=None, next=0)
+        device = _current_device()
         t0 = self.clock()
-        steps_done = 0
-        cell_steps = 0
-        max_active = 0
-        with Batch() as batch:
-            while pending or active:
-                now = self.clock() - t0
-                # admit arrived requests that fit (first come, first served)
-                while pending and pending[0].arrival <= now:
-                    r = pending[0]
+
+        def prepare():
+            try:
+                _set_device(device)  # solvers live on the caller's current device
+                while True:
+                    with lock:  # the next request, in arrival order
+                        if state["next"] >= len(pending) or state["error"] is not None:
+                            return
+                        r = pending[state["next"]]
+                        state["next"] += 1
+                    with lock:
+                        while self.clock() - t0 < r.arrival:
+                            lock.wait(timeout=min(0.05, max(0.001, r.arrival - (self.clock() - t0))))
                     need = plan_bytes(r.case, self.precision)
                     if need > self.budget:
                         raise ValueError(f"request {r.rid} needs {need} bytes, more than the budget")
-                    if used + need > self.budget:
-                        break
-                    pending.pop(0)
+                    with lock:
+                        while (self.clock() - t0 < r.arrival or state["used"] + need > self.budget
+                               or state["prepared"] >= self.ahead):
+                            lock.wait(timeout=max(0.0, min(0.05, r.arrival - (self.clock() - t0))) or 0.01)
+                        state["used"] += need
+                        state["prepared"] += 1
                     s = Solver.from_case(r.case, precision=self.precision, capacity=r.nsteps)
+                    ready.put((r, s, need))
+            except BaseException as e:  # surfaced by the GPU loop
+                state["error"] = e
+                ready.put(None)
+
+        workers = [threading.Thread(target=prepare, daemon=True) for _ in range(self.threads)]
+        for th in workers:
+            th.start()
+        results: list[Result] = []
+        active: dict[int, dict] = {}
+        cell_steps = 0
+        max_active = 0
+        done = 0
+        with Batch() as batch:
+            while done < len(pending):
+                # admit prepared solvers while the GPU is not saturated
+                while True:
+                    cells = sum(a["req"].case.mesh.n_cells for a in active.values())
+                    if active and cells >= self.saturation:
+                        break
+                    try:
+                        item = ready.get(timeout=0.05) if not active else ready.get_nowait()
+                    except queue.Empty:
+                        break
+                    if item is None:
+                        raise state["error"]
+                    r, s, need = item
                     batch.add(s)
-                    used += need
-                    active[r.rid] = dict(req=r, solver=s, left=r.nsteps, need=need,
-                                         admitted=self.clock() - t0)
+                    now = self.clock() - t0
+                    active[r.rid] = dict(req=r, solver=s, left=r.nsteps, need=need, admitted=now)
+                    with lock:
+                        state["prepared"] -= 1
+                        lock.notify_all()
                     if on_admit:
                         on_admit(r, now)
                 if not active:
-                    # idle until the next arrival
-                    wait = pending[0].arrival - (self.clock() - t0)
-                    if wait > 0:
-                        time.sleep(min(wait, 0.05))
                     continue
                 max_active = max(max_active, len(active))
                 q = min(self.quantum, min(a["left"] for a in active.values()))
                 batch.solve(q)
-                steps_done += q
                 cell_steps += q * sum(a["req"].case.mesh.n_cells for a in active.values())
                 for rid in list(active):
                     a = active[rid]
@@ -127,8 +180,13 @@ class Server:
                         results.append(Result(rid, a["req"].arrival, a["admitted"], self.clock() - t0,
                                               a["req"].nsteps, a["req"].case.mesh.n_cells, tr, s.time))
                         s.close()
-                        used -= a["need"]
                         del active[rid]
+                        done += 1
+                        with lock:
+                            state["used"] -= a["need"]
+                            lock.notify_all()
+        for th in workers:
+            th.join(timeout=5.0)
         elapsed = self.clock() - t0
         lat = np.array([r.latency for r in results]) if results else np.zeros(1)
         stats = dict(requests=len(results), elapsed_s=elapsed,
@@ -137,6 +195,20 @@ class Server:
                      gcell_steps_per_s=cell_steps / elapsed / 1e9 if elapsed > 0 else 0.0,
                      max_active=max_active)
         return sorted(results, key=lambda r: r.rid), stats
+
+
+def _current_device():
+    try:
+        import torch
+        return torch.cuda.current_device() if torch.cuda.is_available() else None
+    except ImportError:
+        return None
+
+
+def _set_device(device):
+    if device is not None:
+        import torch
+        torch.cuda.set_device(device)
 
 
 def run_sequential(requests: list[Request], precision: str = "f64") -> tuple[list[Result], dict]:

@@ -178,6 +178,12 @@ class Solver:
         N.check(self._lib.pn_solver_kernel_times(self._h, ms, n))
         return {"velocity": (ms[0], n[0]), "stress": (ms[1], n[1]), "grid_step": (ms[2], n[2])}
 
+    def energy(self):
+        """(kinetic, strain) energy of the current state, in FP64 (pn_solver_energy)."""
+        k, e = c_double(0.0), c_double(0.0)
+        N.check(self._lib.pn_solver_energy(self._h, ctypes.byref(k), ctypes.byref(e)))
+        return k.value, e.value
+
     def synchronize(self):
         N.check(self._lib.pn_solver_synchronize(self._h))
 

@@ -11,12 +11,13 @@ from pannde_gb300.solver import Solver
 pytestmark = pytest.mark.gpu
 
 
-def small_requests(n=6, seed=3):
+def small_requests(n=6, seed=3, gap=0.005, steps=(500, 900)):
+    """Small plates arriving almost together: each runs for many quanta, so the
+    later ones are prepared and admitted while the first ones are on the GPU."""
     rng = np.random.default_rng(seed)
     reqs = []
     for i in range(n):
-        reqs.append(serving.mapod_request(i, 0.02 * i, rng, cells_range=(2e4, 1.5e5),
-                                          steps_range=(80, 260)))
+        reqs.append(serving.mapod_request(i, gap * i, rng, cells_range=(2e4, 1.5e5), steps_range=steps))
     return reqs
 
 
@@ -27,7 +28,7 @@ def rel_l2(a, b):
 
 def test_results_same_alone_and_in_the_mix(cuda_device):
     reqs = small_requests()
-    srv = serving.Server(hbm_budget_bytes=8 << 30, precision="f32", quantum=40)
+    srv = serving.Server(hbm_budget_bytes=8 << 30, precision="f32", quantum=40, prepare_ahead=6)
     results, stats = srv.run(reqs)
     assert stats["requests"] == len(reqs) and stats["max_active"] >= 2
     for r, q in zip(results, sorted(reqs, key=lambda q: q.rid)):
