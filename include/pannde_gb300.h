@@ -397,6 +397,14 @@ int pn_batch_solve(pn_batch *b, int32_t nsteps);
    pn_batch_solve. */
 int pn_batch_solve_noalloc(pn_batch *b, int32_t nsteps);
 int pn_batch_synchronize(pn_batch *b);
+/* Launch planning of pn_batch_solve: the launch shape (how one step's work is
+   spread over the GPU) is autotuned once per class of batch (form,
+   precision, member count and work size) by timing candidates on real steps,
+   and a chunk of steps whose launch sequence repeats the previous chunk's is
+   captured as a CUDA graph and replayed (work on a created stream only).
+   Neither changes results.  Reports the graph replays and captures so far
+   and the number of tuned classes (any pointer may be NULL). */
+int pn_batch_plan_stats(pn_batch *b, int64_t *graph_launches, int64_t *graph_captures, int32_t *tuned_classes);
 int pn_batch_destroy(pn_batch *b);
 
 /* Free all device memory of the solver. */

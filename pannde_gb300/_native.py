@@ -137,6 +137,7 @@ SIGNATURES = {
     "pn_batch_set_stream": (c_int, [c_void_p, c_void_p]),
     "pn_batch_solve": (c_int, [c_void_p, c_int32]),
     "pn_batch_solve_noalloc": (c_int, [c_void_p, c_int32]),
+    "pn_batch_plan_stats": (c_int, [c_void_p, POINTER(c_int64), POINTER(c_int64), P_int32]),
     "pn_batch_synchronize": (c_int, [c_void_p]),
     "pn_batch_destroy": (c_int, [c_void_p]),
 }

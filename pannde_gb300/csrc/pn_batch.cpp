@@ -7,13 +7,24 @@
 // arithmetic of a member does not depend on the others, so a member's result
 // is the same alone and in any batch.  pn_batch_solve returns when the steps
 // are done (it waits for the GPU at the end of every signal-table chunk).
+#include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <type_traits>
 
 #include "pn_noalloc.hpp"
 #include "pn_solver.hpp"
+
+// The launch sequence of one chunk, as far as a CUDA graph of it depends on it
+// (kernel arguments are device pointers to the staged blocks plus the step).
+struct ChunkSignature {
+  int form, precision, n, shape, chunk, total0, total1, sym, tma;
+  const void *p[4];
+  bool operator==(const ChunkSignature &o) const { return std::memcmp(this, &o, sizeof(*this)) == 0; }
+};
 
 struct pn_batch {
   std::vector<pn_solver *> members;
@@ -23,7 +34,18 @@ struct pn_batch {
   int *d_start[2] = {nullptr, nullptr};
   size_t cap_args = 0, cap_start = 0;
 
+  // autotuner: launch shape chosen per (form, precision, member-count and
+  // work-size class), by timing the candidates on real steps
+  std::map<std::tuple<int, int, int, int>, int> tuned;
+  // CUDA graph of the last chunk whose launch sequence repeated
+  bool seen = false;
+  ChunkSignature last{};
+  cudaGraphExec_t exec = nullptr;
+  ChunkSignature exec_sig{};
+  int64_t graph_launches = 0, graph_captures = 0;
+
   ~pn_batch() {
+    if (exec) cudaGraphExecDestroy(exec);
     for (int k = 0; k < 2; k++) {
       if (d_args[k]) cudaFree(d_args[k]);
       if (d_start[k]) cudaFree(d_start[k]);
@@ -114,6 +136,93 @@ int32_t common_chunk(pn_batch *b, int32_t want, bool may_alloc = true) {
   return std::max<int32_t>(chunk, 1);
 }
 
+// ---- launch planning: autotuned shapes and graph replay -------------------
+//
+// A "shape" is how the work of one step is spread over the GPU; it never
+// changes what a member computes (every node and cell is updated by one
+// thread with the same arithmetic), only how fast:
+//   table form  resident blocks per SM of the tile-walking kernels
+//   grid form   z chunks per tile column (blocks = tiles x chunks)
+// The first chunk of a new (form, precision, members, work) class long
+// enough for it runs two steps with each candidate, timed with CUDA events on
+// the batch stream, and keeps the fastest for the rest of the chunk and for
+// later chunks of the class.  A chunk whose launch sequence equals the
+// previous chunk's is captured as a CUDA graph and replayed from then on
+// (work on a created stream only; the legacy default stream cannot be
+// captured).  Neither runs in the allocation-free solve.
+constexpr int kTableShapes[] = {8, 4, 16, 2};  // blocks per SM
+constexpr int kGridShapes[] = {0, 1, 2};       // 0: the launcher's choice; else chunks per column
+constexpr int kTunePerShape = 2;               // timed steps per candidate
+
+int log2_class(int64_t v) { return v <= 1 ? 0 : (int)std::log2((double)v); }
+
+template <typename Prepare, typename Launch>
+void run_chunk(pn_batch *b, std::tuple<int, int, int, int> cls, int n_shapes, int32_t chunk, bool may_plan,
+               ChunkSignature sig, Prepare &&prepare, Launch &&launch) {
+  int32_t k = 0;
+  auto it = b->tuned.find(cls);
+  int best = it == b->tuned.end() ? -1 : it->second;
+  if (best < 0 && may_plan && n_shapes > 1 && chunk >= n_shapes * kTunePerShape + 1) {
+    cudaEvent_t ev[2 * 4];
+    for (int c = 0; c < 2 * n_shapes; c++) pn::ck(cudaEventCreate(&ev[c]), "tune event");
+    for (int c = 0; c < n_shapes; c++) {
+      prepare(c);
+      pn::ck(cudaEventRecord(ev[2 * c], b->stream), "tune event");
+      for (int j = 0; j < kTunePerShape; j++) launch(c, k++);
+      pn::ck(cudaEventRecord(ev[2 * c + 1], b->stream), "tune event");
+    }
+    pn::ck(cudaStreamSynchronize(b->stream), "tune sync");
+    float best_ms = 0.f;
+    for (int c = 0; c < n_shapes; c++) {
+      float ms = 0.f;
+      pn::ck(cudaEventElapsedTime(&ms, ev[2 * c], ev[2 * c + 1]), "tune time");
+      if (best < 0 || ms < best_ms) {
+        best = c;
+        best_ms = ms;
+      }
+    }
+    for (int c = 0; c < 2 * n_shapes; c++) cudaEventDestroy(ev[c]);
+    b->tuned[cls] = best;
+  }
+  if (best < 0) best = 0;
+  const int units = prepare(best);  // work units of the shape (part of the launch sequence)
+  if (k == 0 && may_plan && b->stream != nullptr) {
+    sig.shape = best;
+    sig.chunk = chunk;
+    sig.total1 += units;
+    if (b->exec && sig == b->exec_sig) {
+      pn::ck(cudaGraphLaunch(b->exec, b->stream), "graph launch");
+      b->graph_launches++;
+      return;
+    }
+    if (b->seen && sig == b->last) {  // second time in a row: capture, then replay
+      cudaGraph_t graph = nullptr;
+      pn::ck(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "capture");
+      try {
+        for (; k < chunk; k++) launch(best, k);
+      } catch (...) {
+        cudaStreamEndCapture(b->stream, &graph);
+        if (graph) cudaGraphDestroy(graph);
+        throw;
+      }
+      pn::ck(cudaStreamEndCapture(b->stream, &graph), "capture end");
+      if (b->exec) cudaGraphExecDestroy(b->exec);
+      b->exec = nullptr;
+      const cudaError_t e = cudaGraphInstantiate(&b->exec, graph, 0);
+      cudaGraphDestroy(graph);
+      pn::ck(e, "graph instantiate");
+      b->exec_sig = sig;
+      b->graph_captures++;
+      pn::ck(cudaGraphLaunch(b->exec, b->stream), "graph launch");
+      b->graph_launches++;
+      return;
+    }
+    b->seen = true;
+    b->last = sig;
+  }
+  for (; k < chunk; k++) launch(best, k);
+}
+
 // per-member bookkeeping after `chunk` steps (time accumulated step by step,
 // as solve() does)
 void advance(pn_batch *b, int32_t chunk) {
@@ -171,10 +280,27 @@ void solve_table(pn_batch *b, int32_t nsteps, int precision, const Stage &stage,
     L.str_start = g.start[1];
     L.vel_tiles = vs[n];
     L.str_tiles = ss[n];
-    // blocks walk the tiles: enough resident blocks for the GPU, never more than tiles
-    L.blocks_vel = std::min(vs[n], sms * 8);
-    L.blocks_str = std::min(ss[n], sms * 8);
-    for (int32_t k = 0; k < chunk; k++) pn::ck(pn::launch_table_batch(L, precision, k, b->stream), "batch step");
+    // blocks walk the tiles: resident blocks per SM by the tuned shape, never more than tiles
+    auto shape = [&](int c) {
+      L.blocks_vel = std::min(vs[n], sms * kTableShapes[c]);
+      L.blocks_str = std::min(ss[n], sms * kTableShapes[c]);
+      return 0;
+    };
+    ChunkSignature sig{};
+    sig.form = PN_FORM_TABLE;
+    sig.precision = precision;
+    sig.n = n;
+    sig.total0 = vs[n];
+    sig.total1 = ss[n];
+    sig.p[0] = g.args[0];
+    sig.p[1] = g.args[1];
+    sig.p[2] = g.start[0];
+    sig.p[3] = g.start[1];
+    run_chunk(b, std::make_tuple((int)PN_FORM_TABLE, precision, log2_class(n), log2_class(vs[n] + ss[n])),
+              (int)(sizeof(kTableShapes) / sizeof(int)), chunk, may_alloc, sig, shape, [&](int c, int32_t k) {
+                shape(c);
+                pn::ck(pn::launch_table_batch(L, precision, k, b->stream), "batch step");
+              });
     pn::ck(cudaStreamSynchronize(b->stream), "batch chunk");  // staging is reused next chunk
     advance(b, chunk);
     done += chunk;
@@ -193,55 +319,80 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision, const Stage &stage, 
   int32_t done = 0;
   while (done < nsteps) {
     const int32_t chunk = common_chunk(b, nsteps - done, may_alloc);
-    for (int m = 0; m < n; m++) {
-      pn_solver *s = b->members[m];
-      pn::GridArgs<T> a;
-      pn::grid_args<T>(s, a);
-      const int64_t nsig = (int64_t)s->src.size();
-      if (nsig > 0) {
-        const int64_t row0 = pn::sig_row(s, 0);
-        a.sigval = (const T *)s->d_sig + row0 * nsig;
-        a.sig_stride = (int32_t)nsig;
-        a.sig_rows = (int32_t)(s->sig_rows - row0);
-      }
-      a.rec = s->rec_count;
-      a.kchunk = pn::grid_chunk_layers(precision, a.nx, a.ny, a.nz, tma);
-      for (int p = 0; p < 2; p++) {  // step parity: buffers swap every step
-        pn::GridArgs<T> q = a;
-        const int in = s->cur ^ p, out = in ^ 1;
-        q.tmaps = tma ? pn::grid_maps_for(s, in) : nullptr;
-        for (int c = 0; c < 3; c++) {
-          q.V_in[c] = (const T *)s->V[in][c];
-          q.V_out[c] = (T *)s->V[out][c];
+    // argument blocks of every member for z-chunk shape c (0: the launcher's
+    // choice, else c chunks per column), both step parities, staged
+    Staging g{};
+    int staged_shape = -1;
+    auto prepare = [&](int c) {
+      if (c == staged_shape) return bs[n];
+      for (int m = 0; m < n; m++) {
+        pn_solver *s = b->members[m];
+        pn::GridArgs<T> a;
+        pn::grid_args<T>(s, a);
+        const int64_t nsig = (int64_t)s->src.size();
+        if (nsig > 0) {
+          const int64_t row0 = pn::sig_row(s, 0);
+          a.sigval = (const T *)s->d_sig + row0 * nsig;
+          a.sig_stride = (int32_t)nsig;
+          a.sig_rows = (int32_t)(s->sig_rows - row0);
         }
-        for (int c = 0; c < 6; c++) {
-          q.S_in[c] = (const T *)s->S[in][c];
-          q.S_out[c] = (T *)s->S[out][c];
+        a.rec = s->rec_count;
+        const int per = kGridShapes[c];
+        a.kchunk = per == 0 ? pn::grid_chunk_layers(precision, a.nx, a.ny, a.nz, tma)
+                            : std::min(pn::kGridChunkMax, std::max(1, (a.nz + per - 1) / per));
+        for (int p = 0; p < 2; p++) {  // step parity: buffers swap every step
+          pn::GridArgs<T> q = a;
+          const int in = s->cur ^ p, out = in ^ 1;
+          q.tmaps = tma ? pn::grid_maps_for(s, in) : nullptr;
+          for (int cc = 0; cc < 3; cc++) {
+            q.V_in[cc] = (const T *)s->V[in][cc];
+            q.V_out[cc] = (T *)s->V[out][cc];
+          }
+          for (int cc = 0; cc < 6; cc++) {
+            q.S_in[cc] = (const T *)s->S[in][cc];
+            q.S_out[cc] = (T *)s->S[out][cc];
+          }
+          ga[p][m] = q;
         }
-        ga[p][m] = q;
+        const int64_t blocks = (int64_t)(a.nx / (tx - 1) + 1) * (a.ny / (ty - 1) + 1) *
+                               ((a.nz + a.kchunk - 1) / a.kchunk);
+        bs[m + 1] = (int)(bs[m] + blocks);
+        sym = std::min(sym, s->sym);
       }
-      const int64_t blocks = (int64_t)(a.nx / (tx - 1) + 1) * (a.ny / (ty - 1) + 1) *
-                             ((a.nz + a.kchunk - 1) / a.kchunk);
-      bs[m + 1] = (int)(bs[m] + blocks);
-      sym = std::min(sym, s->sym);
-    }
-    const Staging g = stage(sizeof(pn::GridArgs<T>) * n, n + 1);
-    for (int p = 0; p < 2; p++)
-      pn::ck(cudaMemcpyAsync(g.args[p], ga[p].data(), sizeof(pn::GridArgs<T>) * n, cudaMemcpyHostToDevice,
-                             b->stream), "batch args");
-    pn::ck(cudaMemcpyAsync(g.start[0], bs.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, b->stream),
-           "batch blocks");
-    for (int32_t k = 0; k < chunk; k++) {
-      pn::GridBatchLaunch L;
-      L.n_members = n;
-      L.args = g.args[k & 1];
-      L.block_start = g.start[0];
-      L.total_blocks = bs[n];
-      L.sym = sym;
-      pn::ck(tma ? pn::launch_grid_tma_batch(L, precision, k, b->stream)
-                 : pn::launch_grid_batch(L, precision, k, b->stream),
-             "batch step");
-    }
+      g = stage(sizeof(pn::GridArgs<T>) * n, n + 1);
+      for (int p = 0; p < 2; p++)
+        pn::ck(cudaMemcpyAsync(g.args[p], ga[p].data(), sizeof(pn::GridArgs<T>) * n, cudaMemcpyHostToDevice,
+                               b->stream), "batch args");
+      pn::ck(cudaMemcpyAsync(g.start[0], bs.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, b->stream),
+             "batch blocks");
+      staged_shape = c;
+      return bs[n];
+    };
+    prepare(0);
+    int64_t work = 0;
+    for (pn_solver *s : b->members) work += (int64_t)s->grid.nx * s->grid.ny * s->grid.nz / 1024;
+    ChunkSignature sig{};
+    sig.form = PN_FORM_GRID;
+    sig.precision = precision;
+    sig.n = n;
+    sig.sym = sym;
+    sig.tma = tma ? 1 : 0;
+    sig.p[0] = g.args[0];
+    sig.p[1] = g.args[1];
+    sig.p[2] = g.start[0];
+    run_chunk(b, std::make_tuple((int)PN_FORM_GRID, precision, log2_class(n), log2_class(work)),
+              (int)(sizeof(kGridShapes) / sizeof(int)), chunk, may_alloc, sig, prepare, [&](int c, int32_t k) {
+                prepare(c);
+                pn::GridBatchLaunch L;
+                L.n_members = n;
+                L.args = g.args[k & 1];
+                L.block_start = g.start[0];
+                L.total_blocks = bs[n];
+                L.sym = sym;
+                pn::ck(tma ? pn::launch_grid_tma_batch(L, precision, k, b->stream)
+                           : pn::launch_grid_batch(L, precision, k, b->stream),
+                       "batch step");
+              });
     pn::ck(cudaStreamSynchronize(b->stream), "batch chunk");
     advance(b, chunk);
     done += chunk;
@@ -368,6 +519,14 @@ int pn_batch_solve_noalloc(pn_batch *b, int32_t nsteps) {
     solve_members(b, nsteps, ScratchStaging{(unsigned char *)scratch}, false);
     return PN_OK;
   });
+}
+
+int pn_batch_plan_stats(pn_batch *b, int64_t *graph_launches, int64_t *graph_captures, int32_t *tuned_classes) {
+  if (!b) return berr(PN_ERR_INVALID, "null batch");
+  if (graph_launches) *graph_launches = b->graph_launches;
+  if (graph_captures) *graph_captures = b->graph_captures;
+  if (tuned_classes) *tuned_classes = (int32_t)b->tuned.size();
+  return PN_OK;
 }
 
 int pn_batch_synchronize(pn_batch *b) {

@@ -143,6 +143,9 @@ class Server:
         max_active = 0
         done = 0
         with Batch() as batch:
+            stream = _new_stream()
+            if stream is not None:  # a created stream: repeated quanta replay as CUDA graphs
+                batch.set_stream(stream)
             while done < len(pending):
                 # admit prepared solvers while the GPU is not saturated
                 while True:
@@ -201,6 +204,14 @@ def _current_device():
     try:
         import torch
         return torch.cuda.current_device() if torch.cuda.is_available() else None
+    except ImportError:
+        return None
+
+
+def _new_stream():
+    try:
+        import torch
+        return torch.cuda.Stream() if torch.cuda.is_available() else None
     except ImportError:
         return None
 

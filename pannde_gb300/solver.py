@@ -222,6 +222,12 @@ class Batch:
         device scratch, with no device allocation."""
         N.check(self._lib.pn_batch_solve_noalloc(self._h, int(nsteps)))
 
+    def plan_stats(self) -> dict:
+        """{"graph_launches", "graph_captures", "tuned_classes"} (pn_batch_plan_stats)"""
+        gl, gc, tc = c_int64(0), c_int64(0), ctypes.c_int32(0)
+        N.check(self._lib.pn_batch_plan_stats(self._h, ctypes.byref(gl), ctypes.byref(gc), ctypes.byref(tc)))
+        return {"graph_launches": gl.value, "graph_captures": gc.value, "tuned_classes": tc.value}
+
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
             self._lib.pn_batch_destroy(self._h)

@@ -87,3 +87,27 @@ def test_batch_rejects_mixed_members(cuda_device):
             b.add(ex)
     for s in (a, b32, ex):
         s.close()
+
+
+@pytest.mark.parametrize("form", ["grid", "table"])
+def test_tuned_shapes_and_graph_replay_keep_results(cuda_device, form):
+    """On a created stream, equal chunks are captured once as a CUDA graph and
+    replayed; the first chunk tunes the launch shape on real steps.  Results
+    stay bit-identical to the members run alone."""
+    import torch
+    cs = members()
+    ref = [alone(c, "f32", form, 60) for c in cs]
+    sv = [Solver.from_case(c, precision="f32", form=form, capacity=60) for c in cs]
+    stream = torch.cuda.Stream()
+    with Batch() as b:
+        b.set_stream(stream)
+        for s in sv:
+            b.add(s)
+        for _ in range(4):
+            b.solve(15)
+        st = b.plan_stats()
+    assert st["tuned_classes"] == 1
+    assert st["graph_captures"] == 1 and st["graph_launches"] >= 2
+    for s, r in zip(sv, ref):
+        same((s.get_state(), s.traces(), s.time), r)
+        s.close()
