@@ -333,6 +333,10 @@ void grid_args(pn_solver *s, GridArgs<T> &a) {
   a.sig_rows = 1;
   a.err = s->d_err;
   a.n_rows = s->mat.n_mat + 1;
+  // failure-path test hook: PN_TEST_GRID_SKIP_COPY=<layer> leaves that layer's
+  // tile copies unissued, so the tensor-copy kernel's bounded wait runs out
+  const char *skip = std::getenv("PN_TEST_GRID_SKIP_COPY");
+  a.test_skip_layer = skip && *skip ? std::atoi(skip) : kNoLayer;
 }
 
 const void *grid_maps_for(const pn_solver *s, int in) {

@@ -224,16 +224,43 @@ __device__ __forceinline__ int member_of(const int *__restrict__ tile_start, int
   return lo;
 }
 
-// batches: blocks walk the tiles of all members (grid-stride)
+// batches: block b takes the contiguous share [b*T/B, (b+1)*T/B) of the T
+// tiles of all members (members' tiles in member order).  The argument block
+// of the member being worked on sits in shared memory, copied in once when
+// the share reaches the member; the member of the first tile is found by
+// binary search, later ones by stepping forward.
+template <typename A>
+__device__ __forceinline__ void load_args(A &dst, const A *src) {
+  static_assert(sizeof(A) % 8 == 0, "argument blocks are copied in 8-byte words");
+  unsigned long long *d = reinterpret_cast<unsigned long long *>(&dst);
+  const unsigned long long *q = reinterpret_cast<const unsigned long long *>(src);
+  for (int w = threadIdx.x; w < (int)(sizeof(A) / 8); w += blockDim.x) d[w] = __ldg(q + w);
+}
+
+__device__ __forceinline__ void share_of_tiles(int total, int &t0, int &t1) {
+  t0 = (int)((long long)total * blockIdx.x / gridDim.x);
+  t1 = (int)((long long)total * (blockIdx.x + 1) / gridDim.x);
+}
+
 template <typename R>
 __global__ void __launch_bounds__(kTile) k_velocity_batch(const VelArgs<typename Num<R>::S> *__restrict__ args,
                                                           const int *__restrict__ tile_start, int n_members,
                                                           int step) {
-  const int total = __ldg(tile_start + n_members);
-  for (int t = blockIdx.x; t < total; t += gridDim.x) {
-    const int m = member_of(tile_start, n_members, t);
-    const VelArgs<typename Num<R>::S> a = args[m];
-    const int tl = t - __ldg(tile_start + m);
+  __shared__ __align__(16) VelArgs<typename Num<R>::S> a;
+  int t0, t1;
+  share_of_tiles(__ldg(tile_start + n_members), t0, t1);
+  if (t0 >= t1) return;
+  int m = member_of(tile_start, n_members, t0), m_end = -1, m_begin = 0;
+  for (int t = t0; t < t1; t++) {
+    if (t >= m_end) {  // the share reaches member m (first tile, or the previous member ended)
+      while (t >= __ldg(tile_start + m + 1)) m++;
+      __syncthreads();  // every thread is done with the previous member's block
+      load_args(a, args + m);
+      m_begin = __ldg(tile_start + m);
+      m_end = __ldg(tile_start + m + 1);
+      __syncthreads();
+    }
+    const int tl = t - m_begin;
     const int n = tl * kTile + threadIdx.x;
     if (n >= a.n_nodes) continue;
     if (a.gnode) velocity_node<R, false>(a, n, tl, step);
@@ -245,11 +272,21 @@ template <typename R>
 __global__ void __launch_bounds__(kTile) k_stress_batch(const StressArgs<typename Num<R>::S> *__restrict__ args,
                                                         const int *__restrict__ tile_start, int n_members,
                                                         int step) {
-  const int total = __ldg(tile_start + n_members);
-  for (int t = blockIdx.x; t < total; t += gridDim.x) {
-    const int m = member_of(tile_start, n_members, t);
-    const StressArgs<typename Num<R>::S> a = args[m];
-    const int tl = t - __ldg(tile_start + m);
+  __shared__ __align__(16) StressArgs<typename Num<R>::S> a;
+  int t0, t1;
+  share_of_tiles(__ldg(tile_start + n_members), t0, t1);
+  if (t0 >= t1) return;
+  int m = member_of(tile_start, n_members, t0), m_end = -1, m_begin = 0;
+  for (int t = t0; t < t1; t++) {
+    if (t >= m_end) {
+      while (t >= __ldg(tile_start + m + 1)) m++;
+      __syncthreads();
+      load_args(a, args + m);
+      m_begin = __ldg(tile_start + m);
+      m_end = __ldg(tile_start + m + 1);
+      __syncthreads();
+    }
+    const int tl = t - m_begin;
     const int c = tl * kTile + threadIdx.x;
     if (c >= a.n_cells) continue;
     if (a.gcell) stress_cell<R, false>(a, c, tl, step);

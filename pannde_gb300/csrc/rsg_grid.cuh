@@ -8,6 +8,7 @@
 // sorted by (block, layer, local index) with one [begin,end) range per
 // (block, layer).
 #pragma once
+#include <climits>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -50,7 +51,10 @@ struct GridArgs {
   int32_t *err;          // device error word (bounded waits that gave up), or null
   const void *tmaps;     // tensor maps of this step's input buffers (rsg_grid_tma.cu), or null
   int32_t n_rows;        // rows of ctab (materials + the void row)
+  int32_t test_skip_layer;  // failure-path test: the layer whose copies are never issued (kNoLayer: none)
 };
+
+constexpr int32_t kNoLayer = INT32_MIN;  // no layer index (layers run from -1 to nz)
 
 constexpr int kGridChunkMax = 64;     // cell layers per z chunk, at most
 constexpr int kGridTmaRowsMax = 32;   // stiffness rows the tensor-copy kernel stages

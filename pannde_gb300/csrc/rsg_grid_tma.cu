@@ -206,6 +206,7 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
   const int xs_m = floor_to(i0, 16), om = i0 - xs_m;
 
   auto issue = [&](int L) {  // thread 0: copies of layer L into slot L&3, node slot L&1
+    if (L == a.test_skip_layer) return;  // failure-path test: this layer's wait runs out
     const uint32_t bar = bars + 8u * (uint32_t)(L & 3);
     unsigned char *sl = base + (L & 3) * G::SLOT;
     unsigned char *vl = base + G::OFF_V + (L & 1) * G::VSLOT;
