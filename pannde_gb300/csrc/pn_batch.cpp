@@ -357,7 +357,6 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision, const Stage &stage, 
         const int64_t blocks = (int64_t)(a.nx / (tx - 1) + 1) * (a.ny / (ty - 1) + 1) *
                                ((a.nz + a.kchunk - 1) / a.kchunk);
         bs[m + 1] = (int)(bs[m] + blocks);
-        sym = std::min(sym, s->sym);
       }
       g = stage(sizeof(pn::GridArgs<T>) * n, n + 1);
       for (int p = 0; p < 2; p++)
@@ -368,6 +367,13 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision, const Stage &stage, 
       staged_shape = c;
       return bs[n];
     };
+    sym = 2;  // the most general symmetry class among the members
+    for (pn_solver *s : b->members) sym = std::min(sym, s->sym);
+    if (tma) {  // the cubic variant when every member has its 0.25/h folded in
+      bool cubic = true;
+      for (pn_solver *s : b->members) cubic = cubic && s->gfold != 1.0;
+      if (cubic) sym |= 4;
+    }
     prepare(0);
     int64_t work = 0;
     for (pn_solver *s : b->members) work += (int64_t)s->grid.nx * s->grid.ny * s->grid.nz / 1024;

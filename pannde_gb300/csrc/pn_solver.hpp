@@ -85,6 +85,9 @@ struct pn_solver {
   int sym = 0;             // material symmetry class of the stiffness table
   uint8_t *d_gmat = nullptr;
   void *d_tmaps = nullptr;   // tensor maps [2 input parities] (null: classic kernel)
+  // cubic lattice with the tensor-copy kernel: 0.25/h folded into dt/rho, dt*C
+  // and the force weights (the kernel's g is then 1); 1.0 when not folded
+  double gfold = 1.0;
   int32_t *d_err = nullptr;  // device error word of the grid kernels
 
   // energy audit tables (pn_energy.cpp; built on the first call)

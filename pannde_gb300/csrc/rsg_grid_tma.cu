@@ -172,6 +172,9 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
   using N = GNum<R>;
   using St = typename N::S;
   using G = Geo<(int)sizeof(St)>;
+  // SYM: material symmetry class (bits 0-1, see c_used) | 4 when the lattice is
+  // cubic and 0.25/h has been folded into the coefficients (g = 1)
+  constexpr bool CUBIC = (SYM & 4) != 0;
   constexpr int SB = G::SBOX / (int)sizeof(St);  // field stride in a slot (elements)
   constexpr int VB = G::VBOX / (int)sizeof(St);
   extern __shared__ unsigned char smem_raw[];
@@ -279,9 +282,16 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
       A = cellv(5, ra); B = cellv(5, ib); C = cellv(5, ic); D = cellv(5, id);
       const R px5 = (B + C) - (A + D), py5 = (C + D) - (A + B);
       if (k >= k0) {
-        R ax = gx * (vpx0 + px0) + gy * (vpy5 + py5) + gz * (s4 - vs4);
-        R ay = gx * (vpx5 + px5) + gy * (vpy1 + py1) + gz * (s3 - vs3);
-        R az = gx * (vpx4 + px4) + gy * (vpy3 + py3) + gz * (s2 - vs2);
+        R ax, ay, az;
+        if constexpr (CUBIC) {  // 0.25/h folded into dt/rho and the force weights
+          ax = (vpx0 + px0) + (vpy5 + py5) + (s4 - vs4);
+          ay = (vpx5 + px5) + (vpy1 + py1) + (s3 - vs3);
+          az = (vpx4 + px4) + (vpy3 + py3) + (s2 - vs2);
+        } else {
+          ax = gx * (vpx0 + px0) + gy * (vpy5 + py5) + gz * (s4 - vs4);
+          ay = gx * (vpx5 + px5) + gy * (vpy1 + py1) + gz * (s3 - vs3);
+          az = gx * (vpx4 + px4) + gy * (vpy3 + py3) + gz * (s2 - vs2);
+        }
         const int2 fr = sRf[k - k0 + 1];
         for (int e = fr.x; e < fr.y; e++) {  // force sources of this block and layer
           const int key = __ldg(a.f_key + e);
@@ -345,12 +355,21 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
         const R d01 = spx[1] + px[1], d11 = spy[1] + py[1], d21 = s[1] - ss[1];
         const R d02 = spx[2] + px[2], d12 = spy[2] + py[2], d22 = s[2] - ss[2];
         R e[6];
-        e[0] = gx * d00;
-        e[1] = gy * d11;
-        e[2] = gz * d22;
-        e[3] = gy * d12 + gz * d21;
-        e[4] = gx * d02 + gz * d20;
-        e[5] = gx * d01 + gy * d10;
+        if constexpr (CUBIC) {  // 0.25/h folded into dt*C
+          e[0] = d00;
+          e[1] = d11;
+          e[2] = d22;
+          e[3] = d12 + d21;
+          e[4] = d02 + d20;
+          e[5] = d01 + d10;
+        } else {
+          e[0] = gx * d00;
+          e[1] = gy * d11;
+          e[2] = gz * d22;
+          e[3] = gy * d12 + gz * d21;
+          e[4] = gx * d02 + gz * d20;
+          e[5] = gx * d01 + gy * d10;
+        }
         const unsigned char *sl = base + (kc & 3) * G::SLOT;
         const St *Sc = reinterpret_cast<const St *>(sl);
         const int own = ra + G::BWC + 1;  // cell (i, j)
@@ -374,7 +393,7 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
         for (int kk = 0; kk < 6; kk++) {
 #pragma unroll
           for (int jj = 0; jj < 6; jj++)
-            if (c_used(SYM, kk, jj)) acc[kk] = acc[kk] + N::val(Cm[6 * kk + jj]) * e[jj];
+            if (c_used(SYM & 3, kk, jj)) acc[kk] = acc[kk] + N::val(Cm[6 * kk + jj]) * e[jj];
           N::st(a.S_out[kk], cg, acc[kk]);
         }
       }
@@ -475,20 +494,35 @@ cudaError_t launch_batch_t(const GridBatchLaunch &b, int step, cudaStream_t st) 
   return cudaGetLastError();
 }
 
+template <typename T> inline bool is_one(T v) { return v == T(1); }
+template <> inline bool is_one<float2>(float2 v) { return v.x == 1.0f && v.y == 0.0f; }
+
 template <typename R>
 cudaError_t launch_sym(const GridArgs<typename GNum<R>::S> &a, int sym, cudaStream_t st) {
   if (a.nx <= 0 || a.ny <= 0 || a.nz <= 0) return cudaSuccess;
   if (!a.tmaps || a.n_rows > ROWS_MAX) return cudaErrorInvalidValue;
-  if (sym == 2) return launch_t<R, 2>(a, st);
-  if (sym == 1) return launch_t<R, 1>(a, st);
-  return launch_t<R, 0>(a, st);
+  const bool cubic = is_one(a.g[0]) && is_one(a.g[1]) && is_one(a.g[2]);
+  switch ((sym & 3) | (cubic ? 4 : 0)) {
+    case 2: return launch_t<R, 2>(a, st);
+    case 1: return launch_t<R, 1>(a, st);
+    case 0: return launch_t<R, 0>(a, st);
+    case 6: return launch_t<R, 6>(a, st);
+    case 5: return launch_t<R, 5>(a, st);
+    default: return launch_t<R, 4>(a, st);
+  }
 }
 
+// b.sym: the members' most general symmetry class | 4 when every member is cubic
 template <typename R>
 cudaError_t launch_batch_sym(const GridBatchLaunch &b, int step, cudaStream_t st) {
-  if (b.sym == 2) return launch_batch_t<R, 2>(b, step, st);
-  if (b.sym == 1) return launch_batch_t<R, 1>(b, step, st);
-  return launch_batch_t<R, 0>(b, step, st);
+  switch (b.sym) {
+    case 2: return launch_batch_t<R, 2>(b, step, st);
+    case 1: return launch_batch_t<R, 1>(b, step, st);
+    case 0: return launch_batch_t<R, 0>(b, step, st);
+    case 6: return launch_batch_t<R, 6>(b, step, st);
+    case 5: return launch_batch_t<R, 5>(b, step, st);
+    default: return launch_batch_t<R, 4>(b, step, st);
+  }
 }
 
 // ---- tensor-map encoding (driver entry point, no libcuda link) ------------------
