@@ -94,3 +94,36 @@ def test_transducer_job_keys(tmp_path):
     for key in ("XD0/XCenter", "XD0/YCenter", "XD0/ZCenter", "XD0/Radius", "XD0/SignalTimes", "XD0/SignalValues"):
         assert key in fd
     assert np.array_equal(fd["XD0/SignalValues"], c.sources[0].values)
+
+
+def test_standin_gateway_reads_and_writes(tmp_path):
+    """include/standin/VTKGateway.hpp over the reference's HostData factories."""
+    import os
+    ref = Path(os.environ.get("PANNDE_REFERENCE", "/root/reference"))
+    if not (ref / "modules" / "HostData" / "include" / "HostField.hpp").exists():
+        pytest.skip("reference headers not present")
+    inc = ["-I", str(ROOT / "include" / "standin"), "-I", str(ROOT / "include")]
+    for m in ("PanNDE", "Controller", "HostData"):
+        inc += ["-I", str(ref / "modules" / m / "include")]
+    exe = tmp_path / "gateway_check"
+    r = subprocess.run(["g++", "-std=c++14", "-O1", "-w", *inc, str(ROOT / "tests" / "cxx" / "gateway_check.cpp"),
+                        "-lz", "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    pts, hexes, pdata, cdata, fdata = sample()
+    job = tmp_path / "job.vtu"
+    vtu.write_vtu(job, pts, hexes, pdata, cdata, fdata, encoding="appended", compress=True)
+    r = subprocess.run([str(exe), str(job), str(tmp_path / "sol")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    nn, nc, trho, tvx, rsum, vsum, dt, nwt = r.stdout.split()
+    assert int(nn) == len(pts) and int(nc) == len(hexes)
+    assert int(trho) == 1 and int(tvx) == 0  # CELL, NODE
+    assert float(rsum) == pytest.approx(cdata["density"].sum(), rel=1e-15)
+    assert float(vsum) == pytest.approx(pdata["Vx"].sum(), rel=1e-12)
+    assert float(dt) == fdata["dt"][0] and int(nwt) == fdata["write_times"].size
+    sol = vtu.read_vtu(tmp_path / "sol_3.vtu")
+    assert np.array_equal(sol["points"], pts) and np.array_equal(sol["hexes"], hexes)
+    assert np.array_equal(sol["cell_data"]["density"], cdata["density"])
+    assert np.array_equal(sol["point_data"]["Vx"], pdata["Vx"])
+    assert sol["field_data"]["time"][0] == 1.5e-6
+    tab = vtu.read_vtt(tmp_path / "sol_table_3.vtt")
+    assert np.array_equal(tab["columns"]["write_times"], fdata["write_times"])
