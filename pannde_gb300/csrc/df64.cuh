@@ -11,6 +11,7 @@
 //                  arithmetic" (2001): two_sum of the high words, add the low
 //                  words, renormalise (11 flops)
 //   mul            two_prod of the high words plus the cross terms, renormalised
+//   madd           a*b + c with one renormalisation
 // Every step uses the _rn intrinsics so the compiler can neither contract a
 // product into a following add nor reorder the sums the algorithms rely on.
 // Values must stay inside the float exponent range (about 1e-38..3e38).
@@ -57,6 +58,63 @@ __device__ __forceinline__ df64 operator*(df64 a, df64 b) {
 }
 
 __device__ __forceinline__ df64 &operator+=(df64 &a, df64 b) { return a = a + b; }
+
+// a*b + c without renormalising the product first: the two_prod error terms
+// join c's low word before the one renormalisation (15 flops against 18 for
+// a separate mul and add; the same "sloppy" error bound)
+__device__ __forceinline__ df64 madd(df64 a, df64 b, df64 c) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  df64 s = two_sum(p, c.hi);
+  s.lo = __fadd_rn(s.lo, __fadd_rn(e, c.lo));
+  return quick_two_sum(s.hi, s.lo);
+}
+// Four-term sums of the stencil with one renormalisation at the end: the
+// high words go through error-free two_sums, the low words and the errors
+// are summed as floats ("lazy" double-float accumulation; 27 flops for
+// (b+c)-(a+d) against 33 for three renormalised adds).
+struct df64_unnorm {
+  float hi, lo;  // hi + lo, |lo| not yet bounded by ulp(hi)/2
+};
+__device__ __forceinline__ df64_unnorm add_lazy(df64 a, df64 b) {
+  const df64 s = two_sum(a.hi, b.hi);
+  return {s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo))};
+}
+__device__ __forceinline__ df64 sub_norm(df64_unnorm a, df64_unnorm b) {
+  const df64 s = two_sum(a.hi, -b.hi);
+  return quick_two_sum(s.hi, __fadd_rn(s.lo, __fsub_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ df64 add_norm(df64_unnorm a, df64_unnorm b) {
+  const df64 s = two_sum(a.hi, b.hi);
+  return quick_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+// (b + c) - (a + d)
+__device__ __forceinline__ df64 diff22(df64 b, df64 c, df64 a, df64 d) {
+  return sub_norm(add_lazy(b, c), add_lazy(a, d));
+}
+// (a + b) + (c + d)
+__device__ __forceinline__ df64 sum22(df64 a, df64 b, df64 c, df64 d) {
+  return add_norm(add_lazy(a, b), add_lazy(c, d));
+}
+// (c + d) - (a + b) and (a + b) + (c + d) sharing the pair sums
+__device__ __forceinline__ void diffsum22(df64 a, df64 b, df64 c, df64 d, df64 &diff, df64 &sum) {
+  const df64_unnorm ab = add_lazy(a, b), cd = add_lazy(c, d);
+  diff = sub_norm(cd, ab);
+  sum = add_norm(ab, cd);
+}
+template <typename T> __device__ __forceinline__ T diff22(T b, T c, T a, T d) { return (b + c) - (a + d); }
+template <typename T> __device__ __forceinline__ T sum22(T a, T b, T c, T d) { return (a + b) + (c + d); }
+template <typename T> __device__ __forceinline__ void diffsum22(T a, T b, T c, T d, T &diff, T &sum) {
+  const T ab = a + b, cd = c + d;
+  diff = cd - ab;
+  sum = ab + cd;
+}
+
+// the same for the native types: the compiler contracts a*b + c into one FMA
+__device__ __forceinline__ float madd(float a, float b, float c) { return a * b + c; }
+__device__ __forceinline__ double madd(double a, double b, double c) { return a * b + c; }
 
 __device__ __forceinline__ bool operator==(df64 a, df64 b) { return a.hi == b.hi && a.lo == b.lo; }
 

@@ -268,19 +268,19 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
       const int ib = ra + 1, id = ra + G::BWC, ic = id + 1;
       R A, B, C, D;
       A = cellv(0, ra); B = cellv(0, ib); C = cellv(0, ic); D = cellv(0, id);
-      const R px0 = (B + C) - (A + D);
+      const R px0 = diff22(B, C, A, D);
       A = cellv(1, ra); B = cellv(1, ib); C = cellv(1, ic); D = cellv(1, id);
-      const R py1 = (C + D) - (A + B);
+      const R py1 = diff22(C, D, A, B);
       A = cellv(2, ra); B = cellv(2, ib); C = cellv(2, ic); D = cellv(2, id);
-      const R s2 = (A + B) + (C + D);
+      const R s2 = sum22(A, B, C, D);
       A = cellv(3, ra); B = cellv(3, ib); C = cellv(3, ic); D = cellv(3, id);
-      R ab = A + B, cd = C + D;
-      const R py3 = cd - ab, s3 = ab + cd;
+      R py3, s3;
+      diffsum22(A, B, C, D, py3, s3);
       A = cellv(4, ra); B = cellv(4, ib); C = cellv(4, ic); D = cellv(4, id);
-      R bc = B + C, ad = A + D;
-      const R px4 = bc - ad, s4 = bc + ad;
+      R px4, s4;
+      diffsum22(A, D, B, C, px4, s4);
       A = cellv(5, ra); B = cellv(5, ib); C = cellv(5, ic); D = cellv(5, id);
-      const R px5 = (B + C) - (A + D), py5 = (C + D) - (A + B);
+      const R px5 = diff22(B, C, A, D), py5 = diff22(C, D, A, B);
       if (k >= k0) {
         R ax, ay, az;
         if constexpr (CUBIC) {  // 0.25/h folded into dt/rho and the force weights
@@ -288,19 +288,19 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
           ay = (vpx5 + px5) + (vpy1 + py1) + (s3 - vs3);
           az = (vpx4 + px4) + (vpy3 + py3) + (s2 - vs2);
         } else {
-          ax = gx * (vpx0 + px0) + gy * (vpy5 + py5) + gz * (s4 - vs4);
-          ay = gx * (vpx5 + px5) + gy * (vpy1 + py1) + gz * (s3 - vs3);
-          az = gx * (vpx4 + px4) + gy * (vpy3 + py3) + gz * (s2 - vs2);
+          ax = madd(gz, s4 - vs4, madd(gy, vpy5 + py5, gx * (vpx0 + px0)));
+          ay = madd(gz, s3 - vs3, madd(gy, vpy1 + py1, gx * (vpx5 + px5)));
+          az = madd(gz, s2 - vs2, madd(gy, vpy3 + py3, gx * (vpx4 + px4)));
         }
         const int2 fr = sRf[k - k0 + 1];
         for (int e = fr.x; e < fr.y; e++) {  // force sources of this block and layer
           const int key = __ldg(a.f_key + e);
           if ((key & 0xffff) != t) continue;
-          const R v = N::val(a.f_w[e]) * N::val(sigrow[__ldg(a.f_sig + e)]);
+          const R w = N::val(a.f_w[e]), sg = N::val(sigrow[__ldg(a.f_sig + e)]);
           const int d = key >> 16;
-          if (d == 0) ax = ax + v;
-          else if (d == 1) ay = ay + v;
-          else az = az + v;
+          if (d == 0) ax = madd(w, sg, ax);
+          else if (d == 1) ay = madd(w, sg, ay);
+          else az = madd(w, sg, az);
         }
         const St *Vk = reinterpret_cast<const St *>(base + G::OFF_V + (k & 1) * G::VSLOT);
         R vn[3];
@@ -308,9 +308,9 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
         for (int c = 0; c < 3; c++) vn[c] = N::val(Vk[c * VB + rv]);
         const R cf = N::val(Vk[3 * VB + rv]);
         if (!(cf == R())) {
-          vn[0] = vn[0] + cf * ax;
-          vn[1] = vn[1] + cf * ay;
-          vn[2] = vn[2] + cf * az;
+          vn[0] = madd(cf, ax, vn[0]);
+          vn[1] = madd(cf, ay, vn[1]);
+          vn[2] = madd(cf, az, vn[2]);
         }
         St *Vt = sVt + (k & 1) * 3 * NT;
 #pragma unroll
@@ -344,10 +344,8 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
       for (int c = 0; c < 3; c++) {
         const R A = N::val(Vt[c * NT + ia]), B = N::val(Vt[c * NT + ib]);
         const R C = N::val(Vt[c * NT + ic]), D = N::val(Vt[c * NT + id]);
-        const R ab = A + B, cd = C + D;
-        px[c] = (B + C) - (A + D);
-        py[c] = cd - ab;
-        s[c] = ab + cd;
+        px[c] = diff22(B, C, A, D);
+        diffsum22(A, B, C, D, py[c], s[c]);
       }
       const int kc = k - 2;
       if (kc >= k0 && cell_own) {
@@ -366,9 +364,9 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
           e[0] = gx * d00;
           e[1] = gy * d11;
           e[2] = gz * d22;
-          e[3] = gy * d12 + gz * d21;
-          e[4] = gx * d02 + gz * d20;
-          e[5] = gx * d01 + gy * d10;
+          e[3] = madd(gz, d21, gy * d12);
+          e[4] = madd(gz, d20, gx * d02);
+          e[5] = madd(gy, d10, gx * d01);
         }
         const unsigned char *sl = base + (kc & 3) * G::SLOT;
         const St *Sc = reinterpret_cast<const St *>(sl);
@@ -382,18 +380,18 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
         for (int ee = mr.x; ee < mr.y; ee++) {  // moment sources of this block and cell layer
           const int key = __ldg(a.m_key + ee);
           if ((key & 0xffff) != t) continue;
-          const R v = N::val(a.m_w[ee]) * N::val(sigrow[__ldg(a.m_sig + ee)]);
+          const R w = N::val(a.m_w[ee]), sg = N::val(sigrow[__ldg(a.m_sig + ee)]);
           const int kk = key >> 16;
 #pragma unroll
           for (int f = 0; f < 6; f++)
-            if (f == kk) acc[f] = acc[f] + v;
+            if (f == kk) acc[f] = madd(w, sg, acc[f]);
         }
         const int64_t cg = (int64_t)kc * cplane + cidx0;
 #pragma unroll
         for (int kk = 0; kk < 6; kk++) {
 #pragma unroll
           for (int jj = 0; jj < 6; jj++)
-            if (c_used(SYM & 3, kk, jj)) acc[kk] = acc[kk] + N::val(Cm[6 * kk + jj]) * e[jj];
+            if (c_used(SYM & 3, kk, jj)) acc[kk] = madd(N::val(Cm[6 * kk + jj]), e[jj], acc[kk]);
           N::st(a.S_out[kk], cg, acc[kk]);
         }
       }
