@@ -407,6 +407,33 @@ int pn_batch_synchronize(pn_batch *b);
 int pn_batch_plan_stats(pn_batch *b, int64_t *graph_launches, int64_t *graph_captures, int32_t *tuned_classes);
 int pn_batch_destroy(pn_batch *b);
 
+/* ---- partitioned solve ----------------------------------------------------
+   One mesh solved as n_parts partitions on the current device, with the
+   reference's domain decomposition (MetisHexPartitioner.hpp) and its single
+   exchange per step (HostUTModel.hpp:316-326): nodes get a home partition by
+   recursive coordinate bisection (in place of METIS); a partition's local
+   mesh is every cell touching a home node plus those cells' nodes; a step
+   updates the velocity of home nodes in every partition, copies each halo
+   node's velocity from its home partition on the device, then updates the
+   stress of every local cell (halo cells recomputed, as the reference does).
+   Results equal the single-partition solve.  Precision PN_PREC_F64,
+   PN_PREC_F32 or PN_PREC_DF64 (table form); the mesh must not carry
+   node_owner.  Replaces the reference's MPI decomposition for one device; on
+   several devices the exchange lists are the messages to send. */
+typedef struct pn_partitioned pn_partitioned;
+
+int pn_partitioned_create(const pn_mesh *mesh, const pn_material_table *materials, double dt, int32_t precision,
+                          int32_t n_parts, pn_partitioned **out);
+int pn_partitioned_add_sources(pn_partitioned *p, const pn_window_source *sources, int32_t n);
+int pn_partitioned_set_sensors(pn_partitioned *p, const int32_t *nodes, int32_t n, int32_t capacity_steps);
+int pn_partitioned_set_state(pn_partitioned *p, const double *const *V, const double *const *S);
+int pn_partitioned_solve(pn_partitioned *p, int32_t nsteps, double *time_out);
+int pn_partitioned_get_state(pn_partitioned *p, double *const *V, double *const *S);
+int pn_partitioned_get_traces(pn_partitioned *p, double *out, int64_t max_records, int64_t *n_records);
+/* partitions, halo node copies, local cells summed over partitions */
+int pn_partitioned_info(pn_partitioned *p, int32_t *n_parts, int64_t *halo_nodes, int64_t *local_cells);
+int pn_partitioned_destroy(pn_partitioned *p);
+
 /* Free all device memory of the solver. */
 int pn_solver_destroy(pn_solver *s);
 

@@ -140,6 +140,16 @@ SIGNATURES = {
     "pn_batch_plan_stats": (c_int, [c_void_p, POINTER(c_int64), POINTER(c_int64), P_int32]),
     "pn_batch_synchronize": (c_int, [c_void_p]),
     "pn_batch_destroy": (c_int, [c_void_p]),
+    "pn_partitioned_create": (c_int, [POINTER(PnMesh), POINTER(PnMaterialTable), c_double, c_int32, c_int32,
+                                      POINTER(c_void_p)]),
+    "pn_partitioned_add_sources": (c_int, [c_void_p, POINTER(PnWindowSource), c_int32]),
+    "pn_partitioned_set_sensors": (c_int, [c_void_p, P_int32, c_int32, c_int32]),
+    "pn_partitioned_set_state": (c_int, [c_void_p, POINTER(P_double), POINTER(P_double)]),
+    "pn_partitioned_solve": (c_int, [c_void_p, c_int32, P_double]),
+    "pn_partitioned_get_state": (c_int, [c_void_p, POINTER(P_double), POINTER(P_double)]),
+    "pn_partitioned_get_traces": (c_int, [c_void_p, P_double, c_int64, POINTER(c_int64)]),
+    "pn_partitioned_info": (c_int, [c_void_p, P_int32, POINTER(c_int64), POINTER(c_int64)]),
+    "pn_partitioned_destroy": (c_int, [c_void_p]),
 }
 
 

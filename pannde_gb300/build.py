@@ -9,6 +9,7 @@ Sources (``pannde_gb300/csrc``):
   pn_noalloc.cu fixed scratch of the allocation-free batch solve   nvcc
   rsg_energy.cu FP64 energy audit             nvcc, sm_103a
   pn_energy.cpp energy audit tables           g++
+  pn_partition.cpp partitioned solve (halo exchange on one device)  g++
   pn_setup.cpp  host table construction       g++, -ffp-contract=off, OpenMP loops
   pn_table.cpp  table form (any hex mesh)     g++
   pn_grid.cpp   grid form (voxel meshes)      g++
@@ -61,6 +62,7 @@ def _jobs() -> list[tuple[list[str], Path]]:
         (common_cu + ["-c", str(CSRC / "pn_noalloc.cu")], OUT / "pn_noalloc.o"),
         (common_cu + ["-c", str(CSRC / "rsg_energy.cu")], OUT / "rsg_energy.o"),
         (common_cc + ["-c", str(CSRC / "pn_energy.cpp")], OUT / "pn_energy.o"),
+        (common_cc + ["-c", str(CSRC / "pn_partition.cpp")], OUT / "pn_partition.o"),
         (common_cc + ["-c", str(CSRC / "pn_setup.cpp")], OUT / "pn_setup.o"),
         (common_cc + ["-c", str(CSRC / "pn_table.cpp")], OUT / "pn_table.o"),
         (common_cc + ["-c", str(CSRC / "pn_grid.cpp")], OUT / "pn_grid.o"),

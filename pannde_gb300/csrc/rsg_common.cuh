@@ -117,6 +117,8 @@ struct BatchLaunch {
 };
 // precision: PN_PREC_F64 (1), PN_PREC_F32 (2), PN_PREC_DF64 (3)
 cudaError_t launch_table_batch(const BatchLaunch &b, int precision, int step, cudaStream_t st);
+// one or both half steps of a batch step: halves bit 0 velocity, bit 1 stress
+cudaError_t launch_table_batch_halves(const BatchLaunch &b, int precision, int step, int halves, cudaStream_t st);
 
 cudaError_t launch_velocity_exact(const VelArgs<double> &a, int step, cudaStream_t st);
 cudaError_t launch_stress_exact(const StressArgs<double> &a, int step, cudaStream_t st);

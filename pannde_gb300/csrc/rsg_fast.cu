@@ -313,12 +313,12 @@ cudaError_t launch_str(const StressArgs<typename Num<R>::S> &a, int step, bool u
 }
 
 template <typename R>
-cudaError_t launch_batch(const BatchLaunch &b, int step, cudaStream_t st) {
+cudaError_t launch_batch(const BatchLaunch &b, int step, int halves, cudaStream_t st) {
   using S = typename Num<R>::S;
-  if (b.vel_tiles > 0)
+  if ((halves & 1) && b.vel_tiles > 0)
     k_velocity_batch<R><<<b.blocks_vel, kTile, 0, st>>>((const VelArgs<S> *)b.vel_args, b.vel_start,
                                                          b.n_members, step);
-  if (b.str_tiles > 0)
+  if ((halves & 2) && b.str_tiles > 0)
     k_stress_batch<R><<<b.blocks_str, kTile, 0, st>>>((const StressArgs<S> *)b.str_args, b.str_start,
                                                        b.n_members, step);
   return cudaGetLastError();
@@ -345,9 +345,13 @@ cudaError_t launch_stress_df64(const StressArgs<float2> &a, int step, bool unifo
   return launch_str<df64>(a, step, uniform, st);
 }
 cudaError_t launch_table_batch(const BatchLaunch &b, int precision, int step, cudaStream_t st) {
-  if (precision == 2) return launch_batch<float>(b, step, st);
-  if (precision == 3) return launch_batch<df64>(b, step, st);
-  return launch_batch<double>(b, step, st);
+  return launch_table_batch_halves(b, precision, step, 3, st);
+}
+
+cudaError_t launch_table_batch_halves(const BatchLaunch &b, int precision, int step, int halves, cudaStream_t st) {
+  if (precision == 2) return launch_batch<float>(b, step, halves, st);
+  if (precision == 3) return launch_batch<df64>(b, step, halves, st);
+  return launch_batch<double>(b, step, halves, st);
 }
 
 }  // namespace pn

@@ -58,6 +58,19 @@ __global__ void __launch_bounds__(256) k_state_load(const R *__restrict__ src, i
   }
 }
 
+// halo exchange of a partitioned solve: V[dst part][c][dst] = V[src part][c][src]
+// for every entry (dst part, dst node, src part, src node) -- the halo copy of
+// a node takes its owner's freshly updated velocity
+template <typename R>
+__global__ void __launch_bounds__(256) k_halo(const int4 *__restrict__ ex, int64_t n, R *const *__restrict__ vptr) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int4 e = __ldg(ex + i);
+#pragma unroll
+    for (int c = 0; c < 3; c++) vptr[3 * e.x + c][e.y] = vptr[3 * e.z + c][e.w];
+  }
+}
+
 int blocks_for(int64_t n) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -92,6 +105,21 @@ cudaError_t launch_state_load(int precision, const void *src, int64_t n, const i
     case PN_PREC_F32: k_state_load<float><<<nb, 256, 0, st>>>((const float *)src, n, map, dst); break;
     case PN_PREC_DF64: k_state_load<float2><<<nb, 256, 0, st>>>((const float2 *)src, n, map, dst); break;
     default: k_state_load<double><<<nb, 256, 0, st>>>((const double *)src, n, map, dst); break;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace pn
+
+namespace pn {
+
+cudaError_t launch_halo_exchange(int precision, const int4 *ex, int64_t n, void *const *vptr, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int nb = blocks_for(n);
+  switch (precision) {
+    case PN_PREC_F32: k_halo<float><<<nb, 256, 0, st>>>(ex, n, (float *const *)vptr); break;
+    case PN_PREC_DF64: k_halo<float2><<<nb, 256, 0, st>>>(ex, n, (float2 *const *)vptr); break;
+    default: k_halo<double><<<nb, 256, 0, st>>>(ex, n, (double *const *)vptr); break;
   }
   return cudaGetLastError();
 }

@@ -16,4 +16,10 @@ cudaError_t launch_state_store(int precision, const double *src, int64_t n, cons
 cudaError_t launch_state_load(int precision, const void *src, int64_t n, const int64_t *map,
                               double *dst, cudaStream_t st);
 
+// Halo exchange of a partitioned solve: for each entry e of ex[n]
+// (dst part, dst node, src part, src node), V[e.x][c][e.y] = V[e.z][c][e.w]
+// for c = 0..2, with vptr[3*part + c] the device address of that velocity
+// component (vptr itself in device memory).
+cudaError_t launch_halo_exchange(int precision, const int4 *ex, int64_t n, void *const *vptr, cudaStream_t st);
+
 }  // namespace pn

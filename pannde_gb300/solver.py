@@ -244,3 +244,75 @@ class Batch:
 
     def __exit__(self, *exc):
         self.close()
+
+
+class Partitioned:
+    """One mesh as several partitions on the current device with a halo
+    exchange per step (pn_partitioned_*); results equal a single Solver."""
+
+    def __init__(self, case: Case, n_parts: int, precision="f64"):
+        self._lib = N.load()
+        self.mesh = case.mesh
+        m, keep = case.mesh.as_struct()
+        tab, keep_t = case.material_table()
+        h = c_void_p()
+        N.check(self._lib.pn_partitioned_create(ctypes.byref(m), ctypes.byref(tab), float(case.dt),
+                                                PRECISIONS[precision], int(n_parts), ctypes.byref(h)))
+        self._h = h
+        self.n_sensors = 0
+        del keep, keep_t
+
+    def add_sources(self, sources):
+        arr, keep = sources_struct(sources)
+        N.check(self._lib.pn_partitioned_add_sources(self._h, arr, len(sources)))
+        del keep
+
+    def set_sensors(self, nodes, capacity_steps):
+        nd = N.i32(nodes)
+        N.check(self._lib.pn_partitioned_set_sensors(self._h, N.iptr(nd), int(nd.shape[0]), int(capacity_steps)))
+        self.n_sensors = int(nd.shape[0])
+
+    def set_state(self, V=None, S=None):
+        v = [N.f64(a) if a is not None else None for a in (V or [None] * 3)]
+        s = [N.f64(a) if a is not None else None for a in (S or [None] * 6)]
+        N.check(self._lib.pn_partitioned_set_state(self._h, N.ptr_array(v), N.ptr_array(s)))
+
+    def solve(self, nsteps=1) -> float:
+        t = c_double(0.0)
+        N.check(self._lib.pn_partitioned_solve(self._h, int(nsteps), ctypes.byref(t)))
+        return t.value
+
+    def get_state(self):
+        V = [np.empty(self.mesh.n_nodes) for _ in range(3)]
+        S = [np.empty(self.mesh.n_cells) for _ in range(6)]
+        N.check(self._lib.pn_partitioned_get_state(self._h, N.ptr_array(V), N.ptr_array(S)))
+        return V, S
+
+    def traces(self) -> np.ndarray:
+        n = c_int64(0)
+        N.check(self._lib.pn_partitioned_get_traces(self._h, N.P_double(), 0, ctypes.byref(n)))
+        out = np.zeros((max(n.value, 1), max(self.n_sensors, 1), 3))
+        N.check(self._lib.pn_partitioned_get_traces(self._h, N.dptr(out), n.value, ctypes.byref(n)))
+        return out[:n.value, :self.n_sensors]
+
+    def info(self) -> dict:
+        p, hn, lc = ctypes.c_int32(0), c_int64(0), c_int64(0)
+        N.check(self._lib.pn_partitioned_info(self._h, ctypes.byref(p), ctypes.byref(hn), ctypes.byref(lc)))
+        return {"n_parts": p.value, "halo_nodes": hn.value, "local_cells": lc.value}
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.pn_partitioned_destroy(self._h)
+            self._h = c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
