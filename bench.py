@@ -8,8 +8,9 @@ radius patch centred on the top face, 64 seeded top-face sensors recorded
 every step.  Synthetic inputs with the published workload's shapes.
 
 A step is one leapfrog step over the whole mesh: the node velocity update
-then the cell stress update (two kernel launches).  Every step moves more
-than the 129 MB L2 (about 1.9 GB in FP64), so no L2 flush is needed.
+then the cell stress update (one fused launch on voxel meshes, two on the
+connectivity-table form).  Every step moves more than the 129 MB L2 (about
+1 GB in FP64), so no L2 flush is needed.
 
 value  = cells x steps / device time of the timed region (CUDA events on the
          solver's stream), FP64 drop-in form, summed over ranks.
@@ -95,19 +96,25 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic(case, form, prec):
-    """DRAM bytes per launch from the committed ncu summaries (profiles/*.txt),
-    lines 'traffic <case>.<form>.<precision>.<kernel> = <bytes>'."""
+def profile_figures(case, form, prec, what="traffic"):
+    """Per-kernel figures from the committed ncu summaries (profiles/*.txt),
+    lines '<what> <case>.<form>.<precision>.<kernel> = <value>': 'traffic'
+    (DRAM bytes per launch), 'fp64pipe' (FP64 pipe busy fraction), 'dpops'
+    (FP64 operations per cell-step)."""
     out = {}
     prefix = f"{case}.{form}.{prec}."
     for f in sorted((ROOT / "profiles").glob("*.txt")):
         for line in f.read_text().splitlines():
-            if line.startswith("traffic ") and "=" in line:
-                key, val = line[len("traffic "):].split("=", 1)
+            if line.startswith(what + " ") and "=" in line:
+                key, val = line[len(what) + 1:].split("=", 1)
                 key = key.strip()
                 if key.startswith(prefix):
                     out[key[len(prefix):]] = float(val.split()[0])
     return out
+
+
+def profile_traffic(case, form, prec):
+    return profile_figures(case, form, prec, "traffic")
 
 
 class Clocks:
@@ -223,13 +230,25 @@ def roofline(case, info, kt, prec, peak, peak_kind):
                "stress": nc * (12 * e + 36) + nn * 3 * e}
     dom = max(avg, key=lambda k: avg[k])
     achieved = alg[dom] / (avg[dom] * 1e-3) / 1e9
-    traffic = profile_traffic(case, info.get("form_name", "table"), prec).get(dom)
+    form = info.get("form_name", "table")
+    traffic = profile_traffic(case, form, prec).get(dom)
     step_ms = sum(avg.values())
-    return {"bound": "hbm", "kernel": dom, "form": info.get("form_name"), "achieved": round(achieved, 1),
-            "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-            "traffic": traffic, "algorithmic_bytes": alg[dom],
-            "avg_ms": {k: round(v, 4) for k, v in avg.items()},
-            "step_bytes_frac": round(sum(alg.values()) / (step_ms * 1e-3) / 1e9 / peak, 4)}
+    out = {"bound": "hbm", "kernel": dom, "form": form, "achieved": round(achieved, 1),
+           "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+           "traffic": traffic, "algorithmic_bytes": alg[dom],
+           "avg_ms": {k: round(v, 4) for k, v in avg.items()},
+           "step_bytes_frac": round(sum(alg.values()) / (step_ms * 1e-3) / 1e9 / peak, 4)}
+    if prec == "f64":
+        # the FP64 form is bound by GB300's FP64 pipe, not by HBM: its operation
+        # count per cell-step and the pipe's busy fraction come from ncu
+        dp = profile_figures(case, form, prec, "dpops").get(dom)
+        busy = profile_figures(case, form, prec, "fp64pipe").get(dom)
+        if dp:
+            rate = dp * nc / (avg[dom] * 1e-3)
+            out["fp64_pipe"] = {"ops_per_cell_step_ncu": dp, "achieved_ops_per_s": round(rate, 0),
+                                "busy_frac_ncu": busy,
+                                "note": "DFMA-bound: GB300 runs FP64 at about 1/30 of its FP32 rate"}
+    return out
 
 
 def e2e_run(case, prec, steps, torch):

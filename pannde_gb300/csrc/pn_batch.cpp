@@ -22,9 +22,11 @@
 // (kernel arguments are device pointers to the staged blocks plus the step).
 struct ChunkSignature {
   int form, precision, n, shape, chunk, total0, total1, sym, tma;
+  int reserved;  // keeps the pointers 8-byte aligned with no padding bytes (memcmp below)
   const void *p[4];
   bool operator==(const ChunkSignature &o) const { return std::memcmp(this, &o, sizeof(*this)) == 0; }
 };
+static_assert(sizeof(ChunkSignature) == 10 * sizeof(int) + 4 * sizeof(void *), "no padding");
 
 struct pn_batch {
   std::vector<pn_solver *> members;

@@ -189,22 +189,6 @@ struct pn_solver {
     }
   }
 
-  // download n values of the storage type into doubles
-  void download_real(double *dst, const void *src_, size_t n) {
-    if (n == 0 || !dst) return;
-    if (is_df64()) {
-      std::vector<float> tmp(2 * n);
-      pn::ck(cudaMemcpy(tmp.data(), src_, n * 8, cudaMemcpyDeviceToHost), "download");
-      for (size_t i = 0; i < n; i++) dst[i] = (double)tmp[2 * i] + (double)tmp[2 * i + 1];
-    } else if (esz == 8) {
-      pn::ck(cudaMemcpy(dst, src_, n * 8, cudaMemcpyDeviceToHost), "download");
-    } else {
-      std::vector<float> tmp(n);
-      pn::ck(cudaMemcpy(tmp.data(), src_, n * 4, cudaMemcpyDeviceToHost), "download");
-      for (size_t i = 0; i < n; i++) dst[i] = (double)tmp[i];
-    }
-  }
-
   void upload_raw(void *dst, const void *src_, size_t bytes) {
     if (bytes == 0) return;
     pn::ck(cudaMemcpyAsync(dst, src_, bytes, cudaMemcpyHostToDevice, stream), "upload");
