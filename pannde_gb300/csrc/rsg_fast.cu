@@ -312,15 +312,36 @@ cudaError_t launch_str(const StressArgs<typename Num<R>::S> &a, int step, bool u
   return cudaGetLastError();
 }
 
+// blocks of the batch kernels that are resident at once on the current
+// device: every block's share of tiles is worked in one wave, so a grid
+// larger than this would leave a tail of blocks queued behind the others
+template <typename R>
+int batch_resident(int sms_blocks_wanted, bool stress) {
+  static int per_sm[2][64] = {{0}};
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return sms_blocks_wanted;
+  int &p = per_sm[stress ? 1 : 0][dev & 63];
+  if (p == 0) {
+    int v = 0;
+    const cudaError_t e =
+        stress ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_stress_batch<R>, kTile, 0)
+               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_velocity_batch<R>, kTile, 0);
+    p = (e == cudaSuccess && v > 0) ? v : 1;
+  }
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+    return sms_blocks_wanted;
+  return std::min(sms_blocks_wanted, p * sms);
+}
+
 template <typename R>
 cudaError_t launch_batch(const BatchLaunch &b, int step, int halves, cudaStream_t st) {
   using S = typename Num<R>::S;
   if ((halves & 1) && b.vel_tiles > 0)
-    k_velocity_batch<R><<<b.blocks_vel, kTile, 0, st>>>((const VelArgs<S> *)b.vel_args, b.vel_start,
-                                                         b.n_members, step);
+    k_velocity_batch<R><<<batch_resident<R>(b.blocks_vel, false), kTile, 0, st>>>(
+        (const VelArgs<S> *)b.vel_args, b.vel_start, b.n_members, step);
   if ((halves & 2) && b.str_tiles > 0)
-    k_stress_batch<R><<<b.blocks_str, kTile, 0, st>>>((const StressArgs<S> *)b.str_args, b.str_start,
-                                                       b.n_members, step);
+    k_stress_batch<R><<<batch_resident<R>(b.blocks_str, true), kTile, 0, st>>>(
+        (const StressArgs<S> *)b.str_args, b.str_start, b.n_members, step);
   return cudaGetLastError();
 }
 
