@@ -55,7 +55,7 @@ def parse():
     p.add_argument("--nx", type=int, default=None, help="laminate size override (profiling)")
     p.add_argument("--ny", type=int, default=None)
     p.add_argument("--nz", type=int, default=None)
-    p.add_argument("--precisions", default="f64,f32",
+    p.add_argument("--precisions", default="f64,df64,f32",
                    help="forms to time; the first is the headline value")
     p.add_argument("--form", default="auto", choices=["auto", "table", "grid"],
                    help="device form: voxel-grid kernels or connectivity tables")

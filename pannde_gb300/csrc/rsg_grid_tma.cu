@@ -43,7 +43,8 @@ namespace {
 constexpr int TX = 32, TY = 8, NT = TX * TY;
 constexpr int KC_MAX = kGridChunkMax;  // cell layers per chunk (source-range staging)
 constexpr int ROWS_MAX = kGridTmaRowsMax;
-constexpr int NSLOT = 4;
+constexpr int NMSLOT = 4;  // material slots: read two layers after their copy
+constexpr int NVSLOT = 2;  // velocity + dt/rho slots: read in the layer's own iteration
 
 struct GridMaps {
   CUtensorMap S[6];
@@ -52,9 +53,15 @@ struct GridMaps {
   CUtensorMap mat;
 };
 
-// shared-memory geometry for a storage element of ESZ bytes
+// shared-memory geometry for a storage element of ESZ bytes.  The stress ring
+// holds NS layers: with 4 the stress half reads a cell's old stress from the
+// tile copied two layers before (4-byte storage, latency-bound); with 2 it
+// reads it from global memory (L2), which leaves room for a third block per SM
+// with 8-byte storage.
 template <int ESZ>
 struct Geo {
+  static constexpr int NS = ESZ == 4 ? 4 : 2;
+  static constexpr bool OWN_SMEM = NS == 4;
   static constexpr int A = 16 / ESZ;              // x alignment of a copy (elements)
   static constexpr int BWC = ESZ == 4 ? 36 : 34;  // cell tile width: offset (< A) + 33
   static constexpr int BWN = ESZ == 4 ? 36 : 34;  // node tile width: offset (< A) + 32
@@ -64,23 +71,27 @@ struct Geo {
   static constexpr int VBOX = BWN * TY * ESZ;
   static constexpr int MBOX_BYTES = BWM * (TY - 1);
   static constexpr int MBOX = (MBOX_BYTES + 127) / 128 * 128;
-  static constexpr int SLOT = 6 * SBOX + MBOX;
-  static constexpr int VSLOT = 4 * VBOX;
+  static constexpr int SLOT = 6 * SBOX;                        // S[6] of one layer
+  static constexpr int VSLOT = 4 * VBOX;                       // V[3], dt/rho of one layer
   static constexpr uint32_t TX_BYTES = 6 * SBOX_BYTES + 4 * VBOX + MBOX_BYTES;
-  static constexpr int OFF_V = NSLOT * SLOT;
-  static constexpr int OFF_VT = OFF_V + 2 * VSLOT;             // computed velocity [2][3][NT]
+  static constexpr int OFF_V = NS * SLOT;                      // velocity ring [NVSLOT]
+  static constexpr int OFF_M = OFF_V + NVSLOT * VSLOT;         // material ring [NMSLOT]
+  static constexpr int OFF_VT = OFF_M + NMSLOT * MBOX;         // computed velocity [2][3][NT]
   static constexpr int OFF_C = OFF_VT + 2 * 3 * NT * ESZ;      // dt*C rows [ROWS_MAX][36]
   static constexpr int OFF_R = OFF_C + ROWS_MAX * 36 * ESZ;    // ranges f, s [KC_MAX+2], m [KC_MAX]
-  static constexpr int OFF_B = OFF_R + (3 * KC_MAX + 4) * 8;   // mbarriers [NSLOT]
-  static constexpr int BYTES = OFF_B + NSLOT * 8;
+  static constexpr int OFF_B = OFF_R + (3 * KC_MAX + 4) * 8;   // mbarriers [NS]
+  static constexpr int BYTES = OFF_B + NS * 8;
   static constexpr size_t SMEM = BYTES + 128;                  // + base alignment
-  static_assert(SLOT % 128 == 0 && VBOX % 128 == 0 && OFF_V % 128 == 0 && OFF_B % 8 == 0, "alignment");
+  static_assert(SLOT % 128 == 0 && VBOX % 128 == 0 && OFF_V % 128 == 0 && OFF_M % 128 == 0 && OFF_B % 8 == 0,
+                "alignment");
+  static_assert(NS % NVSLOT == 0 && NMSLOT % NS == 0, "slot counts");
   static_assert(SBOX % ESZ == 0 && VBOX % ESZ == 0, "element size");
 };
 
 template <typename R> struct GNum;
 template <> struct GNum<float> {
   using S = float;
+  static __device__ __forceinline__ float ld(const float *p, int64_t i) { return __ldg(p + i); }
   static __device__ __forceinline__ float val(float v) { return v; }
   static __device__ __forceinline__ float sto(float v) { return v; }
   static __device__ __forceinline__ void st(float *p, int64_t i, float v) { p[i] = v; }
@@ -88,6 +99,7 @@ template <> struct GNum<float> {
 };
 template <> struct GNum<double> {
   using S = double;
+  static __device__ __forceinline__ double ld(const double *p, int64_t i) { return __ldg(p + i); }
   static __device__ __forceinline__ double val(double v) { return v; }
   static __device__ __forceinline__ double sto(double v) { return v; }
   static __device__ __forceinline__ void st(double *p, int64_t i, double v) { p[i] = v; }
@@ -95,6 +107,10 @@ template <> struct GNum<double> {
 };
 template <> struct GNum<df64> {
   using S = float2;
+  static __device__ __forceinline__ df64 ld(const float2 *p, int64_t i) {
+    const float2 v = __ldg(p + i);
+    return df64(v.x, v.y);
+  }
   static __device__ __forceinline__ df64 val(float2 v) { return df64(v.x, v.y); }
   static __device__ __forceinline__ float2 sto(df64 v) { return make_float2(v.hi, v.lo); }
   static __device__ __forceinline__ void st(float2 *p, int64_t i, df64 v) { p[i] = make_float2(v.hi, v.lo); }
@@ -208,24 +224,36 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
   const int xs_n = floor_to(i0, G::A), on = i0 - xs_n;
   const int xs_m = floor_to(i0, 16), om = i0 - xs_m;
 
-  auto issue = [&](int L) {  // thread 0: copies of layer L into slot L&3, node slot L&1
+  // layer L is copy number u = L - k0 + 1 of the block: stress slot and
+  // mbarrier u % NS (phase (u / NS) & 1), velocity slot u % 2, material slot u % 4
+  auto ucount = [&](int L) { return (uint32_t)(L - k0 + 1); };
+  auto sslot = [&](int L) { return base + (ucount(L) % G::NS) * G::SLOT; };
+  auto vslot = [&](int L) { return base + G::OFF_V + (ucount(L) % NVSLOT) * G::VSLOT; };
+  auto mslot = [&](int L) { return base + G::OFF_M + (ucount(L) % NMSLOT) * G::MBOX; };
+  auto bar_of = [&](int L) { return bars + 8u * (ucount(L) % G::NS); };
+  auto parity = [&](int L) { return (ucount(L) / G::NS) & 1u; };
+  auto issue = [&](int L) {  // thread 0: copies of layer L
     if (L == a.test_skip_layer) return;  // failure-path test: this layer's wait runs out
-    const uint32_t bar = bars + 8u * (uint32_t)(L & 3);
-    unsigned char *sl = base + (L & 3) * G::SLOT;
-    unsigned char *vl = base + G::OFF_V + (L & 1) * G::VSLOT;
+    const uint32_t bar = bar_of(L);
+    unsigned char *sl = sslot(L), *vl = vslot(L);
     mbar_expect_tx(bar, G::TX_BYTES);
 #pragma unroll
     for (int f = 0; f < 6; f++) tma_load_3d(smem_u32(sl + f * G::SBOX), &M->S[f], xs_c, j0 - 1, L, bar);
-    tma_load_3d(smem_u32(sl + 6 * G::SBOX), &M->mat, xs_m, j0, L, bar);
 #pragma unroll
     for (int c = 0; c < 3; c++) tma_load_3d(smem_u32(vl + c * G::VBOX), &M->V[c], xs_n, j0, L, bar);
     tma_load_3d(smem_u32(vl + 3 * G::VBOX), &M->coef, xs_n, j0, L, bar);
+    tma_load_3d(smem_u32(mslot(L)), &M->mat, xs_m, j0, L, bar);
   };
-  auto parity = [&](int L) { return (uint32_t)(((L - k0 + 1) >> 2) & 1); };
 
   if (t == 0) {
 #pragma unroll
-    for (int s = 0; s < NSLOT; s++) mbar_init(bars + 8u * s, 1);
+    for (int f = 0; f < 6; f++) tma_prefetch_map(&M->S[f]);
+#pragma unroll
+    for (int c = 0; c < 3; c++) tma_prefetch_map(&M->V[c]);
+    tma_prefetch_map(&M->coef);
+    tma_prefetch_map(&M->mat);
+#pragma unroll
+    for (int s = 0; s < G::NS; s++) mbar_init(bars + 8u * s, 1);
     mbar_init_fence();
   }
   // per-chunk tables: stiffness rows, source and sensor ranges
@@ -261,9 +289,9 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
     }
     // ---- B: velocity of node layer k
     if (k <= k1) {
-      if (mbar_wait(bars + 8u * (uint32_t)(k & 3), parity(k))) waited = k;
+      if (mbar_wait(bar_of(k), parity(k))) waited = k;
       else fail = true;
-      const St *Sk = reinterpret_cast<const St *>(base + (k & 3) * G::SLOT);
+      const St *Sk = reinterpret_cast<const St *>(sslot(k));
       auto cellv = [&](int f, int q) { return N::val(Sk[f * SB + q]); };
       const int ib = ra + 1, id = ra + G::BWC, ic = id + 1;
       R A, B, C, D;
@@ -302,7 +330,7 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
           else if (d == 1) ay = madd(w, sg, ay);
           else az = madd(w, sg, az);
         }
-        const St *Vk = reinterpret_cast<const St *>(base + G::OFF_V + (k & 1) * G::VSLOT);
+        const St *Vk = reinterpret_cast<const St *>(vslot(k));
         R vn[3];
 #pragma unroll
         for (int c = 0; c < 3; c++) vn[c] = N::val(Vk[c * VB + rv]);
@@ -368,14 +396,19 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
           e[4] = madd(gz, d20, gx * d02);
           e[5] = madd(gy, d10, gx * d01);
         }
-        const unsigned char *sl = base + (kc & 3) * G::SLOT;
-        const St *Sc = reinterpret_cast<const St *>(sl);
-        const int own = ra + G::BWC + 1;  // cell (i, j)
-        const int row = sl[6 * G::SBOX + ty * G::BWM + om + tx];
+        const int64_t cg = (int64_t)kc * cplane + cidx0;
+        const int row = mslot(kc)[ty * G::BWM + om + tx];
         const St *Cm = sC + 36 * row;
-        R acc[6];
+        R acc[6];  // the cell's stress before the update
+        if constexpr (G::OWN_SMEM) {
+          const St *Sc = reinterpret_cast<const St *>(sslot(kc));
+          const int own = ra + G::BWC + 1;  // cell (i, j)
 #pragma unroll
-        for (int f = 0; f < 6; f++) acc[f] = N::val(Sc[f * SB + own]);
+          for (int f = 0; f < 6; f++) acc[f] = N::val(Sc[f * SB + own]);
+        } else {  // in L2: its tile was copied two layers ago
+#pragma unroll
+          for (int f = 0; f < 6; f++) acc[f] = N::ld(a.S_in[f], cg);
+        }
         const int2 mr = sRm[kc - k0];
         for (int ee = mr.x; ee < mr.y; ee++) {  // moment sources of this block and cell layer
           const int key = __ldg(a.m_key + ee);
@@ -386,7 +419,6 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
           for (int f = 0; f < 6; f++)
             if (f == kk) acc[f] = madd(w, sg, acc[f]);
         }
-        const int64_t cg = (int64_t)kc * cplane + cidx0;
 #pragma unroll
         for (int kk = 0; kk < 6; kk++) {
 #pragma unroll
@@ -407,21 +439,28 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
       if (t == 0) {
         if (a.err) atomicExch(a.err, kErrWait);
         const int issued = min(k1, max(k + 1, k0));
-        for (int L = waited + 1; L <= issued; L++) (void)mbar_wait(bars + 8u * (uint32_t)(L & 3), parity(L));
+        for (int L = waited + 1; L <= issued; L++) (void)mbar_wait(bar_of(L), parity(L));
       }
       return;
     }
   }
 }
 
+// minimum blocks per SM each storage type is compiled for (the register cap
+// follows): 3 for 8-byte storage (80 registers; shared memory holds 3 blocks);
+// none for 4-byte storage (the compiler's 62-64 registers give 4 blocks, and a
+// cap of 4 blocks measured 6% slower)
+template <typename R> struct GMinBlocks { static constexpr int v = 3; };
+template <> struct GMinBlocks<float> { static constexpr int v = 0; };
+
 template <typename R, int SYM>
-__global__ void __launch_bounds__(NT) k_grid_tma(const GridArgs<typename GNum<R>::S> a, int step) {
+__global__ void __launch_bounds__(NT, GMinBlocks<R>::v) k_grid_tma(const GridArgs<typename GNum<R>::S> a, int step) {
   const GridMaps *M = reinterpret_cast<const GridMaps *>(a.tmaps);
   grid_block_tma<R, SYM>(a, M, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x, step);
 }
 
 template <typename R, int SYM>
-__global__ void __launch_bounds__(NT)
+__global__ void __launch_bounds__(NT, GMinBlocks<R>::v)
     k_grid_tma_batch(const GridArgs<typename GNum<R>::S> *__restrict__ args, const int *__restrict__ block_start,
                      int n_members, int step) {
   const int id = blockIdx.x;
