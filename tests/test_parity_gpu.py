@@ -7,6 +7,10 @@ Tolerances (relative L2 over every field and every trace):
   f64        1e-10
   df64       1e-10  (double-float: 48-bit significand on the FP32 pipes)
   f32        1e-4   (FP32 state; traces are recorded in FP64)
+df64 and f32 have FP32's exponent range: a sensor the wave has not reached
+carries values of 1e-160 and the like in FP64 that they hold as zero, so for
+these two forms each trace's error is taken relative to at least 1e-6 of the
+largest trace's norm (TRACE_FLOOR).
 """
 import numpy as np
 import pytest
@@ -19,12 +23,13 @@ from pannde_gb300.solver import Solver
 pytestmark = pytest.mark.gpu
 
 TOL = {"f64_exact": 0.0, "f64": 1e-10, "df64": 1e-10, "f32": 1e-4}
+TRACE_FLOOR = {"df64": 1e-6, "f32": 1e-6}  # of the largest trace norm
 
 
-def rel_l2(a, b):
+def rel_l2(a, b, floor=0.0):
     a = np.asarray(a, np.float64).ravel()
     b = np.asarray(b, np.float64).ravel()
-    d = np.linalg.norm(b)
+    d = max(np.linalg.norm(b), floor)
     return float(np.linalg.norm(a - b) / (d if d > 0 else 1.0))
 
 
@@ -40,8 +45,10 @@ def compare(prec, dev, ref):
         return 0.0
     errs = [rel_l2(V[k], ref["V"][k]) for k in range(3)] + [rel_l2(S[k], ref["S"][k]) for k in range(6)]
     if tr is not None and ref["traces"].size:
+        rt = ref["traces"]
+        floor = TRACE_FLOOR.get(prec, 0.0) * max(np.linalg.norm(rt[:, i]) for i in range(rt.shape[1]))
         for i in range(tr.shape[1]):  # every trace on its own
-            errs.append(rel_l2(tr[:, i], ref["traces"][:, i]))
+            errs.append(rel_l2(tr[:, i], rt[:, i], floor))
     worst = max(errs)
     assert worst <= TOL[prec], f"{prec}: worst rel L2 {worst:.3e}"
     return worst
