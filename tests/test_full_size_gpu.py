@@ -21,7 +21,11 @@ Checks:
   the plain one to relative L2 <= 1e-15 (all forms).  A kernel that mixed
   values of different steps or blocks would fail it;
 * the FP64 energy audit of the holed plate without sources: bounded, and the
-  FP32 form's energy follows the FP64 form's within 1e-4.
+  FP32 form's energy follows the FP64 form's within 1e-4;
+* the batched workload: 96 seeded L-brackets (51 M cells in all, cracks as
+  disconnected faces, every sixth with a water column), FP32, in one batch:
+  every member bit-identical to its run alone, two members against the oracle
+  (and bit-identical to it in exact mode).
 """
 import dataclasses
 
@@ -30,7 +34,7 @@ import pytest
 
 import oracle
 from pannde_gb300 import cases
-from pannde_gb300.solver import Solver
+from pannde_gb300.solver import Batch, Solver
 from tests.test_energy_gpu import pulse_state
 from tests.test_parity_gpu import compare, random_state, rel_l2, run_dev
 
@@ -140,3 +144,39 @@ def test_holed_plate_energy_audit(cuda_device, holed):
     assert e64[0] > 0
     assert np.all(np.abs(e64 - e64[0]) <= 0.02 * e64[0])
     assert np.max(np.abs(tot["f32"] - e64) / e64) <= 1e-4
+
+
+def test_bracket_batch_full_size(cuda_device):
+    steps = 40
+    cs = [cases.bracket_case(1000 + i, nsteps=steps, water_column=(i % 6 == 0)) for i in range(96)]
+    assert sum(c.mesh.n_cells for c in cs) > 50_000_000
+    alone = []
+    for c in cs:
+        with Solver.from_case(c, precision="f32", capacity=steps) as s:
+            s.solve(steps)
+            alone.append((s.get_state(), s.traces(), s.time))
+    sv = [Solver.from_case(c, precision="f32", capacity=steps) for c in cs]
+    try:
+        with Batch() as b:
+            for s in sv:
+                b.add(s)
+            b.solve(17)
+            b.solve(steps - 17)
+        for s, ((V, S), tr, t) in zip(sv, alone):
+            assert s.time == t
+            Vb, Sb = s.get_state()
+            for x, y in zip(V + S, Vb + Sb):
+                assert np.array_equal(x, y)
+            assert np.array_equal(s.traces(), tr)
+    finally:
+        for s in sv:
+            s.close()
+    for i in (0, 7):  # member 0 carries a water column
+        c = cs[i]
+        ref = oracle.run(c.mesh, c.material_fields(), c.dt, c.sources, steps, c.sensors)
+        (V, S), tr, t = alone[i]
+        assert t == ref["time"]
+        compare("f32", (V, S, tr), ref)
+        dev, t = run_dev(c.mesh, c, c.dt, c.sources, steps, c.sensors, "f64_exact")
+        assert t == ref["time"]
+        compare("f64_exact", dev, ref)

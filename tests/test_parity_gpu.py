@@ -10,7 +10,12 @@ Tolerances (relative L2 over every field and every trace):
 df64 and f32 have FP32's exponent range: a sensor the wave has not reached
 carries values of 1e-160 and the like in FP64 that they hold as zero, so for
 these two forms each trace's error is taken relative to at least 1e-6 of the
-largest trace's norm (TRACE_FLOOR).
+largest trace's norm (TRACE_FLOOR).  A field component can be pure round-off
+(the shear stresses of a solid driven only by a pressure source: 1e-43 beside
+normal stresses of 1e-10), which no form that reorders the arithmetic
+reproduces; outside exact mode each component's error is taken relative to at
+least 1e-6 of the largest norm among the components of its vector / tensor
+(FIELD_FLOOR).
 """
 import numpy as np
 import pytest
@@ -24,6 +29,7 @@ pytestmark = pytest.mark.gpu
 
 TOL = {"f64_exact": 0.0, "f64": 1e-10, "df64": 1e-10, "f32": 1e-4}
 TRACE_FLOOR = {"df64": 1e-6, "f32": 1e-6}  # of the largest trace norm
+FIELD_FLOOR = 1e-6  # of the largest component norm of V (S)
 
 
 def rel_l2(a, b, floor=0.0):
@@ -43,7 +49,10 @@ def compare(prec, dev, ref):
         if tr is not None:
             assert np.array_equal(tr, ref["traces"])
         return 0.0
-    errs = [rel_l2(V[k], ref["V"][k]) for k in range(3)] + [rel_l2(S[k], ref["S"][k]) for k in range(6)]
+    fv = FIELD_FLOOR * max(np.linalg.norm(x) for x in ref["V"])
+    fs = FIELD_FLOOR * max(np.linalg.norm(x) for x in ref["S"])
+    errs = [rel_l2(V[k], ref["V"][k], fv) for k in range(3)] + \
+           [rel_l2(S[k], ref["S"][k], fs) for k in range(6)]
     if tr is not None and ref["traces"].size:
         rt = ref["traces"]
         floor = TRACE_FLOOR.get(prec, 0.0) * max(np.linalg.norm(rt[:, i]) for i in range(rt.shape[1]))
