@@ -104,6 +104,22 @@ __device__ __forceinline__ void diffsum22(df64 a, df64 b, df64 c, df64 d, df64 &
   diff = sub_norm(cd, ab);
   sum = add_norm(ab, cd);
 }
+// (b + c) - (a + d) and (c + d) - (a + b) as (c - a) + (b - d) and
+// (c - a) - (b - d): two pair differences shared (38 flops against 54)
+__device__ __forceinline__ df64_unnorm sub_lazy(df64 a, df64 b) {
+  const df64 s = two_sum(a.hi, -b.hi);
+  return {s.hi, __fadd_rn(s.lo, __fsub_rn(a.lo, b.lo))};
+}
+__device__ __forceinline__ void diffdiff22(df64 a, df64 b, df64 c, df64 d, df64 &dx, df64 &dy) {
+  const df64_unnorm u = sub_lazy(c, a), w = sub_lazy(b, d);
+  dx = add_norm(u, w);
+  dy = sub_norm(u, w);
+}
+template <typename T> __device__ __forceinline__ void diffdiff22(T a, T b, T c, T d, T &dx, T &dy) {
+  const T u = c - a, w = b - d;
+  dx = u + w;
+  dy = u - w;
+}
 template <typename T> __device__ __forceinline__ T diff22(T b, T c, T a, T d) { return (b + c) - (a + d); }
 template <typename T> __device__ __forceinline__ T sum22(T a, T b, T c, T d) { return (a + b) + (c + d); }
 template <typename T> __device__ __forceinline__ void diffsum22(T a, T b, T c, T d, T &diff, T &sum) {

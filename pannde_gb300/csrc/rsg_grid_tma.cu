@@ -308,7 +308,8 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
       R px4, s4;
       diffsum22(A, D, B, C, px4, s4);
       A = cellv(5, ra); B = cellv(5, ib); C = cellv(5, ic); D = cellv(5, id);
-      const R px5 = diff22(B, C, A, D), py5 = diff22(C, D, A, B);
+      R px5, py5;
+      diffdiff22(A, B, C, D, px5, py5);
       if (k >= k0) {
         R ax, ay, az;
         if constexpr (CUBIC) {  // 0.25/h folded into dt/rho and the force weights
