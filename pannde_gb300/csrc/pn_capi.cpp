@@ -116,13 +116,9 @@ int choose_form(const pn::MeshTables &m, const pn::MaterialTables &mt, int preci
                 pn::GridMap &g) {
   if (form == PN_FORM_TABLE) return PN_FORM_TABLE;
   pn::detect_grid(m, g);
-  if (pn::grid_eligible(m, mt, precision, g)) return PN_FORM_GRID;
-  if (form == PN_FORM_GRID) {
-    std::string why = g.ok ? (precision == PN_PREC_F64_EXACT ? "the exact FP64 form has no grid kernel"
-                                                              : "more than 254 materials")
-                           : g.why;
-    throw pn::SetupError{PN_ERR_INVALID, "grid form unavailable: " + why};
-  }
+  std::string why;
+  if (pn::grid_eligible(m, mt, precision, g, &why)) return PN_FORM_GRID;
+  if (form == PN_FORM_GRID) throw pn::SetupError{PN_ERR_INVALID, "grid form unavailable: " + why};
   return PN_FORM_TABLE;
 }
 

@@ -111,9 +111,59 @@ void ranges_of(std::vector<Keyed> &L, int64_t n_slots, std::vector<int32_t> &rng
 
 }  // namespace
 
-bool grid_eligible(const MeshTables &m, const MaterialTables &mt, int precision, const GridMap &g) {
-  (void)m;
-  return g.ok && precision != PN_PREC_F64_EXACT && mt.n_mat < 255;
+std::vector<int32_t> grid_tile_tops(const GridMap &g) {
+  const Tiles T = tiles_of(g);
+  std::vector<int32_t> top((size_t)T.blocks(), 0);
+  for (int by = 0; by < T.by_count; by++)
+    for (int bx = 0; bx < T.bx_count; bx++) {
+      const int64_t i0 = (int64_t)bx * (T.tx - 1), j0 = (int64_t)by * (T.ty - 1);
+      int32_t t = 0;
+      for (int64_t j = std::max<int64_t>(0, j0 - 1); j < std::min<int64_t>(g.ny, j0 + T.ty); j++)
+        for (int64_t i = std::max<int64_t>(0, i0 - 1); i < std::min<int64_t>(g.nx, i0 + T.tx); i++)
+          t = std::max(t, g.col_top[(size_t)(j * g.nx + i)]);
+      top[(size_t)by * T.bx_count + bx] = t;
+    }
+  return top;
+}
+
+// The tensor-copy kernel (rsg_grid_tma.cu) runs when the stiffness table fits
+// its shared-memory rows and every buffer meets the copy rules; otherwise the
+// classic kernel (rsg_grid.cu).  PN_GRID_KERNEL=classic selects the classic
+// kernel for comparisons.
+static bool want_tma(int32_t n_mat) {
+  const char *v = std::getenv("PN_GRID_KERNEL");
+  if (v && std::strcmp(v, "classic") == 0) return false;
+  return n_mat + 1 <= kGridTmaRowsMax;
+}
+
+// The grid form moves about 2.3x fewer bytes per cell-step than the tables;
+// it serves a mesh whose lattice box it marches in at most twice the mesh's
+// own cells.  The tensor-copy kernel stops each tile column at its top solid
+// layer (grid_tile_tops); the classic kernel marches the whole box.
+bool grid_eligible(const MeshTables &m, const MaterialTables &mt, int precision, const GridMap &g,
+                   std::string *why) {
+  auto no = [&](const std::string &r) {
+    if (why) *why = r;
+    return false;
+  };
+  if (!g.ok) return no(g.why);
+  if (precision == PN_PREC_F64_EXACT) return no("the exact FP64 form has no grid kernel");
+  if (mt.n_mat >= 255) return no("more than 254 materials");
+  int64_t marched = 0;
+  if (want_tma(mt.n_mat)) {
+    const Tiles T = tiles_of(g);
+    const std::vector<int32_t> top = grid_tile_tops(g);
+    for (int by = 0; by < T.by_count; by++)
+      for (int bx = 0; bx < T.bx_count; bx++) {
+        const int64_t cols = std::min<int64_t>(T.tx - 1, g.nx - (int64_t)bx * (T.tx - 1)) *
+                             std::min<int64_t>(T.ty - 1, g.ny - (int64_t)by * (T.ty - 1));
+        marched += std::max<int64_t>(cols, 0) * top[(size_t)by * T.bx_count + bx];
+      }
+  } else {
+    marched = g.grid_cells();
+  }
+  if (marched > 2 * (int64_t)m.n_cells) return no("lattice box mostly void");
+  return true;
 }
 
 int64_t grid_footprint(const GridMap &g, const MaterialTables &mt, int precision) {
@@ -123,15 +173,6 @@ int64_t grid_footprint(const GridMap &g, const MaterialTables &mt, int precision
          2 * (int64_t)grid_tma_maps_bytes() + 16;
 }
 
-// The tensor-copy kernel (rsg_grid_tma.cu) runs when the stiffness table fits
-// its shared-memory rows and every buffer meets the copy rules; otherwise the
-// classic kernel (rsg_grid.cu).  PN_GRID_KERNEL=classic selects the classic
-// kernel for comparisons.
-static bool want_tma(const pn_solver *s) {
-  const char *v = std::getenv("PN_GRID_KERNEL");
-  if (v && std::strcmp(v, "classic") == 0) return false;
-  return s->mat.n_mat + 1 <= kGridTmaRowsMax;
-}
 
 void grid_create(pn_solver *s) {
   const GridMap &g = s->grid;
@@ -163,7 +204,7 @@ void grid_create(pn_solver *s) {
   s->cur = 0;
   s->d_err = s->alloc<int32_t>(16);
   ck(cudaMemsetAsync(s->d_err, 0, 16, s->stream), "memset");
-  if (want_tma(s)) {
+  if (want_tma(s->mat.n_mat)) {
     const size_t mb = grid_tma_maps_bytes();
     std::vector<unsigned char> maps(2 * mb);
     bool ok = true;
@@ -176,6 +217,9 @@ void grid_create(pn_solver *s) {
     if (ok) {
       s->d_tmaps = s->alloc<void>(2 * mb);
       s->upload_raw(s->d_tmaps, maps.data(), 2 * mb);
+      const std::vector<int32_t> top = grid_tile_tops(g);
+      s->d_ktop = s->alloc<int32_t>(top.size() * sizeof(int32_t));
+      s->upload_raw(s->d_ktop, top.data(), top.size() * sizeof(int32_t));
       // a cubic lattice: every difference is scaled by the same 0.25/h, which
       // then goes into the coefficients instead of the step (fewer FP64 ops)
       const double h = s->mesh.hx;
@@ -346,6 +390,7 @@ void grid_args(pn_solver *s, GridArgs<T> &a) {
   a.sig_stride = 0;
   a.sig_rows = 1;
   a.err = s->d_err;
+  a.ktop = s->d_ktop;
   a.n_rows = s->mat.n_mat + 1;
   // failure-path test hook: PN_TEST_GRID_SKIP_COPY=<layer> leaves that layer's
   // tile copies unissued, so the tensor-copy kernel's bounded wait runs out

@@ -567,6 +567,12 @@ void detect_grid(const MeshTables &t, GridMap &g, double max_void_fraction) {
     }
     site = 1;
   }
+  g.col_top.assign((size_t)nx * ny, 0);
+  for (int32_t c = 0; c < t.n_cells; c++) {
+    const int64_t q = g.cell_grid[c], i = q % pcx, j = (q / pcx) % ny, k = q / (pcx * ny);
+    int32_t &top = g.col_top[(size_t)(j * nx + i)];
+    top = std::max(top, (int32_t)k + 1);
+  }
   g.ok = true;
 }
 

@@ -109,6 +109,7 @@ struct GridMap {
   int32_t pnx = 0, pcx = 0;        // row pitch (sites) of node / cell buffers
   std::vector<int64_t> node_grid;  // mesh node -> grid node
   std::vector<int64_t> cell_grid;  // mesh cell -> grid cell
+  std::vector<int32_t> col_top;    // [ny][nx] 1 + the highest solid cell layer of column (i, j), 0 if none
   // lattice sites (the box, without padding)
   int64_t grid_nodes() const { return (int64_t)(nx + 1) * (ny + 1) * (nz + 1); }
   int64_t grid_cells() const { return (int64_t)nx * ny * nz; }
@@ -123,7 +124,9 @@ struct GridMap {
 
 // Detects the voxel-grid structure of a uniformly spaced mesh; gives up
 // (ok=false) when the lattice box holds more than max_void_fraction void cells.
-void detect_grid(const MeshTables &t, GridMap &g, double max_void_fraction = 0.5);
+// Whether the grid form pays on a sparse box is decided later by the work of
+// its kernel (grid_eligible).
+void detect_grid(const MeshTables &t, GridMap &g, double max_void_fraction = 0.95);
 
 // Per-tile [begin,end) ranges of a list sorted by element.
 void tile_ranges(const std::vector<int32_t> &elems, int32_t n_elems, int tile,

@@ -85,6 +85,7 @@ struct pn_solver {
   int sym = 0;             // material symmetry class of the stiffness table
   uint8_t *d_gmat = nullptr;
   void *d_tmaps = nullptr;   // tensor maps [2 input parities] (null: classic kernel)
+  int32_t *d_ktop = nullptr; // [tiles] cell layers the tensor-copy kernel marches per tile
   // cubic lattice with the tensor-copy kernel: 0.25/h folded into dt/rho, dt*C
   // and the force weights (the kernel's g is then 1); 1.0 when not folded
   double gfold = 1.0;
@@ -252,7 +253,12 @@ void table_put_state(pn_solver *s, const double *const *V, const double *const *
 void table_get_state(pn_solver *s, double *const *V, double *const *S);
 
 // grid form (pn_grid.cpp)
-bool grid_eligible(const MeshTables &m, const MaterialTables &mt, int precision, const GridMap &g);
+// whether the grid form serves this mesh (why: the reason when not)
+bool grid_eligible(const MeshTables &m, const MaterialTables &mt, int precision, const GridMap &g,
+                   std::string *why = nullptr);
+// per tile: 1 + the highest solid cell layer in the columns of its cell box
+// with the apron, i.e. the cell layers the tensor-copy kernel marches
+std::vector<int32_t> grid_tile_tops(const GridMap &g);
 int64_t grid_footprint(const GridMap &g, const MaterialTables &mt, int precision);
 void grid_create(pn_solver *s);
 void grid_sources(pn_solver *s);

@@ -50,6 +50,9 @@ struct GridArgs {
   int64_t rec_cap;       // records beyond this are not written
   int32_t *err;          // device error word (bounded waits that gave up), or null
   const void *tmaps;     // tensor maps of this step's input buffers (rsg_grid_tma.cu), or null
+  const int32_t *ktop;   // [tiles] cell layers below the tile's top solid cell + 1 (its
+                         // node layers above are void; the tensor-copy kernel stops
+                         // there), or null: nz
   int32_t n_rows;        // rows of ctab (materials + the void row)
   int32_t test_skip_layer;  // failure-path test: the layer whose copies are never issued (kNoLayer: none)
 };

@@ -216,8 +216,12 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
   const R gx = N::val(a.g[0]), gy = N::val(a.g[1]), gz = N::val(a.g[2]);
   const St *sigrow = a.sigval ? a.sigval + (int64_t)min(step, a.sig_rows - 1) * a.sig_stride : nullptr;
   const int64_t rec = a.rec + step;
-  const int k0 = bz * a.kchunk, k1 = min(nz, k0 + a.kchunk);
-  const bool last_chunk = k1 == nz;
+  // columns of the tile (and its apron) hold no solid cell at or above ktop:
+  // the march ends there, and a chunk above it has nothing to do
+  const int ktop = a.ktop ? min(nz, __ldg(a.ktop + blk)) : nz;
+  const int k0 = bz * a.kchunk, k1 = min(ktop, k0 + a.kchunk);
+  if (k0 >= ktop) return;
+  const bool last_chunk = k1 == ktop;
 
   // tile origins of the copies (x on the 16-byte boundary) and offsets in them
   const int xs_c = floor_to(i0 - 1, G::A), oc = i0 - 1 - xs_c;

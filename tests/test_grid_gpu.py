@@ -62,6 +62,56 @@ def test_grid_holes_random_state(cuda_device, prec):
     compare(prec, dev, ref)
 
 
+def stepped_solid():
+    """Columns of many heights: a staircase along y for x < 29, short columns
+    (4 layers) for x >= 29 so that the second tile column stops early, a void
+    shaft, and an overhang (void below solid)."""
+    solid = np.zeros((50, 20, 24), dtype=bool)
+    for j in range(20):
+        solid[:29, j, :3 + (5 * j) % 21] = True
+    solid[29:, :, :4] = True
+    solid[12:17, 6:9, :] = False
+    solid[3:8, 14:18, 2:5] = False
+    return solid
+
+
+@pytest.mark.parametrize("kchunk", [None, "3"])
+@pytest.mark.parametrize("prec", PRECS)
+def test_grid_stepped_columns(cuda_device, prec, kchunk, monkeypatch):
+    """The tensor-copy kernel stops each tile's march at the tile's top solid
+    layer; columns of every height, with and without z chunks, against the
+    oracle from a random state with a force and a moment source."""
+    if kchunk:
+        monkeypatch.setenv("PN_GRID_KCHUNK", kchunk)
+    m = cases.voxel_mesh(stepped_solid(), 1e-4)
+    c = cases.Case("steps", m, np.array([2700.0]),
+                   cases.c21_from_6x6(cases.isotropic(70e9, 0.33))[None], np.zeros(m.n_cells, np.int32), 4e-9)
+    t = np.linspace(0.0, 2e-7, 60)
+    v = np.sin(2e7 * t)
+    src = [cases.WindowSource(N.PN_SOURCE_FORCE, 0, 2, (1.0e-3, 1.5e-3, 0.4e-3), 0.3e-3, 1e-4, t, v),
+           cases.WindowSource(N.PN_SOURCE_MOMENT, 1, 0, (4.0e-3, 1.0e-3, 0.2e-3), 0.3e-3, 1e-4, t, v)]
+    V0, S0 = random_state(m, 21)
+    sens = np.array([0, 101, m.n_nodes // 3, m.n_nodes - 1], np.int32)
+    ref = oracle.run(m, c.material_fields(), c.dt, src, 30, sens, V0=V0, S0=S0)
+    with Solver(m, c, c.dt, prec, "grid") as s:
+        assert s.info()["kernel_name"] == "tma"
+    dev, _ = run_grid(m, c, c.dt, src, 30, sens, prec, V0=V0, S0=S0, chunks=[11, 19])
+    compare(prec, dev, ref)
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_grid_slab_cracked_brackets(cuda_device, prec):
+    """L-brackets (crack as a removed cell slab) take the grid form: their
+    lattice box is mostly void, but the march per tile ends at the tile's top
+    solid layer."""
+    for seed, wc in ((1003, False), (1006, True)):
+        c = cases.bracket_case(seed, nsteps=40, water_column=wc, crack="slab", scale=0.35)
+        ref = oracle.run(c.mesh, c.material_fields(), c.dt, c.sources, c.nsteps, c.sensors)
+        dev, t = run_grid(c.mesh, c, c.dt, c.sources, c.nsteps, c.sensors, prec)
+        assert t == ref["time"]
+        compare(prec, dev, ref)
+
+
 @pytest.mark.parametrize("prec", PRECS)
 def test_grid_laminate_moments_and_forces(cuda_device, prec):
     c = cases.laminate_case(nx=33, ny=29, nz=8, nsteps=40, radius=0.5e-3, n_sensors=6)

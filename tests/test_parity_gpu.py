@@ -7,15 +7,18 @@ Tolerances (relative L2 over every field and every trace):
   f64        1e-10
   df64       1e-10  (double-float: 48-bit significand on the FP32 pipes)
   f32        1e-4   (FP32 state; traces are recorded in FP64)
-df64 and f32 have FP32's exponent range: a sensor the wave has not reached
-carries values of 1e-160 and the like in FP64 that they hold as zero, so for
-these two forms each trace's error is taken relative to at least 1e-6 of the
-largest trace's norm (TRACE_FLOOR).  A field component can be pure round-off
-(the shear stresses of a solid driven only by a pressure source: 1e-43 beside
-normal stresses of 1e-10), which no form that reorders the arithmetic
-reproduces; outside exact mode each component's error is taken relative to at
-least 1e-6 of the largest norm among the components of its vector / tensor
-(FIELD_FLOOR).
+df64 and f32 have FP32's exponent range.  A sensor the wave has not reached
+holds only the stencil's leakage ahead of the wave front, values of 1e-160
+and the like in FP64, which these forms hold as zero or as subnormals (FP32
+below 1.2e-38; a double-float below about 2e-31, whose low word is then
+subnormal) with few significand bits.  For these two forms each trace's
+error is therefore taken relative to at least 1e-6 of the largest trace's
+norm (TRACE_FLOOR) and at least 1e-30 per value in root-mean-square
+(RANGE_FLOOR).  A field component can be pure round-off (the shear stresses
+of a solid driven only by a pressure source: 1e-43 beside normal stresses of
+1e-10), which no form that reorders the arithmetic reproduces; outside exact
+mode each component's error is taken relative to at least 1e-6 of the
+largest norm among the components of its vector / tensor (FIELD_FLOOR).
 """
 import numpy as np
 import pytest
@@ -30,6 +33,7 @@ pytestmark = pytest.mark.gpu
 TOL = {"f64_exact": 0.0, "f64": 1e-10, "df64": 1e-10, "f32": 1e-4}
 TRACE_FLOOR = {"df64": 1e-6, "f32": 1e-6}  # of the largest trace norm
 FIELD_FLOOR = 1e-6  # of the largest component norm of V (S)
+RANGE_FLOOR = {"df64": 1e-30, "f32": 1e-30}  # root-mean-square per value
 
 
 def rel_l2(a, b, floor=0.0):
@@ -49,13 +53,15 @@ def compare(prec, dev, ref):
         if tr is not None:
             assert np.array_equal(tr, ref["traces"])
         return 0.0
-    fv = FIELD_FLOOR * max(np.linalg.norm(x) for x in ref["V"])
-    fs = FIELD_FLOOR * max(np.linalg.norm(x) for x in ref["S"])
+    tiny = RANGE_FLOOR.get(prec, 0.0)
+    fv = max(FIELD_FLOOR * max(np.linalg.norm(x) for x in ref["V"]), tiny * np.sqrt(ref["V"][0].size))
+    fs = max(FIELD_FLOOR * max(np.linalg.norm(x) for x in ref["S"]), tiny * np.sqrt(ref["S"][0].size))
     errs = [rel_l2(V[k], ref["V"][k], fv) for k in range(3)] + \
            [rel_l2(S[k], ref["S"][k], fs) for k in range(6)]
     if tr is not None and ref["traces"].size:
         rt = ref["traces"]
-        floor = TRACE_FLOOR.get(prec, 0.0) * max(np.linalg.norm(rt[:, i]) for i in range(rt.shape[1]))
+        floor = max(TRACE_FLOOR.get(prec, 0.0) * max(np.linalg.norm(rt[:, i]) for i in range(rt.shape[1])),
+                    tiny * np.sqrt(rt[:, 0].size))
         for i in range(tr.shape[1]):  # every trace on its own
             errs.append(rel_l2(tr[:, i], rt[:, i], floor))
     worst = max(errs)
