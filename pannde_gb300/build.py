@@ -6,6 +6,7 @@ Sources (``pannde_gb300/csrc``):
   rsg_grid.cu   fused voxel-grid step kernel  nvcc, sm_103a
   rsg_grid_tma.cu  grid step, tensor-copy staging  nvcc, sm_103a
   rsg_state.cu  state convert / permute       nvcc, sm_103a
+  rsg_split.cu  grid form: fix-up of split lattice sites (cracks)  nvcc, sm_103a
   pn_noalloc.cu fixed scratch of the allocation-free batch solve   nvcc
   rsg_energy.cu FP64 energy audit             nvcc, sm_103a
   pn_energy.cpp energy audit tables           g++
@@ -59,6 +60,7 @@ def _jobs() -> list[tuple[list[str], Path]]:
         (common_cu + ["-c", str(CSRC / "rsg_grid.cu")], OUT / "rsg_grid.o"),
         (common_cu + ["-c", str(CSRC / "rsg_grid_tma.cu")], OUT / "rsg_grid_tma.o"),
         (common_cu + ["-c", str(CSRC / "rsg_state.cu")], OUT / "rsg_state.o"),
+        (common_cu + ["-c", str(CSRC / "rsg_split.cu")], OUT / "rsg_split.o"),
         (common_cu + ["-c", str(CSRC / "pn_noalloc.cu")], OUT / "pn_noalloc.o"),
         (common_cu + ["-c", str(CSRC / "rsg_energy.cu")], OUT / "rsg_energy.o"),
         (common_cc + ["-c", str(CSRC / "pn_energy.cpp")], OUT / "pn_energy.o"),

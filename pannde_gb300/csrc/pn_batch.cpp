@@ -314,6 +314,7 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision, const Stage &stage, 
   const int n = (int)b->members.size();
   std::vector<pn::GridArgs<T>> ga[2] = {std::vector<pn::GridArgs<T>>(n), std::vector<pn::GridArgs<T>>(n)};
   std::vector<int> bs(n + 1, 0);
+  std::vector<int> split(2 * (n + 1), 0);  // prefixes of the members' copies, then of their fix cells
   const int tx = pn::grid_tile_x(), ty = pn::grid_tile_y();
   int sym = 2;
   bool tma = true;  // the tensor-copy kernel when every member has its maps
@@ -359,13 +360,17 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision, const Stage &stage, 
         const int64_t blocks = (int64_t)(a.nx / (tx - 1) + 1) * (a.ny / (ty - 1) + 1) *
                                ((a.nz + a.kchunk - 1) / a.kchunk);
         bs[m + 1] = (int)(bs[m] + blocks);
+        split[m + 1] = split[m] + a.n_copies;
+        split[n + 1 + m + 1] = split[n + 1 + m] + a.n_fix;
       }
-      g = stage(sizeof(pn::GridArgs<T>) * n, n + 1);
+      g = stage(sizeof(pn::GridArgs<T>) * n, 2 * (n + 1));
       for (int p = 0; p < 2; p++)
         pn::ck(cudaMemcpyAsync(g.args[p], ga[p].data(), sizeof(pn::GridArgs<T>) * n, cudaMemcpyHostToDevice,
                                b->stream), "batch args");
       pn::ck(cudaMemcpyAsync(g.start[0], bs.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, b->stream),
              "batch blocks");
+      pn::ck(cudaMemcpyAsync(g.start[1], split.data(), sizeof(int) * split.size(), cudaMemcpyHostToDevice,
+                             b->stream), "batch split sites");
       staged_shape = c;
       return bs[n];
     };
@@ -388,6 +393,7 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision, const Stage &stage, 
     sig.p[0] = g.args[0];
     sig.p[1] = g.args[1];
     sig.p[2] = g.start[0];
+    sig.p[3] = g.start[1];
     run_chunk(b, std::make_tuple((int)PN_FORM_GRID, precision, log2_class(n), log2_class(work)),
               (int)(sizeof(kGridShapes) / sizeof(int)), chunk, may_alloc, sig, prepare, [&](int c, int32_t k) {
                 prepare(c);
@@ -400,6 +406,16 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision, const Stage &stage, 
                 pn::ck(tma ? pn::launch_grid_tma_batch(L, precision, k, b->stream)
                            : pn::launch_grid_batch(L, precision, k, b->stream),
                        "batch step");
+                if (split[n] > 0 || split[2 * n + 1] > 0) {
+                  pn::GridSplitBatch F;
+                  F.n_members = n;
+                  F.args = g.args[k & 1];
+                  F.copy_start = g.start[1];
+                  F.fix_start = g.start[1] + n + 1;
+                  F.total_copies = split[n];
+                  F.total_fix = split[2 * n + 1];
+                  pn::ck(pn::launch_grid_split_batch(F, precision, k, b->stream), "batch split sites");
+                }
               });
     pn::ck(cudaStreamSynchronize(b->stream), "batch chunk");
     advance(b, chunk);
@@ -426,6 +442,7 @@ size_t scratch_bytes(const pn_batch *b) {
   const size_t n = b->members.size();
   const pn_solver *f = b->members.front();
   size_t args = 0;
+  const size_t starts = f->form == PN_FORM_GRID ? 2 * (n + 1) : n + 1;  // grid: block and split prefixes
   if (f->form == PN_FORM_GRID)
     args = f->is_df64() ? sizeof(pn::GridArgs<float2>) : f->esz == 8 ? sizeof(pn::GridArgs<double>)
                                                                        : sizeof(pn::GridArgs<float>);
@@ -433,7 +450,7 @@ size_t scratch_bytes(const pn_batch *b) {
     args = f->is_df64() ? std::max(sizeof(pn::VelArgs<float2>), sizeof(pn::StressArgs<float2>))
          : f->esz == 8  ? std::max(sizeof(pn::VelArgs<double>), sizeof(pn::StressArgs<double>))
                         : std::max(sizeof(pn::VelArgs<float>), sizeof(pn::StressArgs<float>));
-  return ScratchStaging::bytes(args * n, n + 1);
+  return ScratchStaging::bytes(args * n, starts);
 }
 
 }  // namespace

@@ -27,11 +27,11 @@ static void energy_tables(pn_solver *s) {
   s->upload_raw(s->d_ecomp, comp.data(), comp.size() * sizeof(double));
   if (s->form == PN_FORM_GRID) {
     const GridMap &g = s->grid;
-    std::vector<double> site((size_t)g.node_sites(), 0.0);
+    std::vector<double> site((size_t)g.node_len(), 0.0);
     for (int32_t u = 0; u < nn; u++) site[(size_t)g.node_grid[u]] = mass[u];
     s->d_emass = s->alloc<double>(site.size() * sizeof(double));
     s->upload_raw(s->d_emass, site.data(), site.size() * sizeof(double));
-    s->e_nodes = g.node_sites();
+    s->e_nodes = g.node_len();
     s->e_cells = g.cell_sites();
   } else {
     std::vector<double> vol((size_t)nc);

@@ -168,7 +168,7 @@ bool grid_eligible(const MeshTables &m, const MaterialTables &mt, int precision,
 
 int64_t grid_footprint(const GridMap &g, const MaterialTables &mt, int precision) {
   const int64_t e = precision == PN_PREC_F32 ? 4 : 8;
-  const int64_t gn = g.node_sites(), gc = g.cell_sites();
+  const int64_t gn = g.node_len(), gc = g.cell_sites();
   return 2 * (3 * gn + 6 * gc) * e + gn * e + gc + (int64_t)(mt.n_mat + 1) * 36 * e +
          2 * (int64_t)grid_tma_maps_bytes() + 16;
 }
@@ -176,7 +176,7 @@ int64_t grid_footprint(const GridMap &g, const MaterialTables &mt, int precision
 
 void grid_create(pn_solver *s) {
   const GridMap &g = s->grid;
-  const int64_t gn = g.node_sites(), gc = g.cell_sites();
+  const int64_t gn = g.node_len(), gc = g.cell_sites();
   const size_t e = s->esz;
   for (int b = 0; b < 2; b++) {
     for (int k = 0; k < 3; k++) {
@@ -234,7 +234,81 @@ void grid_create(pn_solver *s) {
       }
     }
   }
+  grid_split_upload(s);
   ck(cudaStreamSynchronize(s->stream), "create sync");
+}
+
+void grid_split_upload(pn_solver *s) {
+  const GridMap &g = s->grid;
+  s->release(s->d_copies); s->release(s->d_fix);
+  s->release(s->d_cf_dir); s->release(s->d_cf_sig); s->release(s->d_cf_w); s->release(s->d_cs_idx);
+  s->release(s->d_cm_comp); s->release(s->d_cm_sig); s->release(s->d_cm_w);
+  if (g.copy_node.empty()) return;
+  auto &F = s->split_forces;
+  auto &Sn = s->split_sensors;
+  auto &M = s->fix_moments;
+  std::stable_sort(F.begin(), F.end(), [](const auto &a, const auto &b) { return a.copy < b.copy; });
+  std::stable_sort(Sn.begin(), Sn.end(), [](const auto &a, const auto &b) { return a.copy < b.copy; });
+  std::stable_sort(M.begin(), M.end(), [](const auto &a, const auto &b) { return a.fix < b.fix; });
+  std::vector<SplitCopy> cp(g.copy_node.size());
+  size_t f = 0, e = 0;
+  for (size_t q = 0; q < cp.size(); q++) {
+    int64_t i, j, k;
+    node_ijk(g, g.copy_site[q], i, j, k);
+    SplitCopy &c = cp[q];
+    c.i = (int32_t)i;
+    c.j = (int32_t)j;
+    c.k = (int32_t)k;
+    c.mask = g.copy_mask[q];
+    c.v = g.node_grid[(size_t)g.copy_node[q]];
+    c.f0 = (int32_t)f;
+    while (f < F.size() && F[f].copy == (int32_t)q) f++;
+    c.f1 = (int32_t)f;
+    c.s0 = (int32_t)e;
+    while (e < Sn.size() && Sn[e].copy == (int32_t)q) e++;
+    c.s1 = (int32_t)e;
+  }
+  std::vector<FixCell> fx(g.fix_cell.size());
+  size_t m = 0;
+  for (size_t q = 0; q < fx.size(); q++) {
+    const int32_t c = g.fix_cell[q];
+    fx[q].cell = g.cell_grid[(size_t)c];
+    for (int kb = 0; kb < 8; kb++) fx[q].v[kb] = g.node_grid[(size_t)s->mesh.hex[(size_t)c * 8 + kb]];
+    fx[q].m0 = (int32_t)m;
+    while (m < M.size() && M[m].fix == (int32_t)q) m++;
+    fx[q].m1 = (int32_t)m;
+  }
+  s->d_copies = s->alloc<SplitCopy>(cp.size() * sizeof(SplitCopy));
+  s->upload_raw(s->d_copies, cp.data(), cp.size() * sizeof(SplitCopy));
+  s->d_fix = s->alloc<FixCell>(fx.size() * sizeof(FixCell));
+  s->upload_raw(s->d_fix, fx.data(), fx.size() * sizeof(FixCell));
+  std::vector<int32_t> dir(F.size()), sig(F.size()), idx(Sn.size()), comp(M.size()), msig(M.size());
+  std::vector<double> w(F.size()), mw(M.size());
+  for (size_t q = 0; q < F.size(); q++) {
+    dir[q] = F[q].dir;
+    sig[q] = F[q].sig;
+    w[q] = F[q].w;
+  }
+  for (size_t q = 0; q < Sn.size(); q++) idx[q] = Sn[q].idx;
+  for (size_t q = 0; q < M.size(); q++) {
+    comp[q] = M[q].comp;
+    msig[q] = M[q].sig;
+    mw[q] = M[q].w;
+  }
+  s->d_cf_dir = s->alloc<int32_t>(dir.size() * 4);
+  s->d_cf_sig = s->alloc<int32_t>(sig.size() * 4);
+  s->d_cf_w = s->alloc<void>(w.size() * s->esz);
+  s->d_cs_idx = s->alloc<int32_t>(idx.size() * 4);
+  s->d_cm_comp = s->alloc<int32_t>(comp.size() * 4);
+  s->d_cm_sig = s->alloc<int32_t>(msig.size() * 4);
+  s->d_cm_w = s->alloc<void>(mw.size() * s->esz);
+  s->upload_raw(s->d_cf_dir, dir.data(), dir.size() * 4);
+  s->upload_raw(s->d_cf_sig, sig.data(), sig.size() * 4);
+  s->upload_real(s->d_cf_w, w.data(), w.size());
+  s->upload_raw(s->d_cs_idx, idx.data(), idx.size() * 4);
+  s->upload_raw(s->d_cm_comp, comp.data(), comp.size() * 4);
+  s->upload_raw(s->d_cm_sig, msig.data(), msig.size() * 4);
+  s->upload_real(s->d_cm_w, mw.data(), mw.size());
 }
 
 // node / cell -> lattice position maps on the device (first transfer)
@@ -254,7 +328,7 @@ static void ensure_grid_maps(pn_solver *s) {
 // fields scattered to their lattice positions on the device (rsg_state.cu).
 void grid_put_state(pn_solver *s, const double *const *V, const double *const *S) {
   const GridMap &g = s->grid;
-  const int64_t gn = g.node_sites(), gc = g.cell_sites();
+  const int64_t gn = g.node_len(), gc = g.cell_sites();
   ensure_grid_maps(s);
   for (int k = 0; k < 3; k++) {
     ck(cudaMemsetAsync(s->V[s->cur][k], 0, (size_t)gn * s->esz, s->stream), "memset");
@@ -309,7 +383,15 @@ void grid_sources(pn_solver *s) {
     s->upload_real(w, wt.data(), wt.size());
   };
   std::vector<Keyed> F, M;
+  s->split_forces.clear();
+  s->fix_moments.clear();
   for (size_t q = 0; q < fe.size(); q++) {
+    if (q == 0 || fe[q].elem != fe[q - 1].elem) s->n_src_nodes++;
+    const int32_t cp = g.copy_of_node.empty() ? -1 : g.copy_of_node[(size_t)fe[q].elem];
+    if (cp >= 0) {  // a node of a split site: the fix-up applies it
+      s->split_forces.push_back({cp, fe[q].comp, fe[q].sig, fe[q].w / s->gfold});
+      continue;
+    }
     int64_t i, j, k;
     node_ijk(g, g.node_grid[fe[q].elem], i, j, k);
     // every block that computes this node's velocity gets the entry: the
@@ -318,7 +400,6 @@ void grid_sources(pn_solver *s) {
     T.each_block_computing(i, j, [&](int32_t blk, int32_t t) {
       F.push_back(Keyed{(int64_t)blk * (g.nz + 1) + k, t | (fe[q].comp << 16), fe[q].sig, 0, fe[q].w / s->gfold});
     });
-    if (q == 0 || fe[q].elem != fe[q - 1].elem) s->n_src_nodes++;
   }
   for (size_t q = 0; q < me.size(); q++) {
     int64_t i, j, k;
@@ -327,9 +408,12 @@ void grid_sources(pn_solver *s) {
     T.locate(i, j, blk, t);
     M.push_back(Keyed{(int64_t)blk * g.nz + k, t | (me[q].comp << 16), me[q].sig, 0, s->dt * me[q].w});
     if (q == 0 || me[q].elem != me[q - 1].elem) s->n_src_cells++;
+    const int32_t fx = g.fix_of_cell.empty() ? -1 : g.fix_of_cell[(size_t)me[q].elem];
+    if (fx >= 0) s->fix_moments.push_back({fx, me[q].comp, me[q].sig, s->dt * me[q].w});
   }
   upload(F, g.nz + 1, s->d_frng, s->d_fkey, s->d_fsig, s->d_fw);
   upload(M, g.nz, s->d_mrng, s->d_mkey, s->d_msig, s->d_mw);
+  grid_split_upload(s);
   ck(cudaStreamSynchronize(s->stream), "sources upload");
 }
 
@@ -337,7 +421,13 @@ void grid_sensors(pn_solver *s, const std::vector<std::pair<int32_t, int32_t>> &
   const GridMap &g = s->grid;
   const Tiles T = tiles_of(g);
   std::vector<Keyed> L;
+  s->split_sensors.clear();
   for (auto &p : pr) {
+    const int32_t cp = g.copy_of_node.empty() ? -1 : g.copy_of_node[(size_t)p.first];
+    if (cp >= 0) {  // a node of a split site: the fix-up records it
+      s->split_sensors.push_back({cp, p.second});
+      continue;
+    }
     int64_t i, j, k;
     node_ijk(g, g.node_grid[p.first], i, j, k);
     int32_t blk, t;
@@ -357,6 +447,7 @@ void grid_sensors(pn_solver *s, const std::vector<std::pair<int32_t, int32_t>> &
   s->upload_raw(s->d_srng, r.data(), r.size() * 4);
   s->upload_raw(s->d_skey, key.data(), key.size() * 4);
   s->upload_raw(s->d_sidx, idx.data(), idx.size() * 4);
+  grid_split_upload(s);
 }
 
 template <typename T>
@@ -392,6 +483,17 @@ void grid_args(pn_solver *s, GridArgs<T> &a) {
   a.err = s->d_err;
   a.ktop = s->d_ktop;
   a.n_rows = s->mat.n_mat + 1;
+  a.n_copies = (int32_t)g.copy_node.size();
+  a.n_fix = (int32_t)g.fix_cell.size();
+  a.copies = s->d_copies;
+  a.cf_dir = s->d_cf_dir;
+  a.cf_sig = s->d_cf_sig;
+  a.cf_w = (const T *)s->d_cf_w;
+  a.cs_idx = s->d_cs_idx;
+  a.fix = s->d_fix;
+  a.cm_comp = s->d_cm_comp;
+  a.cm_sig = s->d_cm_sig;
+  a.cm_w = (const T *)s->d_cm_w;
   // failure-path test hook: PN_TEST_GRID_SKIP_COPY=<layer> leaves that layer's
   // tile copies unissued, so the tensor-copy kernel's bounded wait runs out
   const char *skip = std::getenv("PN_TEST_GRID_SKIP_COPY");
@@ -444,6 +546,7 @@ void run(pn_solver *s, int32_t nsteps) {
       else if constexpr (std::is_same<T, float2>::value) e = launch_grid_df64(a, s->sym, s->stream);
       else if constexpr (std::is_same<T, double>::value) e = launch_grid_f64(a, s->sym, s->stream);
       else e = launch_grid_f32(a, s->sym, s->stream);
+      if (e == cudaSuccess && (a.n_copies > 0 || a.n_fix > 0)) e = launch_grid_split(&a, s->precision, s->stream);
       if (s->timing) {
         ck(cudaEventRecord(m.b, s->stream), "event");
         s->marks.push_back(m);

@@ -531,14 +531,21 @@ void detect_grid(const MeshTables &t, GridMap &g, double max_void_fraction) {
   g.node_grid.resize(t.n_nodes);
 #pragma omp parallel for schedule(static)
   for (int32_t n = 0; n < t.n_nodes; n++) g.node_grid[n] = g.node_at(gi[n], gj[n], gk[n]);
-  std::vector<uint8_t> taken((size_t)g.node_sites(), 0);
+  // the first node on a site keeps it; later ones get tail slots (split sites)
+  std::vector<int32_t> first((size_t)g.node_sites(), -1);
+  std::vector<uint8_t> split((size_t)g.node_sites(), 0);
   for (int32_t n = 0; n < t.n_nodes; n++) {
-    uint8_t &site = taken[(size_t)g.node_grid[n]];
-    if (site) {
-      g.why = "two nodes on one lattice site";
-      return;
+    const int64_t site = g.node_grid[n];
+    if (first[(size_t)site] < 0) {
+      first[(size_t)site] = n;
+    } else {
+      split[(size_t)site] = 1;
+      g.node_grid[n] = g.node_sites() + g.n_extra++;
     }
-    site = 1;
+  }
+  if (g.n_extra > t.n_nodes / 8) {
+    g.why = "too many nodes sharing lattice sites";
+    return;
   }
   static const int bx[8] = {0, 1, 1, 0, 0, 1, 1, 0}, by[8] = {0, 0, 1, 1, 0, 0, 1, 1},
                    bz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
@@ -566,6 +573,32 @@ void detect_grid(const MeshTables &t, GridMap &g, double max_void_fraction) {
       return;
     }
     site = 1;
+  }
+  if (g.n_extra > 0) {  // copies and fix cells
+    g.copy_of_node.assign((size_t)t.n_nodes, -1);
+    for (int32_t n = 0; n < t.n_nodes; n++)
+      if (split[(size_t)g.node_at(gi[n], gj[n], gk[n])]) {
+        g.copy_of_node[n] = (int32_t)g.copy_node.size();
+        g.copy_node.push_back(n);
+        g.copy_site.push_back(g.node_at(gi[n], gj[n], gk[n]));
+      }
+    g.copy_mask.assign(g.copy_node.size(), 0);
+    g.fix_of_cell.assign((size_t)t.n_cells, -1);
+    for (int32_t c = 0; c < t.n_cells; c++) {
+      const int32_t *h = &t.hex[(size_t)c * 8];
+      bool fix = false;
+      for (int kb = 0; kb < 8; kb++) {
+        const int32_t cp = g.copy_of_node[h[kb]];
+        if (cp < 0) continue;
+        fix = true;
+        // the cell sits at (1-bx, 1-by, 1-bz) among the eight around its corner kb
+        g.copy_mask[(size_t)cp] |= (uint8_t)(1u << ((1 - bx[kb]) + 2 * (1 - by[kb]) + 4 * (1 - bz[kb])));
+      }
+      if (fix) {
+        g.fix_of_cell[c] = (int32_t)g.fix_cell.size();
+        g.fix_cell.push_back(c);
+      }
+    }
   }
   g.col_top.assign((size_t)nx * ny, 0);
   for (int32_t c = 0; c < t.n_cells; c++) {

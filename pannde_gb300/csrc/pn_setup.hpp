@@ -93,7 +93,7 @@ void build_source_entries(const MeshTables &t, const std::vector<pn_window_sourc
 
 // Voxel-grid view of a mesh: every node on the lattice x0 + i*hx (etc.),
 // every cell the axis-aligned box (i..i+1, j..j+1, k..k+1) with its corners
-// in the reference's corner order, no two nodes or cells on one lattice site.
+// in the reference's corner order, no two cells on one lattice site.
 // Lattice sites without a mesh node / cell are "void": their velocity and
 // stress stay zero, which is what a missing (-1) slot contributes in the
 // reference (RightHex.hpp:225-231).  Internal numbering is x fastest with
@@ -102,6 +102,13 @@ void build_source_entries(const MeshTables &t, const std::vector<pn_window_sourc
 //   grid node (i,j,k) -> (k*(ny+1) + j)*pnx + i,  pnx = (nx+1) rounded up to 4
 //   grid cell (i,j,k) -> (k*ny + j)*pcx + i,      pcx = nx rounded up to 16
 // Padding sites are void.
+// Several mesh nodes may share a lattice site: a crack modelled as
+// disconnected faces gives the cells on either side nodes of their own there.
+// Such a site is "split"; its first node lives in the lattice buffers, the
+// others ("extra copies") in a tail after the lattice sites, and every node of
+// a split site is a "copy" with the mask of the site's eight cells it joins
+// (bit a + 2b + 4c for cell (i-1+a, j-1+b, k-1+c)).  Cells with a corner on a
+// split site are "fix cells": the grid step's fix-up recomputes them.
 struct GridMap {
   bool ok = false;
   std::string why;               // reason when not a grid
@@ -110,12 +117,20 @@ struct GridMap {
   std::vector<int64_t> node_grid;  // mesh node -> grid node
   std::vector<int64_t> cell_grid;  // mesh cell -> grid cell
   std::vector<int32_t> col_top;    // [ny][nx] 1 + the highest solid cell layer of column (i, j), 0 if none
+  int64_t n_extra = 0;                // extra copies (tail slots node_sites() + e)
+  std::vector<int32_t> copy_node;     // mesh node of every copy (nodes of split sites), ascending
+  std::vector<int64_t> copy_site;     // [copies] lattice node index of the copy's site
+  std::vector<uint8_t> copy_mask;     // [copies] cells of the site the copy joins
+  std::vector<int32_t> copy_of_node;  // mesh node -> copy, or -1 (empty when no site is split)
+  std::vector<int32_t> fix_cell;      // mesh cells with a corner on a split site, ascending
+  std::vector<int32_t> fix_of_cell;   // mesh cell -> fix cell, or -1 (empty when no site is split)
   // lattice sites (the box, without padding)
   int64_t grid_nodes() const { return (int64_t)(nx + 1) * (ny + 1) * (nz + 1); }
   int64_t grid_cells() const { return (int64_t)nx * ny * nz; }
   // buffer lengths (with padding)
   int64_t node_sites() const { return (int64_t)pnx * (ny + 1) * (nz + 1); }
   int64_t cell_sites() const { return (int64_t)pcx * ny * nz; }
+  int64_t node_len() const { return node_sites() + n_extra; }  // node buffers: lattice + tail
   int64_t node_at(int64_t i, int64_t j, int64_t k) const { return (k * (ny + 1) + j) * pnx + i; }
   int64_t cell_at(int64_t i, int64_t j, int64_t k) const { return (k * ny + j) * pcx + i; }
   static int32_t node_pitch(int64_t nx) { return (int32_t)((nx + 1 + 3) / 4 * 4); }

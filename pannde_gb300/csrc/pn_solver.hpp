@@ -90,6 +90,19 @@ struct pn_solver {
   // and the force weights (the kernel's g is then 1); 1.0 when not folded
   double gfold = 1.0;
   int32_t *d_err = nullptr;  // device error word of the grid kernels
+  // split sites (grid.copy_node / fix_cell): the step's fix-up tables, rebuilt
+  // when sources or sensors change; host lists of the copies' forces and
+  // sensors and the fix cells' moments (per copy / fix cell, in order)
+  struct SplitForce { int32_t copy, dir, sig; double w; };
+  struct SplitSensor { int32_t copy, idx; };
+  struct FixMoment { int32_t fix, comp, sig; double w; };
+  std::vector<SplitForce> split_forces;
+  std::vector<SplitSensor> split_sensors;
+  std::vector<FixMoment> fix_moments;
+  pn::SplitCopy *d_copies = nullptr;
+  pn::FixCell *d_fix = nullptr;
+  int32_t *d_cf_dir = nullptr, *d_cf_sig = nullptr, *d_cs_idx = nullptr, *d_cm_comp = nullptr, *d_cm_sig = nullptr;
+  void *d_cf_w = nullptr, *d_cm_w = nullptr;
 
   // energy audit tables (pn_energy.cpp; built on the first call)
   double *d_emass = nullptr, *d_evol = nullptr, *d_ecomp = nullptr, *d_epart = nullptr;
@@ -265,6 +278,7 @@ void grid_sources(pn_solver *s);
 void grid_sensors(pn_solver *s, const std::vector<std::pair<int32_t, int32_t>> &sorted);
 void grid_run(pn_solver *s, int32_t nsteps);
 void grid_put_state(pn_solver *s, const double *const *V, const double *const *S);
+void grid_split_upload(pn_solver *s);  // the fix-up tables of split sites
 void grid_get_state(pn_solver *s, double *const *V, double *const *S);
 
 // algorithmic HBM bytes of one step in the solver's form

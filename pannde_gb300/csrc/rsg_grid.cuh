@@ -14,6 +14,21 @@
 
 namespace pn {
 
+// split lattice sites (rsg_split.cu): a copy is one mesh node of a site that
+// several nodes share; a fix cell is a cell with a corner on such a site
+struct SplitCopy {
+  int32_t i, j, k;    // the site
+  uint32_t mask;      // the site's cells (i-1+a, j-1+b, k-1+c) the copy joins: bit a + 2b + 4c
+  int64_t v;          // index of the copy in the node buffers (lattice site or tail slot)
+  int32_t f0, f1;     // its force entries [f0, f1)
+  int32_t s0, s1;     // its sensor entries [s0, s1)
+};
+struct FixCell {
+  int64_t cell;       // lattice cell
+  int64_t v[8];       // node-buffer index of each corner (reference corner order)
+  int32_t m0, m1;     // its moment entries [m0, m1)
+};
+
 template <typename T>
 struct GridArgs {
   int32_t nx, ny, nz;  // cells per axis
@@ -54,6 +69,17 @@ struct GridArgs {
                          // node layers above are void; the tensor-copy kernel stops
                          // there), or null: nz
   int32_t n_rows;        // rows of ctab (materials + the void row)
+  // split sites, redone after the step kernel by the fix-up (rsg_split.cu)
+  int32_t n_copies, n_fix;
+  const SplitCopy *copies;
+  const int32_t *cf_dir;  // copy forces: direction, signal, weight (as f_w)
+  const int32_t *cf_sig;
+  const T *cf_w;
+  const int32_t *cs_idx;  // copy sensors: sensor number
+  const FixCell *fix;
+  const int32_t *cm_comp;  // fix-cell moments: Voigt component, signal, weight (as m_w)
+  const int32_t *cm_sig;
+  const T *cm_w;
   int32_t test_skip_layer;  // failure-path test: the layer whose copies are never issued (kNoLayer: none)
 };
 
@@ -95,5 +121,17 @@ int grid_tma_blocks_per_sm(int precision);
 cudaError_t launch_grid_tma(const void *args /* GridArgs<storage type> */, int precision, int sym,
                             cudaStream_t st);
 cudaError_t launch_grid_tma_batch(const GridBatchLaunch &b, int precision, int step, cudaStream_t st);
+
+// fix-up of split sites after a step launch (rsg_split.cu): the copies'
+// velocities, then the fix cells' stresses, from the step's input buffers
+cudaError_t launch_grid_split(const void *args /* GridArgs<storage type> */, int precision, cudaStream_t st);
+struct GridSplitBatch {
+  int n_members;
+  const void *args;         // GridArgs<S>[n_members] (device)
+  const int *copy_start;    // [n_members + 1] prefix of n_copies
+  const int *fix_start;     // [n_members + 1] prefix of n_fix
+  int total_copies, total_fix;
+};
+cudaError_t launch_grid_split_batch(const GridSplitBatch &b, int precision, int step, cudaStream_t st);
 
 }  // namespace pn

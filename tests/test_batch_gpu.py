@@ -111,3 +111,22 @@ def test_tuned_shapes_and_graph_replay_keep_results(cuda_device, form):
     for s, r in zip(sv, ref):
         same((s.get_state(), s.traces(), s.time), r)
         s.close()
+
+
+@pytest.mark.parametrize("prec", ["f64", "df64", "f32"])
+def test_batch_cracked_brackets_grid(cuda_device, prec):
+    """Grid-form members with split lattice sites (cracks as disconnected
+    faces, one with a water column) beside a member without any: the batch's
+    fix-up of split sites gives every member the same bits as alone."""
+    cs = [cases.bracket_case(1000 + i, nsteps=30, water_column=(i == 0), scale=0.3) for i in range(3)]
+    cs.append(members()[0])
+    ref = [alone(c, prec, "grid", 30) for c in cs]
+    sv = [Solver.from_case(c, precision=prec, form="grid", capacity=30) for c in cs]
+    with Batch() as b:
+        for s in sv:
+            b.add(s)
+        b.solve(11)
+        b.solve(19)
+    for s, r in zip(sv, ref):
+        same((s.get_state(), s.traces(), s.time), r)
+        s.close()

@@ -112,6 +112,64 @@ def test_grid_slab_cracked_brackets(cuda_device, prec):
         compare(prec, dev, ref)
 
 
+def cracked_block(h=1e-4):
+    """A 24 x 14 x 10 voxel block (two materials) with a crack as
+    disconnected faces in the lattice plane z = 5, x in (5, 15), y in (3, 9):
+    the cells above it get nodes of their own there (split lattice sites)."""
+    solid = np.ones((24, 14, 10), dtype=bool)
+    m = cases.voxel_mesh(solid, h)
+    ni, nj, nk = m.node_ijk[:, 0], m.node_ijk[:, 1], m.node_ijk[:, 2]
+    on_face = (nk == 5) & (ni > 5) & (ni < 15) & (nj > 3) & (nj < 9)
+    above = np.flatnonzero(m.cell_ijk[:, 2] >= 5)
+    n0 = m.n_nodes
+    m = cases.disconnect_face(m, above, on_face)
+    assert m.n_nodes == n0 + int(on_face.sum())
+    mat = (m.cell_ijk[:, 0] >= 12).astype(np.int32)
+    cij = np.stack([cases.c21_from_6x6(cases.isotropic(70e9, 0.33)),
+                    cases.c21_from_6x6(cases.isotropic(200e9, 0.29))])
+    c = cases.Case("crack", m, np.array([2700.0, 7800.0]), cij, mat, 4e-9)
+    return c, np.flatnonzero(on_face), np.arange(n0, m.n_nodes)
+
+
+@pytest.mark.parametrize("h", [1e-4, (1e-4, 1.2e-4, 0.8e-4)], ids=["cubic", "graded"])
+@pytest.mark.parametrize("prec", PRECS)
+def test_grid_crack_as_disconnected_faces(cuda_device, prec, h):
+    """Split lattice sites: force windows on the crack plane (both faces'
+    nodes), a moment window beside it, sensors on both copies of crack nodes,
+    from a random state; cubic voxels (0.25/h folded into the coefficients)
+    and unequal spacings."""
+    c, lower, upper = cracked_block(h)
+    m = c.mesh
+    hx, hy, hz = (h, h, h) if np.isscalar(h) else h
+    t = np.linspace(0.0, 2e-7, 60)
+    v = np.sin(2e7 * t)
+    src = [cases.WindowSource(N.PN_SOURCE_FORCE, 0, 2, (10 * hx, 6 * hy, 5 * hz), 2.5 * hx, hz, t, v),
+           cases.WindowSource(N.PN_SOURCE_FORCE, 1, 0, (8 * hx, 5 * hy, 5 * hz), 2.0 * hx, hz, t, -v),
+           cases.WindowSource(N.PN_SOURCE_MOMENT, 2, 1, (14 * hx, 7 * hy, 4.5 * hz), 2.0 * hx, hz, t, v)]
+    V0, S0 = random_state(m, 31)
+    sens = np.sort(np.concatenate([lower[::7], upper[::5], [0, m.n_nodes // 2]])).astype(np.int32)
+    ref = oracle.run(m, c.material_fields(), c.dt, src, 25, sens, V0=V0, S0=S0)
+    with Solver(m, c, c.dt, prec, "grid") as s:
+        assert s.info()["form_name"] == "grid"
+    dev, t_end = run_grid(m, c, c.dt, src, 25, sens, prec, V0=V0, S0=S0, chunks=[9, 16])
+    assert t_end == ref["time"]
+    compare(prec, dev, ref)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_grid_cracked_brackets(cuda_device, prec):
+    """L-brackets with the crack as disconnected faces (with and without a
+    water column) take the grid form and match the oracle."""
+    for seed, wc in ((1003, False), (1006, True)):
+        c = cases.bracket_case(seed, nsteps=40, water_column=wc, scale=0.35)
+        with Solver.from_case(c, precision=prec) as s:
+            assert s.info()["form_name"] == "grid"
+        ref = oracle.run(c.mesh, c.material_fields(), c.dt, c.sources, c.nsteps, c.sensors)
+        dev, t = run_grid(c.mesh, c, c.dt, c.sources, c.nsteps, c.sensors, prec)
+        assert t == ref["time"]
+        compare(prec, dev, ref)
+
+
 @pytest.mark.parametrize("prec", PRECS)
 def test_grid_laminate_moments_and_forces(cuda_device, prec):
     c = cases.laminate_case(nx=33, ny=29, nz=8, nsteps=40, radius=0.5e-3, n_sensors=6)
