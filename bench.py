@@ -66,6 +66,8 @@ def parse():
     p.add_argument("--no-batch", action="store_true", help="skip the batched-brackets leg")
     p.add_argument("--batch-members", type=int, default=96)
     p.add_argument("--batch-sample-steps", type=int, default=300)
+    p.add_argument("--batch-form", default="auto", choices=["auto", "table", "grid"],
+                   help="device form of the batch members (auto: grid, the brackets are lattices)")
     p.add_argument("--no-serving", action="store_true", help="skip the serving leg")
     p.add_argument("--serving-requests", type=int, default=8)
     p.add_argument("--serving-rate", type=float, default=1.0, help="Poisson arrivals per second")
@@ -284,20 +286,23 @@ def e2e_run(case, prec, steps, torch):
     return (t1 - t0), h2d, d2h
 
 
-def batch_leg(n_members, sample_steps, torch, steps_total=3000):
+def batch_leg(n_members, sample_steps, torch, steps_total=3000, form="auto"):
     """Batched sims/hour: n_members seeded L-brackets (legs 60-220 cells, 12-30
     thick, 40-160 deep, 0.1 mm voxels, a 1-6 mm crack at the inner fillet as
     disconnected faces; every sixth with an acoustic-fluid column and a
     pressure source, the others a z-force transducer), FP32, 3000 steps each,
-    advanced together by pn_batch_solve (one launch per kernel per step for
-    all members).  A sample of the steps is timed with CUDA events on the
+    advanced together by pn_batch_solve.  The brackets are voxel lattices
+    whose cracks split lattice sites, so they take the grid form: one fused
+    launch per step for all members plus the two small fix-up launches of the
+    split sites (form="table": the connectivity-table kernels, two launches
+    per step).  A sample of the steps is timed with CUDA events on the
     batch's stream; the per-step cost does not change along the run."""
     from pannde_gb300 import cases
     from pannde_gb300.solver import Batch, Solver
     warm = 5
     t0 = time.perf_counter()
     cs = [cases.bracket_case(1000 + i, nsteps=steps_total, water_column=(i % 6 == 0)) for i in range(n_members)]
-    solvers = [Solver.from_case(c, precision="f32", capacity=warm + sample_steps) for c in cs]
+    solvers = [Solver.from_case(c, precision="f32", capacity=warm + sample_steps, form=form) for c in cs]
     setup_s = time.perf_counter() - t0
     cells = sum(c.mesh.n_cells for c in cs)
     forms = sorted({s.info()["form_name"] for s in solvers})
@@ -462,7 +467,7 @@ def main():
                            "how": "pn_solver_set_state from pinned host, one pn_solver_solve per step, "
                                   "pn_solver_get_traces + pn_solver_get_state to pinned host; wall clock"}
         if ws == 1 and not args.no_batch:
-            line["batch"] = batch_leg(args.batch_members, args.batch_sample_steps, torch)
+            line["batch"] = batch_leg(args.batch_members, args.batch_sample_steps, torch, form=args.batch_form)
         if ws == 1 and not args.no_serving:
             line["serving"] = serving_leg(args.serving_requests, args.serving_rate, torch)
         if ws == 1 and not args.no_cpu:
