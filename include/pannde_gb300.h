@@ -381,7 +381,7 @@ int pn_batch_solve(pn_batch *b, int32_t nsteps);
    can also stall every stream of the device while they run).
    pn_batch_solve stages the members' argument blocks in buffers it grows
    with cudaMalloc; this call stages them in one fixed 256 KiB device array
-   compiled into the library (room for about 350 grid-form or 550
+   compiled into the library (room for about 270 grid-form or 550
    table-form members), looked up with
    cudaGetSymbolAddress on the first call on each device -- make that first
    call before any stream capture starts on the device.  Batches whose

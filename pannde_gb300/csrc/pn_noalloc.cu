@@ -14,7 +14,7 @@
 namespace pn {
 namespace {
 
-// argument blocks + tile prefixes of one batch call (about 350 grid-form or
+// argument blocks + tile prefixes of one batch call (about 270 grid-form or
 // 550 table-form members)
 static __device__ __align__(256) unsigned char g_batch_scratch[kNoAllocScratchBytes];
 
