@@ -5,6 +5,9 @@
   ``"ascii"``, or ``"appended"`` raw bytes; ``compress=True`` writes
   vtkZLibDataCompressor blocks).
 * ``read_vtt``: tables (RowData columns, FieldData).
+* ``read_transducer_job`` / ``read_water_column_job``: the problem a
+  TransducerModel / WaterColumnModel runner builds from a job file, as a
+  ``cases.Case`` (mesh, per-cell materials, dt, excitation windows).
 * ``write_transducer_job``: a TransducerModel job for a ``cases.Case`` in the
   key names of PanNDE's StandardNames.hpp (density and C11..C66 CELL fields;
   FieldData dt, write_times, NTransducers, XD<i>/XCenter, YCenter, ZCenter,
@@ -98,7 +101,8 @@ def _decode(elem, info, appended):
     if fmt == "ascii":
         return np.array((elem.text or "").split(), dtype=np.float64).astype(dt)
     hs = 8 if info["header"] == "UInt64" else 4
-    hfmt = "<Q" if hs == 8 else "<I"
+    hc = "Q" if hs == 8 else "I"
+    hfmt = "<" + hc
     if fmt == "binary":
         text = "".join((elem.text or "").split())
         if info["zlib"]:
@@ -110,8 +114,7 @@ def _decode(elem, info, appended):
     data = appended[off:]
     if info["zlib"]:
         nb = struct.unpack(hfmt, data[:hs])[0]
-        bsz, last = struct.unpack(hfmt * 2, data[hs:3 * hs])
-        sizes = struct.unpack(hfmt * nb, data[3 * hs:(3 + nb) * hs])
+        sizes = struct.unpack("<" + hc * nb, data[3 * hs:(3 + nb) * hs])
         p = (3 + nb) * hs
         out = b""
         for s in sizes:
@@ -212,3 +215,57 @@ def write_water_column_job(path, case, write_times, **kw):
             fd[f"WC{i}/{key}"] = np.asarray(vals, dtype=np.float64)
     pts = np.stack([m.x, m.y, m.z], axis=1)
     write_vtu(path, pts, m.hexes, cell_data=cell, field_data=fd, **kw)
+
+
+def _job_base(path):
+    """Mesh, materials (the cells' density and C11..C66, one row per distinct
+    cell) and FieldData of a job file."""
+    from . import cases
+    d = read_vtu(path)
+    pts, hexes = d["points"], d["hexes"].astype(np.int32)
+    mesh = cases.HexMesh(pts[:, 0].copy(), pts[:, 1].copy(), pts[:, 2].copy(), hexes)
+    cd = d["cell_data"]
+    rows = np.stack([np.asarray(cd["density"], np.float64)] +
+                    [np.asarray(cd[k], np.float64) for k in CIJ_NAMES], axis=1)
+    uniq, cell_mat = np.unique(rows, axis=0, return_inverse=True)
+    fd = d["field_data"]
+    # window thickness: |z(corner 0) - z(corner 6)| of cell 0 (Boss.hpp:530-536, 650-658)
+    ds = abs(float(mesh.z[hexes[0, 0]]) - float(mesh.z[hexes[0, 6]]))
+    return mesh, uniq[:, 0].copy(), uniq[:, 1:].copy(), cell_mat.reshape(-1).astype(np.int32), fd, ds
+
+
+def read_transducer_job(path, sensors=None, nsteps=0):
+    """The problem TransducerModel builds from a job: each XD<i> a z-force
+    window (HostNormalXDZ: centre, Radius, the thickness of cell 0) with its
+    SignalTimes / SignalValues (Boss.hpp:496-524)."""
+    from . import _native as N
+    from . import cases
+    mesh, rho, cij, cell_mat, fd, ds = _job_base(path)
+    src = []
+    for i in range(int(fd["NTransducers"][0])):
+        center = tuple(float(fd[f"XD{i}/{a}Center"][0]) for a in "XYZ")
+        src.append(cases.WindowSource(N.PN_SOURCE_FORCE, i, 2, center, float(fd[f"XD{i}/Radius"][0]), ds,
+                                      np.asarray(fd[f"XD{i}/SignalTimes"], np.float64),
+                                      np.asarray(fd[f"XD{i}/SignalValues"], np.float64)))
+    sens = np.zeros(0, np.int32) if sensors is None else np.asarray(sensors, np.int32)
+    return cases.Case(str(path), mesh, rho, cij, cell_mat, float(fd["dt"][0]), src, sens, nsteps,
+                      dict(write_times=np.asarray(fd["write_times"], np.float64)))
+
+
+def read_water_column_job(path, sensors=None, nsteps=0):
+    """The problem WaterColumnModel builds from a job: each WC<i> three
+    moment windows (xx, yy, zz: SignalSigmaXX / YY / ZZ over SignalTimes) at
+    one centre and radius, thickness of cell 0 (Boss.hpp:580-660)."""
+    from . import _native as N
+    from . import cases
+    mesh, rho, cij, cell_mat, fd, ds = _job_base(path)
+    src = []
+    for i in range(int(fd["NWaterColumns"][0])):
+        center = tuple(float(fd[f"WC{i}/{a}Center"][0]) for a in "XYZ")
+        t = np.asarray(fd[f"WC{i}/SignalTimes"], np.float64)
+        for comp, key in ((0, "SignalSigmaXX"), (1, "SignalSigmaYY"), (2, "SignalSigmaZZ")):
+            src.append(cases.WindowSource(N.PN_SOURCE_MOMENT, i, comp, center, float(fd[f"WC{i}/Radius"][0]), ds,
+                                          t, np.asarray(fd[f"WC{i}/{key}"], np.float64)))
+    sens = np.zeros(0, np.int32) if sensors is None else np.asarray(sensors, np.int32)
+    return cases.Case(str(path), mesh, rho, cij, cell_mat, float(fd["dt"][0]), src, sens, nsteps,
+                      dict(write_times=np.asarray(fd["write_times"], np.float64)))

@@ -127,3 +127,36 @@ def test_standin_gateway_reads_and_writes(tmp_path):
     assert sol["field_data"]["time"][0] == 1.5e-6
     tab = vtu.read_vtt(tmp_path / "sol_table_3.vtt")
     assert np.array_equal(tab["columns"]["write_times"], fdata["write_times"])
+
+
+def same_problem(a, b):
+    """Two cases describe the same solve: mesh, every cell's density and
+    stiffness, dt and the excitation windows with their signals."""
+    assert np.array_equal(a.mesh.x, b.mesh.x) and np.array_equal(a.mesh.y, b.mesh.y)
+    assert np.array_equal(a.mesh.z, b.mesh.z) and np.array_equal(a.mesh.hexes, b.mesh.hexes)
+    assert np.array_equal(a.density[a.cell_material], b.density[b.cell_material])
+    assert np.array_equal(a.cij[a.cell_material], b.cij[b.cell_material])
+    assert a.dt == b.dt and len(a.sources) == len(b.sources)
+    key = lambda s: (s.kind, s.group, s.component)
+    for s, t in zip(sorted(a.sources, key=key), sorted(b.sources, key=key)):
+        assert (s.kind, s.component, tuple(s.center), s.radius, s.ds) == \
+               (t.kind, t.component, tuple(t.center), t.radius, t.ds)
+        assert np.array_equal(s.times, t.times) and np.array_equal(s.values, t.values)
+
+
+@pytest.mark.parametrize("encoding,compress", [("binary", False), ("appended", True)])
+def test_transducer_job_reads_back_the_problem(tmp_path, encoding, compress):
+    c = cases.laminate_case(nx=12, ny=10, nz=8, nsteps=20, radius=0.2e-3, n_sensors=4)
+    f = tmp_path / "lam.vtu"
+    vtu.write_transducer_job(f, c, [5 * c.dt, 10 * c.dt], encoding=encoding, compress=compress)
+    r = vtu.read_transducer_job(f, sensors=c.sensors, nsteps=c.nsteps)
+    same_problem(c, r)
+    assert np.array_equal(r.meta["write_times"], [5 * c.dt, 10 * c.dt])
+
+
+@pytest.mark.parametrize("encoding,compress", [("binary", False), ("appended", True)])
+def test_water_column_job_reads_back_the_problem(tmp_path, encoding, compress):
+    c = cases.bracket_case(5, water_column=True, scale=0.12, nsteps=20)
+    f = tmp_path / "wc.vtu"
+    vtu.write_water_column_job(f, c, [5 * c.dt], encoding=encoding, compress=compress)
+    same_problem(c, vtu.read_water_column_job(f, sensors=c.sensors, nsteps=c.nsteps))
