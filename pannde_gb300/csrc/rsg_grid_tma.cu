@@ -43,8 +43,6 @@ namespace {
 constexpr int TX = 32, TY = 8, NT = TX * TY;
 constexpr int KC_MAX = kGridChunkMax;  // cell layers per chunk (source-range staging)
 constexpr int ROWS_MAX = kGridTmaRowsMax;
-constexpr int NMSLOT = 4;  // material slots: read two layers after their copy
-constexpr int NVSLOT = 2;  // velocity + dt/rho slots: read in the layer's own iteration
 
 struct GridMaps {
   CUtensorMap S[6];
@@ -53,15 +51,21 @@ struct GridMaps {
   CUtensorMap mat;
 };
 
-// shared-memory geometry for a storage element of ESZ bytes.  The stress ring
-// holds NS layers: with 4 the stress half reads a cell's old stress from the
-// tile copied two layers before (4-byte storage, latency-bound); with 2 it
-// reads it from global memory (L2), which leaves room for a third block per SM
-// with 8-byte storage.
+// shared-memory geometry for a storage element of ESZ bytes.  Copies run PD
+// layers ahead of the layer being computed.  A layer's stress tile is read in
+// its own iteration (velocity half) and, with OWN_SMEM, two iterations later
+// (a cell's old stress in the stress half; without it that value comes from
+// global memory, mostly L2, which needs fewer slots: the room for a third
+// block per SM with 8-byte storage).  Slots per ring: stress PD + 1 (+ 2 with
+// OWN_SMEM), velocity + dt/rho PD + 1, material PD + 3 (read in the stress
+// half, two iterations after its layer's).
 template <int ESZ>
 struct Geo {
-  static constexpr int NS = ESZ == 4 ? 4 : 2;
-  static constexpr bool OWN_SMEM = NS == 4;
+  static constexpr int PD = 1;
+  static constexpr bool OWN_SMEM = ESZ == 4;
+  static constexpr int NS = PD + 1 + (OWN_SMEM ? 2 : 0);
+  static constexpr int NV = PD + 1;
+  static constexpr int NM = PD + 3;
   static constexpr int A = 16 / ESZ;              // x alignment of a copy (elements)
   static constexpr int BWC = ESZ == 4 ? 36 : 34;  // cell tile width: offset (< A) + 33
   static constexpr int BWN = ESZ == 4 ? 36 : 34;  // node tile width: offset (< A) + 32
@@ -74,9 +78,9 @@ struct Geo {
   static constexpr int SLOT = 6 * SBOX;                        // S[6] of one layer
   static constexpr int VSLOT = 4 * VBOX;                       // V[3], dt/rho of one layer
   static constexpr uint32_t TX_BYTES = 6 * SBOX_BYTES + 4 * VBOX + MBOX_BYTES;
-  static constexpr int OFF_V = NS * SLOT;                      // velocity ring [NVSLOT]
-  static constexpr int OFF_M = OFF_V + NVSLOT * VSLOT;         // material ring [NMSLOT]
-  static constexpr int OFF_VT = OFF_M + NMSLOT * MBOX;         // computed velocity [2][3][NT]
+  static constexpr int OFF_V = NS * SLOT;                      // velocity ring [NV]
+  static constexpr int OFF_M = OFF_V + NV * VSLOT;             // material ring [NM]
+  static constexpr int OFF_VT = OFF_M + NM * MBOX;             // computed velocity [2][3][NT]
   static constexpr int OFF_C = OFF_VT + 2 * 3 * NT * ESZ;      // dt*C rows [ROWS_MAX][36]
   static constexpr int OFF_R = OFF_C + ROWS_MAX * 36 * ESZ;    // ranges f, s [KC_MAX+2], m [KC_MAX]
   static constexpr int OFF_B = OFF_R + (3 * KC_MAX + 4) * 8;   // mbarriers [NS]
@@ -84,7 +88,6 @@ struct Geo {
   static constexpr size_t SMEM = BYTES + 128;                  // + base alignment
   static_assert(SLOT % 128 == 0 && VBOX % 128 == 0 && OFF_V % 128 == 0 && OFF_M % 128 == 0 && OFF_B % 8 == 0,
                 "alignment");
-  static_assert(NS % NVSLOT == 0 && NMSLOT % NS == 0, "slot counts");
   static_assert(SBOX % ESZ == 0 && VBOX % ESZ == 0, "element size");
 };
 
@@ -229,11 +232,11 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
   const int xs_m = floor_to(i0, 16), om = i0 - xs_m;
 
   // layer L is copy number u = L - k0 + 1 of the block: stress slot and
-  // mbarrier u % NS (phase (u / NS) & 1), velocity slot u % 2, material slot u % 4
+  // mbarrier u % NS (phase (u / NS) & 1), velocity slot u % NV, material slot u % NM
   auto ucount = [&](int L) { return (uint32_t)(L - k0 + 1); };
   auto sslot = [&](int L) { return base + (ucount(L) % G::NS) * G::SLOT; };
-  auto vslot = [&](int L) { return base + G::OFF_V + (ucount(L) % NVSLOT) * G::VSLOT; };
-  auto mslot = [&](int L) { return base + G::OFF_M + (ucount(L) % NMSLOT) * G::MBOX; };
+  auto vslot = [&](int L) { return base + G::OFF_V + (ucount(L) % G::NV) * G::VSLOT; };
+  auto mslot = [&](int L) { return base + G::OFF_M + (ucount(L) % G::NM) * G::MBOX; };
   auto bar_of = [&](int L) { return bars + 8u * (ucount(L) % G::NS); };
   auto parity = [&](int L) { return (ucount(L) / G::NS) & 1u; };
   auto issue = [&](int L) {  // thread 0: copies of layer L
@@ -272,8 +275,9 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
   for (int q = t; q < k1 - k0; q += NT) sRm[q] = a.m_rng ? a.m_rng[(int64_t)blk * nz + k0 + q] : make_int2(0, 0);
   __syncthreads();
   if (t == 0) {
-    issue(k0 - 1);
-    issue(k0);
+#pragma unroll
+    for (int d = 0; d <= G::PD; d++)
+      if (k0 - 1 + d <= k1) issue(k0 - 1 + d);
   }
 
   R vpx0 = R(), vpx4 = R(), vpx5 = R(), vpy1 = R(), vpy3 = R(), vpy5 = R(), vs2 = R(), vs3 = R(),
@@ -287,9 +291,9 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
   bool fail = false;
 
   for (int k = k0 - 1; k <= k1 + 1; k++) {
-    if (t == 0 && k >= k0 && k + 1 <= k1) {
+    if (t == 0 && k >= k0 && k + G::PD <= k1) {
       proxy_fence_async_smem();
-      issue(k + 1);
+      issue(k + G::PD);
     }
     // ---- B: velocity of node layer k
     if (k <= k1) {
@@ -443,7 +447,7 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
       // give up: record, drain this block's copies in flight, return
       if (t == 0) {
         if (a.err) atomicExch(a.err, kErrWait);
-        const int issued = min(k1, max(k + 1, k0));
+        const int issued = min(k1, max(k + G::PD, k0 - 1 + G::PD));
         for (int L = waited + 1; L <= issued; L++) (void)mbar_wait(bar_of(L), parity(L));
       }
       return;
