@@ -184,6 +184,23 @@ def dist_setup():
 FORM = "auto"
 
 
+def reduce_max(value, dist, torch):
+    """The largest value over all ranks (every rank calls it: the max-over-ranks
+    time of a step range); the value itself in a single process."""
+    if not dist:
+        return value
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, seconds, ws):
+    """Whole-job throughput: each of ws ranks processed units_per_rank, the
+    slowest in `seconds` (weak scaling: independent replicas)."""
+    return ws * units_per_rank / seconds
+
+
 def time_device(case, prec, steps, warmup, torch, dist):
     """Device throughput of the hot path with inputs resident in HBM."""
     from pannde_gb300.solver import Solver
@@ -202,13 +219,9 @@ def time_device(case, prec, steps, warmup, torch, dist):
     s.solve(steps)
     e1.record(stream)
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
+    ms = reduce_max(e0.elapsed_time(e1), dist, torch)
     kt = s.kernel_times()
     info = s.info()
-    if dist:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
     s.close()
     return ms, kt, info
 
@@ -253,8 +266,10 @@ def roofline(case, info, kt, prec, peak, peak_kind):
     return out
 
 
-def e2e_run(case, prec, steps, torch):
-    """Through the C ABI with host buffers (pinned), copies inside the timed region."""
+def e2e_run(case, prec, steps, torch, dist=None):
+    """Through the C ABI with host buffers (pinned), copies inside the timed
+    region; every rank runs it, started together, and the slowest rank's time
+    counts."""
     from pannde_gb300.solver import Solver
     s = Solver.from_case(case, precision=prec, capacity=steps, form=FORM)
     nn, nc = case.mesh.n_nodes, case.mesh.n_cells
@@ -272,6 +287,8 @@ def e2e_run(case, prec, steps, torch):
     s.synchronize()
     s.clear_traces()
     torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
     t0 = time.perf_counter()
     s.set_state(V0, S0)
     for _ in range(steps):
@@ -283,7 +300,7 @@ def e2e_run(case, prec, steps, torch):
     h2d = (3 * nn + 6 * nc) * 8 + sig_rows * len(case.sources) * 8
     d2h = (3 * nn + 6 * nc) * 8 + tr.size * 8
     s.close()
-    return (t1 - t0), h2d, d2h
+    return reduce_max(t1 - t0, dist, torch), h2d, d2h
 
 
 def batch_leg(n_members, sample_steps, torch, steps_total=3000, form="auto"):
@@ -396,6 +413,8 @@ def main():
     global FORM
     FORM = args.form
     ws, rank, local = dist_setup()
+    if args.impl == "reference" and rank != 0:
+        return 0  # the CPU reference arm runs on rank 0 alone
     assert args.warmup >= 3 or args.impl == "reference", "at least 3 warm-up steps"
     case, desc = make_case(args.case, args.nx, args.ny, args.nz)
     precs = [p for p in args.precisions.split(",") if p]
@@ -403,8 +422,6 @@ def main():
         precs = [p for p in precs if p != "f32"]
 
     if args.impl == "reference":
-        if rank != 0:
-            return 0
         cb = cpu_reference(case, args.cpu_seconds)
         line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT,
                 "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -436,7 +453,7 @@ def main():
         ms, kt, info = time_device(case, head, args.steps, args.warmup, torch, dist)
     clocks = clk.summary()
     cells = info["n_cells"]
-    value = ws * cells * args.steps / (ms * 1e-3) / 1e9
+    value = whole_job_rate(cells * args.steps, ms * 1e-3, ws) / 1e9
     line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -452,20 +469,21 @@ def main():
     forms = {}
     for prec in precs[1:]:
         msp, ktp, infop = time_device(case, prec, args.steps, args.warmup, torch, dist)
-        vp = ws * cells * args.steps / (msp * 1e-3) / 1e9
+        vp = whole_job_rate(cells * args.steps, msp * 1e-3, ws) / 1e9
         forms[prec] = {"value": round(vp, 4), "unit": UNIT, "dtype": DTYPES[prec],
                        "ms_per_step": round(msp / args.steps, 4),
                        "roofline": roofline(args.case, infop, ktp, prec, peak, peak_kind)}
     if forms:
         line["other_forms"] = forms
+    if not args.no_e2e:  # every rank: the slowest rank's wall time counts
+        secs, h2d, d2h = e2e_run(case, head, args.steps, torch, dist)
+        line["e2e"] = {"value": round(whole_job_rate(cells * args.steps, secs, ws) / 1e9, 4), "unit": UNIT,
+                       "h2d_bytes_per_step": int(ws * h2d / args.steps),
+                       "d2h_bytes_per_step": int(ws * d2h / args.steps),
+                       "how": "pn_solver_set_state from pinned host, one pn_solver_solve per step, "
+                              "pn_solver_get_traces + pn_solver_get_state to pinned host; wall clock, "
+                              "max over ranks; bytes summed over ranks"}
     if rank == 0:
-        if not args.no_e2e:
-            secs, h2d, d2h = e2e_run(case, head, args.steps, torch)
-            line["e2e"] = {"value": round(cells * args.steps / secs / 1e9 * ws, 4), "unit": UNIT,
-                           "h2d_bytes_per_step": int(h2d / args.steps),
-                           "d2h_bytes_per_step": int(d2h / args.steps),
-                           "how": "pn_solver_set_state from pinned host, one pn_solver_solve per step, "
-                                  "pn_solver_get_traces + pn_solver_get_state to pinned host; wall clock"}
         if ws == 1 and not args.no_batch:
             line["batch"] = batch_leg(args.batch_members, args.batch_sample_steps, torch, form=args.batch_form)
         if ws == 1 and not args.no_serving:
