@@ -112,15 +112,21 @@ def test_grid_slab_cracked_brackets(cuda_device, prec):
         compare(prec, dev, ref)
 
 
-def cracked_block(h=1e-4):
+def cracked_block(h=1e-4, axis=2):
     """A 24 x 14 x 10 voxel block (two materials) with a crack as
-    disconnected faces in the lattice plane z = 5, x in (5, 15), y in (3, 9):
-    the cells above it get nodes of their own there (split lattice sites)."""
+    disconnected faces in a lattice plane normal to `axis` (z = 5, x in
+    (5, 15), y in (3, 9); x = 12 or y = 7 likewise): the cells on its upper
+    side get nodes of their own there (split lattice sites)."""
     solid = np.ones((24, 14, 10), dtype=bool)
     m = cases.voxel_mesh(solid, h)
     ni, nj, nk = m.node_ijk[:, 0], m.node_ijk[:, 1], m.node_ijk[:, 2]
-    on_face = (nk == 5) & (ni > 5) & (ni < 15) & (nj > 3) & (nj < 9)
-    above = np.flatnonzero(m.cell_ijk[:, 2] >= 5)
+    if axis == 2:
+        on_face = (nk == 5) & (ni > 5) & (ni < 15) & (nj > 3) & (nj < 9)
+    elif axis == 0:
+        on_face = (ni == 12) & (nj > 3) & (nj < 9) & (nk > 2) & (nk < 8)
+    else:
+        on_face = (nj == 7) & (ni > 5) & (ni < 15) & (nk > 2) & (nk < 8)
+    above = np.flatnonzero(m.cell_ijk[:, axis] >= (12, 7, 5)[axis])
     n0 = m.n_nodes
     m = cases.disconnect_face(m, above, on_face)
     assert m.n_nodes == n0 + int(on_face.sum())
@@ -131,14 +137,15 @@ def cracked_block(h=1e-4):
     return c, np.flatnonzero(on_face), np.arange(n0, m.n_nodes)
 
 
-@pytest.mark.parametrize("h", [1e-4, (1e-4, 1.2e-4, 0.8e-4)], ids=["cubic", "graded"])
+@pytest.mark.parametrize("h,axis", [(1e-4, 2), ((1e-4, 1.2e-4, 0.8e-4), 2), (1e-4, 0), (1e-4, 1)],
+                         ids=["z-cubic", "z-graded", "x-cubic", "y-cubic"])
 @pytest.mark.parametrize("prec", PRECS)
-def test_grid_crack_as_disconnected_faces(cuda_device, prec, h):
+def test_grid_crack_as_disconnected_faces(cuda_device, prec, h, axis):
     """Split lattice sites: force windows on the crack plane (both faces'
     nodes), a moment window beside it, sensors on both copies of crack nodes,
     from a random state; cubic voxels (0.25/h folded into the coefficients)
     and unequal spacings."""
-    c, lower, upper = cracked_block(h)
+    c, lower, upper = cracked_block(h, axis)
     m = c.mesh
     hx, hy, hz = (h, h, h) if np.isscalar(h) else h
     t = np.linspace(0.0, 2e-7, 60)
