@@ -483,6 +483,14 @@ void grid_args(pn_solver *s, GridArgs<T> &a) {
   a.err = s->d_err;
   a.ktop = s->d_ktop;
   a.n_rows = s->mat.n_mat + 1;
+  a.ortho_rows = 0;
+  for (int32_t r = 0; r <= s->mat.n_mat && r < 32; r++) {  // the last row: void (zero)
+    bool ortho = true;
+    for (int k = 0; k < 6 && ortho && r < s->mat.n_mat; k++)
+      for (int j = 0; j < 6; j++)
+        if (!((k < 3 && j < 3) || k == j) && s->mat.c36[(size_t)r * 36 + k * 6 + j] != 0.0) ortho = false;
+    if (ortho) a.ortho_rows |= 1u << r;
+  }
   a.n_copies = (int32_t)g.copy_node.size();
   a.n_fix = (int32_t)g.fix_cell.size();
   a.copies = s->d_copies;

@@ -69,6 +69,7 @@ struct GridArgs {
                          // node layers above are void; the tensor-copy kernel stops
                          // there), or null: nz
   int32_t n_rows;        // rows of ctab (materials + the void row)
+  uint32_t ortho_rows;   // bit r: row r is orthotropic (tensor-copy kernel, rows < 32)
   // split sites, redone after the step kernel by the fix-up (rsg_split.cu)
   int32_t n_copies, n_fix;
   const SplitCopy *copies;

@@ -32,6 +32,7 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 
 #include "df64.cuh"
 #include "rsg_common.cuh"
@@ -428,12 +429,29 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
           for (int f = 0; f < 6; f++)
             if (f == kk) acc[f] = madd(w, sg, acc[f]);
         }
+        // FP64 (bound by the FP64 pipe): when every active lane's row is
+        // orthotropic (C11..C33 block and the shear diagonal only: a laminate's
+        // 0/90 plies beside its +-45 ones), the 12-term product; the others are
+        // zero.  (The FP32-pipe forms measured no gain or a loss from the vote.)
+        bool ortho = (SYM & 3) == 2;
+        if constexpr ((SYM & 3) != 2 && std::is_same<R, double>::value)
+          ortho = __all_sync(__activemask(), (a.ortho_rows >> row) & 1u);
+        if (ortho) {
 #pragma unroll
-        for (int kk = 0; kk < 6; kk++) {
+          for (int kk = 0; kk < 6; kk++) {
 #pragma unroll
-          for (int jj = 0; jj < 6; jj++)
-            if (c_used(SYM & 3, kk, jj)) acc[kk] = madd(N::val(Cm[6 * kk + jj]), e[jj], acc[kk]);
-          N::st(a.S_out[kk], cg, acc[kk]);
+            for (int jj = 0; jj < 6; jj++)
+              if (c_used(2, kk, jj)) acc[kk] = madd(N::val(Cm[6 * kk + jj]), e[jj], acc[kk]);
+            N::st(a.S_out[kk], cg, acc[kk]);
+          }
+        } else {
+#pragma unroll
+          for (int kk = 0; kk < 6; kk++) {
+#pragma unroll
+            for (int jj = 0; jj < 6; jj++)
+              if (c_used(SYM & 3, kk, jj)) acc[kk] = madd(N::val(Cm[6 * kk + jj]), e[jj], acc[kk]);
+            N::st(a.S_out[kk], cg, acc[kk]);
+          }
         }
       }
 #pragma unroll
