@@ -262,13 +262,18 @@ int pn_solver_set_state(pn_solver *s, const double *const *V, const double *cons
   return guarded([&]() -> int {
     if (!s) return set_err(PN_ERR_INVALID, "null solver");
     const int32_t nn = s->mesh.n_nodes, nc = s->mesh.n_cells;
+    pn::ck(cudaStreamSynchronize(s->stream), "set_state sync");
+    if (s->form == PN_FORM_GRID) {  // checked on the device while it is written to the idle buffer half
+      const int bad = pn::grid_put_state(s, V, S);
+      if (bad & 1) return set_err(PN_ERR_NOT_FINITE, "non-finite velocity");
+      if (bad & 2) return set_err(PN_ERR_NOT_FINITE, "non-finite stress");
+      return PN_OK;
+    }
     for (int k = 0; k < 3; k++)
       if (V && V[k] && !pn::all_finite(V[k], nn)) return set_err(PN_ERR_NOT_FINITE, "non-finite velocity");
     for (int k = 0; k < 6; k++)
       if (S && S[k] && !pn::all_finite(S[k], nc)) return set_err(PN_ERR_NOT_FINITE, "non-finite stress");
-    pn::ck(cudaStreamSynchronize(s->stream), "set_state sync");
-    if (s->form == PN_FORM_GRID) pn::grid_put_state(s, V, S);
-    else pn::table_put_state(s, V, S);
+    pn::table_put_state(s, V, S);
     pn::ck(cudaStreamSynchronize(s->stream), "set_state");
     return PN_OK;
   });

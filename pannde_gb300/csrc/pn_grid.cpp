@@ -324,20 +324,31 @@ static void ensure_grid_maps(pn_solver *s) {
   }
 }
 
-// The lattice buffers are cleared (void sites stay zero) and the caller's
-// fields scattered to their lattice positions on the device (rsg_state.cu).
-void grid_put_state(pn_solver *s, const double *const *V, const double *const *S) {
+// The idle half of the double buffer is cleared (void sites stay zero) and
+// the caller's fields scattered to their lattice positions on the device
+// (rsg_state.cu), which also checks them for NaN and infinity; the solver
+// switches to that half only when every value is finite.
+int grid_put_state(pn_solver *s, const double *const *V, const double *const *S) {
   const GridMap &g = s->grid;
   const int64_t gn = g.node_len(), gc = g.cell_sites();
+  const int b = s->cur ^ 1;
   ensure_grid_maps(s);
+  if (!s->d_nonfinite) s->d_nonfinite = s->alloc<int32_t>(2 * sizeof(int32_t));
+  ck(cudaMemsetAsync(s->d_nonfinite, 0, 2 * sizeof(int32_t), s->stream), "memset");
   for (int k = 0; k < 3; k++) {
-    ck(cudaMemsetAsync(s->V[s->cur][k], 0, (size_t)gn * s->esz, s->stream), "memset");
-    if (V && V[k]) s->put_field(s->V[s->cur][k], V[k], (size_t)s->mesh.n_nodes, s->d_nmap);
+    ck(cudaMemsetAsync(s->V[b][k], 0, (size_t)gn * s->esz, s->stream), "memset");
+    if (V && V[k]) s->put_field(s->V[b][k], V[k], (size_t)s->mesh.n_nodes, s->d_nmap, s->d_nonfinite);
   }
   for (int k = 0; k < 6; k++) {
-    ck(cudaMemsetAsync(s->S[s->cur][k], 0, (size_t)gc * s->esz, s->stream), "memset");
-    if (S && S[k]) s->put_field(s->S[s->cur][k], S[k], (size_t)s->mesh.n_cells, s->d_cmap);
+    ck(cudaMemsetAsync(s->S[b][k], 0, (size_t)gc * s->esz, s->stream), "memset");
+    if (S && S[k]) s->put_field(s->S[b][k], S[k], (size_t)s->mesh.n_cells, s->d_cmap, s->d_nonfinite + 1);
   }
+  int32_t bad[2] = {0, 0};
+  ck(cudaMemcpyAsync(bad, s->d_nonfinite, sizeof(bad), cudaMemcpyDeviceToHost, s->stream), "finite check");
+  ck(cudaStreamSynchronize(s->stream), "set_state");
+  if (bad[0] || bad[1]) return (bad[0] ? 1 : 0) | (bad[1] ? 2 : 0);
+  s->cur = b;
+  return 0;
 }
 
 void grid_get_state(pn_solver *s, double *const *V, double *const *S) {

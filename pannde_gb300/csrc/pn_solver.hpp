@@ -90,6 +90,7 @@ struct pn_solver {
   // and the force weights (the kernel's g is then 1); 1.0 when not folded
   double gfold = 1.0;
   int32_t *d_err = nullptr;  // device error word of the grid kernels
+  int32_t *d_nonfinite = nullptr;  // [2] set_state's NaN / infinity flags (velocity, stress)
   // split sites (grid.copy_node / fix_cell): the step's fix-up tables, rebuilt
   // when sources or sensors change; host lists of the copies' forces and
   // sensors and the fix cells' moments (per copy / fix cell, in order)
@@ -219,16 +220,39 @@ struct pn_solver {
     if (!d_stage) d_stage = alloc<double>(8 * (size_t)std::max(mesh.n_nodes, mesh.n_cells));
     return d_stage;
   }
-  // host FP64 field[n] -> dst[map[i]] in the storage type (map null: dst[i])
-  void put_field(void *dst, const double *host, size_t n, const int64_t *map) {
+  // The device's address of a caller buffer in page-locked, mapped host
+  // memory (cudaHostAlloc / cudaHostRegister): the conversion kernels then
+  // read or write it directly over the CPU-GPU link, without the staging
+  // copy.  Null for any other memory (staged through device memory).  The
+  // calls that use it wait for the stream before returning.
+  static void *device_view(const void *host) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+  }
+  // host FP64 field[n] -> dst[map[i]] in the storage type (map null: dst[i]);
+  // *nonfinite (device, when given) becomes 1 if a value is NaN or infinite
+  void put_field(void *dst, const double *host, size_t n, const int64_t *map, int32_t *nonfinite = nullptr) {
     if (n == 0) return;
+    if (const void *dv = device_view(host)) {
+      pn::ck(pn::launch_state_store(precision, (const double *)dv, (int64_t)n, map, dst, stream, nonfinite),
+             "put_field kernel");
+      return;
+    }
     double *st = stage();
     pn::ck(cudaMemcpyAsync(st, host, n * 8, cudaMemcpyHostToDevice, stream), "put_field copy");
-    pn::ck(pn::launch_state_store(precision, st, (int64_t)n, map, dst, stream), "put_field kernel");
+    pn::ck(pn::launch_state_store(precision, st, (int64_t)n, map, dst, stream, nonfinite), "put_field kernel");
   }
   // src[map[i]] (or src[i]) in the storage type -> host FP64 field[n]
   void get_field(double *host, const void *src, size_t n, const int64_t *map) {
     if (n == 0 || !host) return;
+    if (void *dv = device_view(host)) {
+      pn::ck(pn::launch_state_load(precision, src, (int64_t)n, map, (double *)dv, stream), "get_field kernel");
+      return;
+    }
     double *st = stage();
     pn::ck(pn::launch_state_load(precision, src, (int64_t)n, map, st, stream), "get_field kernel");
     pn::ck(cudaMemcpyAsync(host, st, n * 8, cudaMemcpyDeviceToHost, stream), "get_field copy");
@@ -277,7 +301,10 @@ void grid_create(pn_solver *s);
 void grid_sources(pn_solver *s);
 void grid_sensors(pn_solver *s, const std::vector<std::pair<int32_t, int32_t>> &sorted);
 void grid_run(pn_solver *s, int32_t nsteps);
-void grid_put_state(pn_solver *s, const double *const *V, const double *const *S);
+// writes the idle half of the double buffer and swaps to it unless a value
+// is NaN or infinite: returns 0, or bit 1 (velocity) / bit 2 (stress) with the
+// state left as it was
+int grid_put_state(pn_solver *s, const double *const *V, const double *const *S);
 void grid_split_upload(pn_solver *s);  // the fix-up tables of split sites
 void grid_get_state(pn_solver *s, double *const *V, double *const *S);
 

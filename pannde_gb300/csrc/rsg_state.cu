@@ -38,12 +38,17 @@ template <> __device__ __forceinline__ double cvt_out<float2>(float2 v) {
 template <typename R>
 __global__ void __launch_bounds__(256) k_state_store(const double *__restrict__ src, int64_t n,
                                                      const int64_t *__restrict__ map,
-                                                     R *__restrict__ dst) {
+                                                     R *__restrict__ dst, int32_t *nonfinite) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  bool bad = false;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     const int64_t j = map ? __ldg(map + i) : i;
-    dst[j] = cvt_in<R>(__ldg(src + i));
+    const double v = __ldg(src + i);
+    // NaN or infinity: every exponent bit set
+    bad = bad || (__double_as_longlong(v) & 0x7ff0000000000000LL) == 0x7ff0000000000000LL;
+    dst[j] = cvt_in<R>(v);
   }
+  if (bad && nonfinite) *nonfinite = 1;
 }
 
 // dst[i] = cvt(src[map ? map[i] : i]), i < n
@@ -86,13 +91,13 @@ int blocks_for(int64_t n) {
 namespace pn {
 
 cudaError_t launch_state_store(int precision, const double *src, int64_t n, const int64_t *map,
-                               void *dst, cudaStream_t st) {
+                               void *dst, cudaStream_t st, int32_t *nonfinite) {
   if (n <= 0) return cudaSuccess;
   const int nb = blocks_for(n);
   switch (precision) {
-    case PN_PREC_F32: k_state_store<float><<<nb, 256, 0, st>>>(src, n, map, (float *)dst); break;
-    case PN_PREC_DF64: k_state_store<float2><<<nb, 256, 0, st>>>(src, n, map, (float2 *)dst); break;
-    default: k_state_store<double><<<nb, 256, 0, st>>>(src, n, map, (double *)dst); break;
+    case PN_PREC_F32: k_state_store<float><<<nb, 256, 0, st>>>(src, n, map, (float *)dst, nonfinite); break;
+    case PN_PREC_DF64: k_state_store<float2><<<nb, 256, 0, st>>>(src, n, map, (float2 *)dst, nonfinite); break;
+    default: k_state_store<double><<<nb, 256, 0, st>>>(src, n, map, (double *)dst, nonfinite); break;
   }
   return cudaGetLastError();
 }

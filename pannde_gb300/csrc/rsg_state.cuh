@@ -6,10 +6,11 @@
 
 namespace pn {
 
-// Convert n FP64 values at src (device) to the storage type of `precision`
-// and write them to dst[map[i]] (dst[i] when map is null).
+// Convert n FP64 values at src (device-accessible) to the storage type of
+// `precision` and write them to dst[map[i]] (dst[i] when map is null); sets
+// *nonfinite (device, when given) to 1 if any value is NaN or infinite.
 cudaError_t launch_state_store(int precision, const double *src, int64_t n, const int64_t *map,
-                               void *dst, cudaStream_t st);
+                               void *dst, cudaStream_t st, int32_t *nonfinite = nullptr);
 
 // Read src[map[i]] (src[i] when map is null) in the storage type of
 // `precision` and write it as FP64 to dst[i] (device), i < n.

@@ -258,3 +258,62 @@ def test_info_bytes(cuda_device, plate):
         inf = s.info()
     assert inf["form_name"] == "grid" and inf["grid"] == (16, 16, 4)
     assert inf["algorithmic_bytes_per_step"] == c.mesh.n_cells * 97 + c.mesh.n_nodes * 56
+
+
+@pytest.mark.parametrize("form", ["grid", "table"])
+@pytest.mark.parametrize("prec", ["f64", "df64", "f32"])
+def test_state_transfer_pinned_and_pageable_agree(cuda_device, plate, prec, form):
+    """set_state / get_state read and write page-locked caller buffers
+    directly and stage any other memory: both give the same bits."""
+    import torch
+    c = plate
+    V0, S0 = random_state(c.mesh, 5)
+
+    def pinned_copy(a):
+        t = torch.empty(a.size, dtype=torch.float64, pin_memory=True).numpy()
+        t[:] = a
+        return t
+
+    out = []
+    for pin in (False, True):
+        Vi = [pinned_copy(a) for a in V0] if pin else V0
+        Si = [pinned_copy(a) for a in S0] if pin else S0
+        with Solver(c.mesh, c, c.dt, prec, form) as s:
+            s.set_state(Vi, Si)
+            s.solve(3)
+            Vo = [torch.empty(c.mesh.n_nodes, dtype=torch.float64, pin_memory=pin).numpy() for _ in range(3)]
+            So = [torch.empty(c.mesh.n_cells, dtype=torch.float64, pin_memory=pin).numpy() for _ in range(6)]
+            s.get_state_into(Vo, So)
+        out.append([x.copy() for x in Vo + So])
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("form", ["grid", "table"])
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_non_finite_state_is_refused_and_changes_nothing(cuda_device, plate, prec, form):
+    """set_state refuses NaN and infinity (PN_ERR_NOT_FINITE, naming the
+    field) and leaves the solver's state as it was: the solve goes on with
+    the same bits as a solver that never saw the call."""
+    c = plate
+    V0, S0 = random_state(c.mesh, 6)
+    results = []
+    for poison in (False, True):
+        with Solver(c.mesh, c, c.dt, prec, form) as s:
+            s.set_state(V0, S0)
+            s.solve(2)
+            if poison:
+                badV = [v.copy() for v in V0]
+                badV[1][7] = np.nan
+                with pytest.raises(N.PnError) as e:
+                    s.set_state(badV, S0)
+                assert e.value.code == N.PN_ERR_NOT_FINITE and "velocity" in e.value.msg
+                badS = [x.copy() for x in S0]
+                badS[3][-1] = np.inf
+                with pytest.raises(N.PnError) as e:
+                    s.set_state(V0, badS)
+                assert e.value.code == N.PN_ERR_NOT_FINITE and "stress" in e.value.msg
+            s.solve(3)
+            results.append(s.get_state())
+    for a, b in zip(results[0][0] + results[0][1], results[1][0] + results[1][1]):
+        assert np.array_equal(a, b)
