@@ -264,29 +264,35 @@ def test_info_bytes(cuda_device, plate):
 @pytest.mark.parametrize("prec", ["f64", "df64", "f32"])
 def test_state_transfer_pinned_and_pageable_agree(cuda_device, plate, prec, form):
     """set_state / get_state read and write page-locked caller buffers
-    directly and stage any other memory: both give the same bits."""
+    directly (aligned or not) and stage any other memory: all give the same
+    bits."""
     import torch
     c = plate
     V0, S0 = random_state(c.mesh, 5)
 
-    def pinned_copy(a):
-        t = torch.empty(a.size, dtype=torch.float64, pin_memory=True).numpy()
+    def buf(n, pin, shift):
+        # page-locked or not; shift 1: starts 8 bytes past a 16-byte boundary
+        return torch.empty(n + shift, dtype=torch.float64, pin_memory=pin).numpy()[shift:]
+
+    def copy_of(a, pin, shift):
+        t = buf(a.size, pin, shift)
         t[:] = a
         return t
 
     out = []
-    for pin in (False, True):
-        Vi = [pinned_copy(a) for a in V0] if pin else V0
-        Si = [pinned_copy(a) for a in S0] if pin else S0
+    for pin, shift in ((False, 0), (True, 0), (True, 1)):
+        Vi = [copy_of(a, pin, shift) for a in V0]
+        Si = [copy_of(a, pin, shift) for a in S0]
         with Solver(c.mesh, c, c.dt, prec, form) as s:
             s.set_state(Vi, Si)
             s.solve(3)
-            Vo = [torch.empty(c.mesh.n_nodes, dtype=torch.float64, pin_memory=pin).numpy() for _ in range(3)]
-            So = [torch.empty(c.mesh.n_cells, dtype=torch.float64, pin_memory=pin).numpy() for _ in range(6)]
+            Vo = [buf(c.mesh.n_nodes, pin, shift) for _ in range(3)]
+            So = [buf(c.mesh.n_cells, pin, shift) for _ in range(6)]
             s.get_state_into(Vo, So)
         out.append([x.copy() for x in Vo + So])
-    for a, b in zip(out[0], out[1]):
-        assert np.array_equal(a, b)
+    for other in out[1:]:
+        for a, b in zip(out[0], other):
+            assert np.array_equal(a, b)
 
 
 @pytest.mark.parametrize("form", ["grid", "table"])
