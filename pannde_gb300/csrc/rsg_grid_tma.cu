@@ -281,8 +281,9 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
       if (k0 - 1 + d <= k1) issue(k0 - 1 + d);
   }
 
-  R vpx0 = R(), vpx4 = R(), vpx5 = R(), vpy1 = R(), vpy3 = R(), vpy5 = R(), vs2 = R(), vs3 = R(),
-    vs4 = R();
+  // per cell layer: A = (x, y differences) + z sum, B = the same - z sum; a
+  // node's acceleration is A of the layer above + B of the layer below
+  R blx = R(), bly = R(), blz = R();  // B of the layer below
   R spx[3], spy[3], ss[3];
 #pragma unroll
   for (int c = 0; c < 3; c++) spx[c] = spy[c] = ss[c] = R();
@@ -319,17 +320,33 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
       A = cellv(5, ra); B = cellv(5, ib); C = cellv(5, ic); D = cellv(5, id);
       R px5, py5;
       diffdiff22(A, B, C, D, px5, py5);
+      // x: Sxx along x, Sxy along y, Sxz along z; y: Sxy, Syy, Syz; z: Sxz, Syz, Szz
+      R tx, ty, tz, ax, ay, az, nbx, nby, nbz;
+      if constexpr (CUBIC) {  // 0.25/h folded into dt/rho and the force weights
+        tx = px0 + py5;
+        ty = px5 + py1;
+        tz = px4 + py3;
+        ax = tx + s4;
+        ay = ty + s3;
+        az = tz + s2;
+        nbx = tx - s4;
+        nby = ty - s3;
+        nbz = tz - s2;
+      } else {
+        tx = madd(gy, py5, gx * px0);
+        ty = madd(gy, py1, gx * px5);
+        tz = madd(gy, py3, gx * px4);
+        ax = madd(gz, s4, tx);
+        ay = madd(gz, s3, ty);
+        az = madd(gz, s2, tz);
+        nbx = madd(-gz, s4, tx);
+        nby = madd(-gz, s3, ty);
+        nbz = madd(-gz, s2, tz);
+      }
       if (k >= k0) {
-        R ax, ay, az;
-        if constexpr (CUBIC) {  // 0.25/h folded into dt/rho and the force weights
-          ax = (vpx0 + px0) + (vpy5 + py5) + (s4 - vs4);
-          ay = (vpx5 + px5) + (vpy1 + py1) + (s3 - vs3);
-          az = (vpx4 + px4) + (vpy3 + py3) + (s2 - vs2);
-        } else {
-          ax = madd(gz, s4 - vs4, madd(gy, vpy5 + py5, gx * (vpx0 + px0)));
-          ay = madd(gz, s3 - vs3, madd(gy, vpy1 + py1, gx * (vpx5 + px5)));
-          az = madd(gz, s2 - vs2, madd(gy, vpy3 + py3, gx * (vpx4 + px4)));
-        }
+        ax = ax + blx;
+        ay = ay + bly;
+        az = az + blz;
         const int2 fr = sRf[k - k0 + 1];
         for (int e = fr.x; e < fr.y; e++) {  // force sources of this block and layer
           const int key = __ldg(a.f_key + e);
@@ -369,8 +386,9 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
           }
         }
       }
-      vpx0 = px0; vpx4 = px4; vpx5 = px5; vpy1 = py1; vpy3 = py3; vpy5 = py5;
-      vs2 = s2; vs3 = s3; vs4 = s4;
+      blx = nbx;
+      bly = nby;
+      blz = nbz;
     }
 
     // ---- C: partial sums of node layer k-1, stress of cell layer k-2
