@@ -275,7 +275,10 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
   }
   for (int q = t; q < k1 - k0; q += NT) sRm[q] = a.m_rng ? a.m_rng[(int64_t)blk * nz + k0 + q] : make_int2(0, 0);
   __syncthreads();
-  if (t == 0) {
+  // the copies are issued (and, on failure, drained) by the first thread of
+  // the last warp: its row is the tile's apron, which has no stress half
+  constexpr int ISSUER = (TY - 1) * TX;
+  if (t == ISSUER) {
 #pragma unroll
     for (int d = 0; d <= G::PD; d++)
       if (k0 - 1 + d <= k1) issue(k0 - 1 + d);
@@ -293,7 +296,7 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
   bool fail = false;
 
   for (int k = k0 - 1; k <= k1 + 1; k++) {
-    if (t == 0 && k >= k0 && k + G::PD <= k1) {
+    if (t == ISSUER && k >= k0 && k + G::PD <= k1) {
       proxy_fence_async_smem();
       issue(k + G::PD);
     }
@@ -481,7 +484,7 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
     }
     if (__syncthreads_or(fail)) {
       // give up: record, drain this block's copies in flight, return
-      if (t == 0) {
+      if (t == ISSUER) {
         if (a.err) atomicExch(a.err, kErrWait);
         const int issued = min(k1, max(k + G::PD, k0 - 1 + G::PD));
         for (int L = waited + 1; L <= issued; L++) (void)mbar_wait(bar_of(L), parity(L));
