@@ -59,6 +59,31 @@ def test_two_calls_match_batch_solve(cuda_device, form, prec):
         y.close()
 
 
+def test_members_with_split_sites(cuda_device):
+    """Grid-form members whose cracks split lattice sites (the staging then
+    also holds the prefixes of their copies and fix cells) beside one
+    without: two calls match pn_batch_solve."""
+    cs = [cases.bracket_case(1000 + i, nsteps=30, water_column=(i == 0), scale=0.3) for i in range(2)]
+    cs.append(members()[0])
+    grown = [Solver.from_case(c, precision="f32", form="grid", capacity=30) for c in cs]
+    fixed = [Solver.from_case(c, precision="f32", form="grid", capacity=30) for c in cs]
+    with Batch() as a, Batch() as b:
+        for s in grown:
+            a.add(s)
+        for s in fixed:
+            b.add(s)
+        a.solve(1)
+        b.solve(1)
+        a.solve(9)
+        a.solve(10)
+        b.solve_noalloc(9)
+        b.solve_noalloc(10)
+    for x, y in zip(grown, fixed):
+        same(snapshot(x), snapshot(y))
+        x.close()
+        y.close()
+
+
 def test_members_without_tables_are_refused(cuda_device):
     c = members()[0]
     with Solver.from_case(c, precision="f32", capacity=10) as s, Batch() as b:
