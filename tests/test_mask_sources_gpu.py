@@ -65,3 +65,36 @@ def test_masks_reproduce_geometry_sources(cuda_device, prec, form):
         tr = s.traces()
     assert tt == ref["time"]
     compare(prec, (V, S, tr), ref)
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_masks_on_split_sites(cuda_device, prec):
+    """The same on a grid-form mesh whose crack (disconnected faces) splits
+    lattice sites: mask forces on both faces' nodes and a mask moment on cells
+    at the crack take the fix-up's lists."""
+    from tests.test_grid_gpu import cracked_block
+    c, lower, upper = cracked_block()
+    m = c.mesh
+    t = np.linspace(0.0, 2e-7, 60)
+    v = np.sin(2e7 * t)
+    src = [cases.WindowSource(N.PN_SOURCE_FORCE, 0, 2, (1.0e-3, 0.6e-3, 0.5e-3), 0.25e-3, 1e-4, t, v),
+           cases.WindowSource(N.PN_SOURCE_MOMENT, 1, 1, (1.2e-3, 0.6e-3, 0.5e-3), 0.2e-3, 1e-4, t, v)]
+    nsteps = 30
+    sens = np.sort(np.concatenate([lower[::7], upper[::5]])).astype(np.int32)
+    ref = oracle.run(m, c.material_fields(), c.dt, src, nsteps, sens)
+    centres = m.cell_centers()
+    nodes = np.stack([m.x, m.y, m.z], axis=1)
+    masks = [(s.kind, s.group, s.component,
+              check_at(s, centres if s.kind == N.PN_SOURCE_FORCE else nodes)) for s in src]
+    values = signal_values(src, c.dt, nsteps)
+    with Solver(m, c, c.dt, prec, "grid") as s:
+        assert s.info()["form_name"] == "grid"
+        s.add_window_masks(masks)
+        s.set_sensors(sens, nsteps)
+        tt = 0.0
+        for a, b in ((0, 11), (11, nsteps)):
+            tt = s.solve_signals(values[a:b])
+        V, S = s.get_state()
+        tr = s.traces()
+    assert tt == ref["time"]
+    compare(prec, (V, S, tr), ref)
