@@ -298,6 +298,25 @@ def test_grid_many_materials_use_classic_kernel(cuda_device):
     compare("df64", dev, ref)
 
 
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_grid_crack_on_the_classic_kernel(cuda_device, prec):
+    """Split sites with more materials than the tensor-copy kernel stages: the
+    classic kernel marches the whole box and the same fix-up follows it."""
+    c0, lower, upper = cracked_block()
+    m = c0.mesh
+    base = cases.c21_from_6x6(cases.isotropic(70e9, 0.33))
+    mats = np.stack([base * (1.0 + 0.01 * q) for q in range(40)])
+    cm = ((m.cell_ijk[:, 0] + 3 * m.cell_ijk[:, 2]) % 40).astype(np.int32)
+    c = cases.Case("crack40", m, np.full(40, 2700.0), mats, cm, 4e-9)
+    V0, S0 = random_state(m, 8)
+    sens = np.sort(np.concatenate([lower[::6], upper[::4]])).astype(np.int32)
+    ref = oracle.run(m, c.material_fields(), c.dt, [], 12, sens, V0=V0, S0=S0)
+    with Solver(m, c, c.dt, prec, "grid") as s:
+        assert s.info()["kernel_name"] == "classic"
+    dev, _ = run_grid(m, c, c.dt, [], 12, sens, prec, V0=V0, S0=S0)
+    compare(prec, dev, ref)
+
+
 def test_grid_split_sites_state_roundtrip_and_energy(cuda_device):
     """Nodes of split sites live in tail slots of the node buffers: a state
     set and read back at zero steps is the same bits, and the FP64 energy
