@@ -316,7 +316,7 @@ def batch_leg(n_members, sample_steps, torch, steps_total=3000, form="auto"):
     batch's stream; the per-step cost does not change along the run."""
     from pannde_gb300 import cases
     from pannde_gb300.solver import Batch, Solver
-    warm = 5
+    warm = 20  # long enough for the launch-shape tuning (2 rounds x up to 4 shapes x 2 steps) to run untimed
     t0 = time.perf_counter()
     cs = [cases.bracket_case(1000 + i, nsteps=steps_total, water_column=(i % 6 == 0)) for i in range(n_members)]
     solvers = [Solver.from_case(c, precision="f32", capacity=warm + sample_steps, form=form) for c in cs]

@@ -156,14 +156,22 @@ __device__ __forceinline__ uint64_t global_ns() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-// wait for phase `parity` of the barrier; false after about one second
-__device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  if (mbar_try_wait(bar, parity)) return true;
+// wait for phase `parity` of the barrier; false after about one second (the
+// loop out of line: the first try usually succeeds)
+__device__ __noinline__ bool mbar_wait_slow(uint32_t bar, uint32_t parity) {
   const uint64_t t0 = global_ns();
   for (uint32_t n = 1;; n++) {
     if (mbar_try_wait(bar, parity)) return true;
     if ((n & 63) == 0 && global_ns() - t0 > 1000000000ull) return false;
   }
+}
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  return mbar_try_wait(bar, parity) || mbar_wait_slow(bar, parity);
+}
+// the whole wait out of line (fewer registers live across it: the batch
+// kernel, which reads its arguments through global memory)
+__device__ __noinline__ bool mbar_wait_call(uint32_t bar, uint32_t parity) {
+  return mbar_try_wait(bar, parity) || mbar_wait_slow(bar, parity);
 }
 __device__ __forceinline__ void proxy_fence_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -186,7 +194,7 @@ __device__ __forceinline__ int floor_to(int v, int m) {  // largest multiple of 
 // error word codes
 constexpr int32_t kErrWait = 1;
 
-template <typename R, int SYM>
+template <typename R, int SYM, bool BATCH = false>
 __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::S> &a, const GridMaps *M,
                                                int bx, int by, int bz, int gxc, int step) {
   using N = GNum<R>;
@@ -198,7 +206,14 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
   constexpr int SB = G::SBOX / (int)sizeof(St);  // field stride in a slot (elements)
   constexpr int VB = G::VBOX / (int)sizeof(St);
   extern __shared__ unsigned char smem_raw[];
-  unsigned char *base = (unsigned char *)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
+  // 128-byte aligned base.  A single launch derives it from smem_raw by an
+  // offset, so that every tile pointer stays in the shared state space (shared
+  // loads and stores, 32-bit addressing: FP32 45.4 -> 47.8, double-float 18.0
+  // -> 19.3 Gcell-steps/s on the laminate).  The batch kernel, which reads its
+  // arguments through global memory, spilled with that and ran slower; it keeps
+  // the generic pointer.
+  unsigned char *base = BATCH ? (unsigned char *)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127)
+                              : smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
   St *sVt = reinterpret_cast<St *>(base + G::OFF_VT);
   St *sC = reinterpret_cast<St *>(base + G::OFF_C);
   int2 *sRf = reinterpret_cast<int2 *>(base + G::OFF_R);
@@ -302,7 +317,7 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
     }
     // ---- B: velocity of node layer k
     if (k <= k1) {
-      if (mbar_wait(bar_of(k), parity(k))) waited = k;
+      if (BATCH ? mbar_wait_call(bar_of(k), parity(k)) : mbar_wait(bar_of(k), parity(k))) waited = k;
       else fail = true;
       const St *Sk = reinterpret_cast<const St *>(sslot(k));
       auto cellv = [&](int f, int q) { return N::val(Sk[f * SB + q]); };
@@ -522,7 +537,7 @@ __global__ void __launch_bounds__(NT, GMinBlocks<R>::v)
   const GridMaps *M = reinterpret_cast<const GridMaps *>(a.tmaps);
   const int local = id - __ldg(block_start + lo);
   const int gxc = a.nx / (TX - 1) + 1, gyc = a.ny / (TY - 1) + 1;
-  grid_block_tma<R, SYM>(a, M, local % gxc, (local / gxc) % gyc, local / (gxc * gyc), gxc, step);
+  grid_block_tma<R, SYM, true>(a, M, local % gxc, (local / gxc) % gyc, local / (gxc * gyc), gxc, step);
 }
 
 template <typename R, int SYM>
