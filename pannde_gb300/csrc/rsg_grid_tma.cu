@@ -379,12 +379,12 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
         R vn[3];
 #pragma unroll
         for (int c = 0; c < 3; c++) vn[c] = N::val(Vk[c * VB + rv]);
+        // dt/rho is 0 at void and padding sites, whose differences are 0 too:
+        // the update leaves them unchanged without a branch
         const R cf = N::val(Vk[3 * VB + rv]);
-        if (!(cf == R())) {
-          vn[0] = madd(cf, ax, vn[0]);
-          vn[1] = madd(cf, ay, vn[1]);
-          vn[2] = madd(cf, az, vn[2]);
-        }
+        vn[0] = madd(cf, ax, vn[0]);
+        vn[1] = madd(cf, ay, vn[1]);
+        vn[2] = madd(cf, az, vn[2]);
         St *Vt = sVt + (k & 1) * 3 * NT;
 #pragma unroll
         for (int c = 0; c < 3; c++) Vt[c * NT + t] = N::sto(vn[c]);
