@@ -85,6 +85,39 @@ def test_form_selection():
     assert rc == N.PN_ERR_INVALID
 
 
+def test_form_selection_sparse_boxes_and_split_sites():
+    """The grid form takes a lattice box it marches in at most twice the mesh's
+    cells (each tile column stops at its top solid layer) and lattice sites
+    that several nodes share (a crack as disconnected faces), within limits."""
+    for crack in ("faces", "slab"):  # L-brackets: about a quarter of the box solid
+        b = cases.bracket_case(1003, nsteps=10, crack=crack, scale=0.35)
+        rc, p, _ = plan(b.mesh, table=b.material_table(), precision=N.PN_PREC_F32)
+        assert rc == 0 and p.form == N.PN_FORM_GRID, crack
+    # solid only along the box's diagonal: the tiles' columns are mostly void
+    solid = np.zeros((60, 60, 6), dtype=bool)
+    for q in range(60):
+        solid[q, q, :] = True
+    d = cases.voxel_mesh(solid, 1e-4)
+    dc = cases.Case("diag", d, np.array([2700.0]), cases.c21_from_6x6(cases.isotropic(70e9, 0.33))[None],
+                    np.zeros(d.n_cells, np.int32), 1e-9)
+    rc, p, _ = plan(d, table=dc.material_table(), precision=N.PN_PREC_F32)
+    assert rc == 0 and p.form == N.PN_FORM_TABLE
+    rc, p, msg = plan(d, table=dc.material_table(), precision=N.PN_PREC_F32 | N.PN_FORM_GRID)
+    assert rc == N.PN_ERR_INVALID and "mostly void" in msg
+    # four cracked planes: more than an eighth of the nodes share a lattice site
+    m = cases.voxel_mesh(np.ones((10, 10, 10), dtype=bool), 1e-4)
+    for z in (2, 4, 6, 8):
+        ni, nj, nk = m.node_ijk[:, 0], m.node_ijk[:, 1], m.node_ijk[:, 2]
+        face = (nk == z) & (ni > 0) & (ni < 10) & (nj > 0) & (nj < 10)
+        m = cases.disconnect_face(m, np.flatnonzero(m.cell_ijk[:, 2] >= z), face)
+    mc = cases.Case("planes", m, np.array([2700.0]), cases.c21_from_6x6(cases.isotropic(70e9, 0.33))[None],
+                    np.zeros(m.n_cells, np.int32), 1e-9)
+    rc, p, msg = plan(m, table=mc.material_table(), precision=N.PN_PREC_F32 | N.PN_FORM_GRID)
+    assert rc == N.PN_ERR_INVALID and "sharing lattice sites" in msg
+    rc, p, _ = plan(m, table=mc.material_table(), precision=N.PN_PREC_F32)
+    assert rc == 0 and p.form == N.PN_FORM_TABLE
+
+
 def test_plan_dedups_field_materials():
     c = cases.laminate_case(nx=6, ny=5, nz=8, nsteps=1, n_sensors=2)
     rc, p, _ = plan(c.mesh, material=c.material_fields())
