@@ -69,9 +69,12 @@ enum pn_precision {
    the same mesh. */
 enum pn_form {
   /* the grid form when the mesh is a voxel grid (every node on a uniform
-     lattice, every cell a lattice box in the reference corner order, at most
-     half of the lattice box void) and the precision is not PN_PREC_F64_EXACT;
-     else the table form */
+     lattice, every cell a lattice box in the reference corner order; several
+     nodes may share a lattice site, as a crack modelled as disconnected faces
+     has them, up to an eighth of the nodes), the fused kernel marches at most
+     twice the mesh's cells in its lattice box (each tile column stops at its
+     top solid layer) and the precision is not PN_PREC_F64_EXACT; else the
+     table form */
   PN_FORM_AUTO = 0,
   /* connectivity tables on the device (cell -> 8 nodes, node -> 8 cell
      slots), two kernels per step; any hex mesh */
@@ -266,7 +269,10 @@ int pn_solver_set_stream(pn_solver *s, void *cuda_stream);
 
 /* Upload the initial condition: V[3] = Vx,Vy,Vz ([n_nodes] each), S[6] =
    Sxx,Syy,Szz,Syz,Sxz,Sxy ([n_cells] each); a NULL pointer means zero.
-   Replaces setupSolution (HostRSGTDUT.hpp:235-239). */
+   Arrays in page-locked host memory are read by the GPU directly, others are
+   staged; returns when the transfer is done.  PN_ERR_NOT_FINITE (state left
+   unchanged) when a value is NaN or infinite.  Replaces setupSolution
+   (HostRSGTDUT.hpp:235-239). */
 int pn_solver_set_state(pn_solver *s, const double *const *V, const double *const *S);
 
 /* Add windowed sources.  Replaces the transducer constructor arguments
@@ -303,7 +309,8 @@ int pn_solver_solve(pn_solver *s, int32_t nsteps, double *time_out);
 int pn_solver_solve_signals(pn_solver *s, int32_t nsteps, const double *values, double *time_out);
 
 /* Synchronise and download the state into caller-owned host arrays (same
-   layout as pn_solver_set_state; NULL pointers are skipped).  Replaces the
+   layout as pn_solver_set_state; NULL pointers are skipped; page-locked
+   arrays are written by the GPU directly).  Replaces the
    host reads the runners make through Model::getStates() (Model.hpp:77-106,
    TransducerModel.cpp:143-149, VTKGrid.hpp:125-160). */
 int pn_solver_get_state(pn_solver *s, double *const *V, double *const *S);
