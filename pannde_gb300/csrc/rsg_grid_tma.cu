@@ -310,6 +310,9 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
   int waited = k0 - 2;                   // last layer this thread has waited for
   bool fail = false;
 
+  // FP32 storage: two layers per unrolled body, so the values carried from
+  // one layer to the next alternate registers instead of moving
+#pragma unroll(sizeof(St) == 4 ? 2 : 1)
   for (int k = k0 - 1; k <= k1 + 1; k++) {
     if (t == ISSUER && k >= k0 && k + G::PD <= k1) {
       proxy_fence_async_smem();
