@@ -39,7 +39,7 @@ enum pn_status {
                             signal arrays, HostUnivariate.hpp:80 */
   PN_ERR_CUDA = 5,       /* a CUDA runtime call failed */
   PN_ERR_ALLOC = 6,      /* device allocation failed or exceeds the HBM budget */
-  PN_ERR_NOT_FINITE = 7, /* NaN/Inf in an input array (checked before upload) */
+  PN_ERR_NOT_FINITE = 7, /* NaN/Inf in an input array (the call changes nothing) */
   PN_ERR_DEVICE_CHECK = 8/* a device-side bounds check recorded an error */
 };
 
@@ -140,7 +140,7 @@ typedef struct pn_material {
    stiffness cij[cell_material[c]][0..20] (same 21-entry order as pn_material).
    Equivalent to CELL fields built from the table; this is how the reference's
    case makers write per-cell properties from a few materials
-   (py_utils/Case_Makers/*: C_arr[:, cell] = C[:, Geom[i,j,k]-1]) without the
+   (the py_utils/Case_Makers scripts: C_arr[:, cell] = C[:, Geom[i,j,k]-1]) without the
    caller expanding them to n_cells x 22 doubles. */
 typedef struct pn_material_table {
   int32_t n_materials;

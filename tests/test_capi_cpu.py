@@ -273,3 +273,27 @@ def test_null_arguments():
     assert lib.pn_solver_create(None, None, 1.0, 1, ctypes.byref(h)) == N.PN_ERR_INVALID
     assert lib.pn_solver_solve(None, 1, None) == N.PN_ERR_INVALID
     assert lib.pn_solver_destroy(None) == N.PN_OK
+
+
+def test_integration_c_example_builds(tmp_path):
+    """The C example of the integration notes compiles as C99 against the
+    header and links against the library; it runs a solve on a GPU and
+    reports that no CUDA device is usable elsewhere."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+    if not shutil.which("gcc"):
+        pytest.skip("no gcc")
+    root = Path(__file__).resolve().parent.parent
+    lib = root / "pannde_gb300" / "_build"
+    exe = tmp_path / "capi_example"
+    r = subprocess.run(["gcc", "-std=c99", "-O1", "-Wall", "-Werror", "-I", str(root / "include"),
+                        str(root / "tests" / "cxx" / "capi_example.c"), "-L", str(lib), "-lpannde_gb300",
+                        f"-Wl,-rpath,{lib}", "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert run.returncode in (0, 3), run.stdout + run.stderr
+    if run.returncode == 0:
+        assert "10 records" in run.stdout
+    else:
+        assert "create:" in run.stdout
