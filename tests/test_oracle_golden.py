@@ -232,3 +232,57 @@ def test_empty_mesh_and_zero_steps():
     p = cases.al_plate_case(nx=4, ny=4, nz=2, nsteps=0, n_sensors=2)
     r = oracle.run(p.mesh, p.material_fields(), p.dt, p.sources, 0, p.sensors)
     assert r["time"] == 0.0 and all(np.all(v == 0) for v in r["V"])
+
+
+def _random_cases():
+    """Seeded small cases the fixtures do not cover together."""
+    from tests.test_grid_gpu import cracked_block
+    rng = np.random.default_rng(2024)
+    out = []
+    # holes, two materials, a transducer, a random state (HostRSGTDUT)
+    solid = np.ones((14, 10, 5), dtype=bool)
+    solid[4:7, 3:6, :] = False
+    solid[10:, :3, 3:] = False
+    m = cases.voxel_mesh(solid, 1e-4)
+    mat = (m.cell_ijk[:, 0] >= 7).astype(np.int32)
+    cij = np.stack([cases.c21_from_6x6(cases.isotropic(70e9, 0.33)),
+                    cases.c21_from_6x6(cases.rotate_about_z(
+                        cases.orthotropic_ply(140e9, 10e9, 10e9, 6e9, 6e9, 4e9, 3e9, 5e9, 5e9), 30.0))])
+    c = cases.Case("holes", m, np.array([2700.0, 1600.0]), cij, mat, 4e-9)
+    t = np.linspace(0.0, 2e-7, 40)
+    v = np.sin(3e7 * t)
+    src = [cases.transducer_z((0.7e-3, 0.5e-3, 0.5e-3), 0.3e-3, 1e-4, t, v)]
+    out.append((c, src, 0))
+    # water-column moments and a transducer (HostUTModel)
+    src2 = [cases.WindowSource(N.PN_SOURCE_MOMENT, 0, k, (0.3e-3, 0.3e-3, 0.5e-3), 0.25e-3, 1e-4, t, v * s)
+            for k, s in ((0, 1.0), (1, 0.5), (2, -0.8))] + src
+    out.append((c, src2, 1))
+    # a crack as disconnected faces
+    cb, _, _ = cracked_block()
+    out.append((cb, [cases.transducer_z((1.0e-3, 0.6e-3, 0.5e-3), 0.25e-3, 1e-4, t, v)], 0))
+    # graded spacing along x
+    g = cases.plate_builder(1.2e-3, 0.8e-3, 0.3e-3, 6, 3)
+    g.x = g.x * (1 + 80.0 * g.x)
+    gc = cases.Case("graded", g, np.array([2700.0]), cij[:1], np.zeros(g.n_cells, np.int32), 2e-9)
+    out.append((gc, [], 0))
+    return [(c, s, k, rng.integers(1 << 30)) for c, s, k in out]
+
+
+@pytest.mark.parametrize("idx", range(4), ids=["holes", "moments", "crack", "graded"])
+def test_port_matches_compiled_reference(idx):
+    """The C restatement against the reference HostSolver compiled from its own
+    sources, on seeded cases from a random state: every field, trace and the
+    time bit for bit."""
+    if oracle.reference() is None:
+        pytest.skip("reference sources not present")
+    c, src, kind, seed = _random_cases()[idx]
+    r = np.random.default_rng(int(seed))
+    V0 = [r.uniform(-1e-3, 1e-3, c.mesh.n_nodes) for _ in range(3)]
+    S0 = [r.uniform(-1e5, 1e5, c.mesh.n_cells) for _ in range(6)]
+    sens = np.sort(r.choice(c.mesh.n_nodes, size=6, replace=False)).astype(np.int32)
+    args = (c.mesh, c.material_fields(), c.dt, src, 15, sens)
+    port = oracle.run(*args, V0=V0, S0=S0, impl="port")
+    ref = oracle.run(*args, V0=V0, S0=S0, impl="reference", model_kind=kind)
+    assert port["time"] == ref["time"]
+    for a, b in zip(port["V"] + port["S"] + [port["traces"]], ref["V"] + ref["S"] + [ref["traces"]]):
+        assert np.array_equal(a, b)
