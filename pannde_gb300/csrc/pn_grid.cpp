@@ -169,8 +169,14 @@ bool grid_eligible(const MeshTables &m, const MaterialTables &mt, int precision,
 int64_t grid_footprint(const GridMap &g, const MaterialTables &mt, int precision) {
   const int64_t e = precision == PN_PREC_F32 ? 4 : 8;
   const int64_t gn = g.node_len(), gc = g.cell_sites();
+  const int64_t tiles = (int64_t)(g.nx / (grid_tile_x() - 1) + 1) * (g.ny / (grid_tile_y() - 1) + 1);
+  // state (two halves), dt/rho, material bytes, stiffness rows, tensor maps,
+  // per-tile top layers, error word and finiteness flags, split-site tables
+  // (the copies' and fix cells' source and sensor entries come with those)
   return 2 * (3 * gn + 6 * gc) * e + gn * e + gc + (int64_t)(mt.n_mat + 1) * 36 * e +
-         2 * (int64_t)grid_tma_maps_bytes() + 16;
+         2 * (int64_t)grid_tma_maps_bytes() + tiles * 4 + 64 + 8 +
+         (int64_t)g.copy_node.size() * (int64_t)sizeof(SplitCopy) +
+         (int64_t)g.fix_cell.size() * (int64_t)sizeof(FixCell) + 16;
 }
 
 

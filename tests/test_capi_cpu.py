@@ -297,3 +297,24 @@ def test_integration_c_example_builds(tmp_path):
         assert "10 records" in run.stdout
     else:
         assert "create:" in run.stdout
+
+
+def test_plan_counts_split_site_storage():
+    """A crack's extra node copies (tail slots of the state and dt/rho
+    buffers) and the fix-up tables are in the grid form's footprint."""
+    solid = np.ones((16, 10, 8), dtype=bool)
+    m0 = cases.voxel_mesh(solid, 1e-4)
+    ni, nj, nk = m0.node_ijk[:, 0], m0.node_ijk[:, 1], m0.node_ijk[:, 2]
+    face = (nk == 4) & (ni > 3) & (ni < 12) & (nj > 2) & (nj < 8)
+    m1 = cases.disconnect_face(m0, np.flatnonzero(m0.cell_ijk[:, 2] >= 4), face)
+    tab = cases.c21_from_6x6(cases.isotropic(70e9, 0.33))[None]
+    sizes = []
+    for m in (m0, m1):
+        c = cases.Case("b", m, np.array([2700.0]), tab, np.zeros(m.n_cells, np.int32), 1e-9)
+        rc, p, _ = plan(m, table=c.material_table(), precision=N.PN_PREC_F64)
+        assert rc == 0 and p.form == N.PN_FORM_GRID
+        sizes.append(p.device_bytes)
+    extra = int(face.sum())
+    copies = 2 * extra                  # both copies of every split site
+    state = extra * (2 * 3 + 1) * 8     # V in both halves and dt/rho, FP64
+    assert sizes[1] - sizes[0] >= state + copies * 40
