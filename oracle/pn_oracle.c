@@ -25,9 +25,12 @@
  *   HostNormalXDZ::evalAt ..... Stubs/include/HostNormalXDZ.hpp:117-123,174-177
  *   HostUnivariate::evalAt .... HostData/include/HostUnivariate.hpp:109-142
  *
- * The node and cell loops are independent per element, so they run under
- * OpenMP when compiled with -fopenmp; results do not depend on the thread
- * count.
+ * The node and cell loops, the spacing and coefficient setup and the source
+ * hit lists are independent per element, so they run under OpenMP when
+ * compiled with -fopenmp; the hit lists are built in two passes (count,
+ * prefix sum, fill) and the spacing check reports the first bad node in node
+ * order, so results and errors do not depend on the thread count.  Only
+ * buildLinks stays serial: a later cell overwrites an earlier one's link.
  */
 #include <math.h>
 #include <stdint.h>
@@ -62,6 +65,7 @@ static int build_links(const pn_mesh *m, int32_t *ncc) {
 
 /* ---- RightHex::cellPrep (RightHex.hpp:253-264) ---------------------------*/
 static void cell_prep(const pn_mesh *m, double *dxc, double *dyc, double *dzc) {
+#pragma omp parallel for schedule(static)
   for (int32_t c = 0; c < m->n_cells; c++) {
     int32_t a = m->hexes[(int64_t)c * 8 + 0], b = m->hexes[(int64_t)c * 8 + 6];
     dxc[c] = m->x[b] - m->x[a];
@@ -73,6 +77,10 @@ static void cell_prep(const pn_mesh *m, double *dxc, double *dyc, double *dzc) {
 /* ---- RightHex::nodePrep (RightHex.hpp:272-309) ---------------------------*/
 static int node_prep(const pn_mesh *m, const int32_t *ncc, double *dxn, double *dyn,
                      double *dzn) {
+  /* every node independently; the reference throws at the first node (in
+     node order) whose spacing is not positive, checking DX, DY, DZ in turn */
+  int32_t first_bad = m->n_nodes;
+#pragma omp parallel for schedule(static) reduction(min : first_bad)
   for (int32_t n = 0; n < m->n_nodes; n++) {
     double node[3] = {m->x[n], m->y[n], m->z[n]};
     double lo[3] = {node[0], node[1], node[2]};
@@ -94,11 +102,15 @@ static int node_prep(const pn_mesh *m, const int32_t *ncc, double *dxn, double *
       if (hi[kd] == node[kd]) hi[kd] = 2. * node[kd] - lo[kd];
     }
     dxn[n] = 0.5 * (hi[0] - lo[0]);
-    if (0 >= dxn[n]) return or_fail(PN_ERR_SPACING, "DX");
     dyn[n] = 0.5 * (hi[1] - lo[1]);
-    if (0 >= dyn[n]) return or_fail(PN_ERR_SPACING, "DY");
     dzn[n] = 0.5 * (hi[2] - lo[2]);
-    if (0 >= dzn[n]) return or_fail(PN_ERR_SPACING, "DZ");
+    if ((0 >= dxn[n] || 0 >= dyn[n] || 0 >= dzn[n]) && n < first_bad) first_bad = n;
+  }
+  if (first_bad < m->n_nodes) {
+    const int32_t n = first_bad;
+    if (0 >= dxn[n]) return or_fail(PN_ERR_SPACING, "DX");
+    if (0 >= dyn[n]) return or_fail(PN_ERR_SPACING, "DY");
+    return or_fail(PN_ERR_SPACING, "DZ");
   }
   return PN_OK;
 }
@@ -233,74 +245,85 @@ static int group_sources(const pn_window_source *src, int32_t nsrc, int kind, in
   return PN_OK;
 }
 
+/* the hits of node n, direction dir, in the loop order of evalXds (kb, then
+   xd); written to out when given; returns their number */
+static int32_t force_hits_at(const pn_mesh *m, const int32_t *ncc, const pn_window_source *src,
+                             const or_groups *g, int32_t n, int dir, int32_t *out) {
+  int32_t cnt = 0;
+  for (int kb = 0; kb < 8; kb++) {
+    int32_t c = ncc[(int64_t)n * 8 + kb];
+    if (c == -1) continue;
+    double cc[3];
+    cell_center(m, c, cc);
+    for (int32_t gi = 0; gi < g->ngroups; gi++) {
+      int32_t si = g->slot[gi * 3 + dir];
+      if (si < 0 || !window_at(&src[si], cc)) continue;
+      if (out) out[cnt] = si;
+      cnt++;
+    }
+  }
+  return cnt;
+}
+
+/* the hits of cell c, Voigt component comp, in the loop order of evalMoments */
+static int32_t moment_hits_at(const pn_mesh *m, const pn_window_source *src, const or_groups *g,
+                              int32_t c, int comp, int32_t *out) {
+  int32_t cnt = 0;
+  for (int kb = 0; kb < 8; kb++) {
+    int32_t q = m->hexes[(int64_t)c * 8 + kb];
+    double r[3] = {m->x[q], m->y[q], m->z[q]};
+    for (int32_t gi = 0; gi < g->ngroups; gi++) {
+      int32_t si = g->slot[gi * 6 + comp];
+      if (si < 0 || !window_at(&src[si], r)) continue;
+      if (out) out[cnt] = si;
+      cnt++;
+    }
+  }
+  return cnt;
+}
+
+/* Hit lists per element and component, built in two passes over the
+   elements in parallel (count, prefix sum, fill): every element's hits keep
+   the reference's order, and the list is the same as a serial build's. */
+static int build_hits(const pn_mesh *m, const int32_t *ncc, const pn_window_source *src,
+                      const or_groups *g, int forces, or_hits *h) {
+  const int ncomp = forces ? 3 : 6;
+  const int32_t nel = forces ? m->n_nodes : m->n_cells;
+  const int64_t ne = (int64_t)nel * ncomp;
+  h->start = (int64_t *)calloc((size_t)ne + 1, sizeof(int64_t));
+  if (!h->start) return or_fail(PN_ERR_ALLOC, "oracle: out of memory");
+  if (g->ngroups > 0) {
+#pragma omp parallel for schedule(static)
+    for (int32_t e = 0; e < nel; e++)
+      for (int k = 0; k < ncomp; k++)
+        h->start[(int64_t)e * ncomp + k + 1] =
+            forces ? force_hits_at(m, ncc, src, g, e, k, NULL) : moment_hits_at(m, src, g, e, k, NULL);
+    for (int64_t q = 0; q < ne; q++) h->start[q + 1] += h->start[q];
+  }
+  h->sig = (int32_t *)malloc(sizeof(int32_t) * (size_t)(h->start[ne] > 0 ? h->start[ne] : 1));
+  if (!h->sig) return or_fail(PN_ERR_ALLOC, "oracle: out of memory");
+  if (g->ngroups > 0 && h->start[ne] > 0) {
+#pragma omp parallel for schedule(static)
+    for (int32_t e = 0; e < nel; e++)
+      for (int k = 0; k < ncomp; k++) {
+        int32_t *out = h->sig + h->start[(int64_t)e * ncomp + k];
+        if (forces) force_hits_at(m, ncc, src, g, e, k, out);
+        else moment_hits_at(m, src, g, e, k, out);
+      }
+  }
+  return PN_OK;
+}
+
 /* force hits per node and direction: loop order of evalXds (kb, then xd). */
 static int force_hits(const pn_mesh *m, const int32_t *ncc, const pn_window_source *src,
                       const or_groups *g, or_hits *h) {
-  int64_t ne = (int64_t)m->n_nodes * 3;
-  h->start = (int64_t *)calloc((size_t)ne + 1, sizeof(int64_t));
-  if (!h->start) return or_fail(PN_ERR_ALLOC, "oracle: out of memory");
-  int64_t cap = 1024, cnt = 0;
-  h->sig = (int32_t *)malloc(sizeof(int32_t) * cap);
-  if (!h->sig) return or_fail(PN_ERR_ALLOC, "oracle: out of memory");
-  for (int32_t n = 0; n < m->n_nodes; n++) {
-    for (int dir = 0; dir < 3; dir++) {
-      h->start[(int64_t)n * 3 + dir] = cnt;
-      if (g->ngroups == 0) continue;
-      for (int kb = 0; kb < 8; kb++) {
-        int32_t c = ncc[(int64_t)n * 8 + kb];
-        if (c == -1) continue;
-        double cc[3];
-        cell_center(m, c, cc);
-        for (int32_t gi = 0; gi < g->ngroups; gi++) {
-          int32_t si = g->slot[gi * 3 + dir];
-          if (si < 0 || !window_at(&src[si], cc)) continue;
-          if (cnt == cap) {
-            cap *= 2;
-            int32_t *p = (int32_t *)realloc(h->sig, sizeof(int32_t) * cap);
-            if (!p) return or_fail(PN_ERR_ALLOC, "oracle: out of memory");
-            h->sig = p;
-          }
-          h->sig[cnt++] = si;
-        }
-      }
-    }
-  }
-  h->start[ne] = cnt;
-  return PN_OK;
+  return build_hits(m, ncc, src, g, 1, h);
 }
 
 /* moment hits per cell and Voigt component: loop order of evalMoments. */
 static int moment_hits(const pn_mesh *m, const pn_window_source *src, const or_groups *g,
                        or_hits *h) {
-  int64_t ne = (int64_t)m->n_cells * 6;
-  h->start = (int64_t *)calloc((size_t)ne + 1, sizeof(int64_t));
-  if (!h->start) return or_fail(PN_ERR_ALLOC, "oracle: out of memory");
-  int64_t cap = 1024, cnt = 0;
-  h->sig = (int32_t *)malloc(sizeof(int32_t) * cap);
-  if (!h->sig) return or_fail(PN_ERR_ALLOC, "oracle: out of memory");
-  for (int32_t c = 0; c < m->n_cells; c++) {
-    for (int comp = 0; comp < 6; comp++) {
-      h->start[(int64_t)c * 6 + comp] = cnt;
-      if (g->ngroups == 0) continue;
-      for (int kb = 0; kb < 8; kb++) {
-        int32_t q = m->hexes[(int64_t)c * 8 + kb];
-        double r[3] = {m->x[q], m->y[q], m->z[q]};
-        for (int32_t gi = 0; gi < g->ngroups; gi++) {
-          int32_t si = g->slot[gi * 6 + comp];
-          if (si < 0 || !window_at(&src[si], r)) continue;
-          if (cnt == cap) {
-            cap *= 2;
-            int32_t *p = (int32_t *)realloc(h->sig, sizeof(int32_t) * cap);
-            if (!p) return or_fail(PN_ERR_ALLOC, "oracle: out of memory");
-            h->sig = p;
-          }
-          h->sig[cnt++] = si;
-        }
-      }
-    }
-  }
-  h->start[ne] = cnt;
-  return PN_OK;
+  return build_hits(m, NULL, src, g, 0, h);
 }
 
 /* ---- operators (RightHex.hpp:100-192, 225-247) ---------------------------*/
@@ -381,7 +404,9 @@ static int model_setup(or_model *M, const pn_mesh *m, const pn_material *mat, do
      setupComms, then RightHex (nodePrep before cellPrep) */
   if ((rc = node_prep(m, M->ncc, M->dxn, M->dyn, M->dzn))) return rc;
   cell_prep(m, M->dxc, M->dyc, M->dzc);
+#pragma omp parallel for schedule(static)
   for (int32_t n = 0; n < m->n_nodes; n++) M->coef[n] = dt / field_at_node(&mat->density, M->ncc, n);
+#pragma omp parallel for schedule(static)
   for (int32_t c = 0; c < m->n_cells; c++)
     for (int k = 0; k < 21; k++) M->cij[(size_t)c * 21 + k] = field_at_cell(m, &mat->cij[k], c);
 
