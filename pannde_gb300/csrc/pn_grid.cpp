@@ -194,12 +194,20 @@ void grid_create(pn_solver *s) {
       ck(cudaMemsetAsync(s->S[b][k], 0, (size_t)gc * e, s->stream), "memset");
     }
   }
-  std::vector<double> coef((size_t)gn, 0.0);
-  for (int32_t u = 0; u < s->mesh.n_nodes; u++) coef[g.node_grid[u]] = s->mat.coef[u];
+  // every mesh node / cell has its own site: the scatters are race-free
+  const int32_t nn = s->mesh.n_nodes, nc = s->mesh.n_cells;
+  hvec<double> coef((size_t)gn);
+#pragma omp parallel for schedule(static)
+  for (int64_t q = 0; q < gn; q++) coef[q] = 0.0;
+#pragma omp parallel for schedule(static)
+  for (int32_t u = 0; u < nn; u++) coef[g.node_grid[u]] = s->mat.coef[u];
   s->d_coef = s->alloc<void>((size_t)gn * e);
   s->upload_real(s->d_coef, coef.data(), coef.size());
-  std::vector<uint8_t> gm((size_t)gc, (uint8_t)s->mat.n_mat);  // void row
-  for (int32_t c = 0; c < s->mesh.n_cells; c++) gm[g.cell_grid[c]] = (uint8_t)s->mat.cell_mat[c];
+  hvec<uint8_t> gm((size_t)gc);
+#pragma omp parallel for schedule(static)
+  for (int64_t q = 0; q < gc; q++) gm[q] = (uint8_t)s->mat.n_mat;  // void row
+#pragma omp parallel for schedule(static)
+  for (int32_t c = 0; c < nc; c++) gm[g.cell_grid[c]] = (uint8_t)s->mat.cell_mat[c];
   s->d_gmat = s->alloc<uint8_t>((size_t)gc);
   s->upload_raw(s->d_gmat, gm.data(), gm.size());
   std::vector<double> ct((size_t)(s->mat.n_mat + 1) * 36, 0.0);
@@ -232,7 +240,8 @@ void grid_create(pn_solver *s) {
       auto near = [](double a, double b) { return std::fabs(a - b) <= 1e-12 * std::fabs(b); };
       if (near(s->mesh.hy, h) && near(s->mesh.hz, h)) {
         const double g = 0.25 / h;
-        for (double &v : coef) v *= g;
+#pragma omp parallel for schedule(static)
+        for (int64_t q = 0; q < gn; q++) coef[q] *= g;
         for (double &v : ct) v *= g;
         s->upload_real(s->d_coef, coef.data(), coef.size());
         s->upload_real(s->d_ctab, ct.data(), ct.size());

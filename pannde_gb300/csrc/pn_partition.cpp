@@ -81,7 +81,7 @@ void rcb(const pn::MeshTables &t, std::vector<int32_t> &idx, int64_t lo, int64_t
     return;
   }
   double mn[3] = {1e308, 1e308, 1e308}, mx[3] = {-1e308, -1e308, -1e308};
-  const std::vector<double> *xyz[3] = {&t.x, &t.y, &t.z};
+  const pn::hvec<double> *xyz[3] = {&t.x, &t.y, &t.z};
   for (int64_t i = lo; i < hi; i++)
     for (int d = 0; d < 3; d++) {
       const double v = (*xyz[d])[(size_t)idx[(size_t)i]];
@@ -91,7 +91,7 @@ void rcb(const pn::MeshTables &t, std::vector<int32_t> &idx, int64_t lo, int64_t
   int ax = 0;
   for (int d = 1; d < 3; d++)
     if (mx[d] - mn[d] > mx[ax] - mn[ax]) ax = d;
-  const std::vector<double> &c = *xyz[ax];
+  const pn::hvec<double> &c = *xyz[ax];
   const int nl = np / 2;
   const int64_t cut = lo + (hi - lo) * nl / np;
   std::nth_element(idx.begin() + lo, idx.begin() + cut, idx.begin() + hi, [&](int32_t a, int32_t b) {

@@ -3,7 +3,10 @@
 // spacings must round as the reference's C++ does.
 #include "pn_setup.hpp"
 
+#include <omp.h>
+
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -15,6 +18,26 @@ namespace {
 [[noreturn]] void fail(int code, const std::string &msg) { throw SetupError{code, msg}; }
 
 bool near_equal(double a, double b) { return std::fabs(a - b) <= 1e-12 * std::fabs(b); }
+
+// *p = max(*p, v) / min(*p, v) when several threads update the same entry
+inline void atomic_max(int32_t *p, int32_t v) {
+  int32_t cur = __atomic_load_n(p, __ATOMIC_RELAXED);
+  while (cur < v && !__atomic_compare_exchange_n(p, &cur, v, true, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {
+  }
+}
+inline void atomic_min(int32_t *p, int32_t v) {
+  int32_t cur = __atomic_load_n(p, __ATOMIC_RELAXED);
+  while (cur > v && !__atomic_compare_exchange_n(p, &cur, v, true, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {
+  }
+}
+
+template <typename T>
+void fill_par(hvec<T> &v, size_t n, T value) {
+  v.resize(n);
+  T *p = v.data();
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < (int64_t)n; i++) p[i] = value;
+}
 }  // namespace
 
 void pinv_sym6(const double *a, double *out) {
@@ -80,32 +103,44 @@ void build_mesh_tables(const pn_mesh &m, MeshTables &t) {
   const int32_t nn = m.n_nodes, nc = m.n_cells;
   t.n_nodes = nn;
   t.n_cells = nc;
-  if (!all_finite(m.x, nn) || !all_finite(m.y, nn) || !all_finite(m.z, nn))
-    fail(PN_ERR_NOT_FINITE, "non-finite node coordinate");
-  t.x.assign(m.x, m.x + nn);
-  t.y.assign(m.y, m.y + nn);
-  t.z.assign(m.z, m.z + nn);
-  t.hex.assign(m.hexes, m.hexes + (size_t)nc * 8);
+  // copies, checks and tables are filled by parallel loops over nodes / cells
+  t.x.resize(nn);
+  t.y.resize(nn);
+  t.z.resize(nn);
+  t.owned.resize(nn);
+  bool finite = true;
+#pragma omp parallel for reduction(&& : finite) schedule(static)
+  for (int32_t n = 0; n < nn; n++) {
+    t.x[n] = m.x[n];
+    t.y[n] = m.y[n];
+    t.z[n] = m.z[n];
+    finite = finite && std::isfinite(m.x[n]) && std::isfinite(m.y[n]) && std::isfinite(m.z[n]);
+    t.owned[n] = m.node_owner ? (m.node_owner[n] == m.partition_id) : 1;
+  }
+  if (!finite) fail(PN_ERR_NOT_FINITE, "non-finite node coordinate");
   // HexMesh::setCell throws std::out_of_range for an invalid node id (the
   // first one in cell order is reported)
   {
-    const int64_t nh = (int64_t)t.hex.size();
+    const int64_t nh = (int64_t)nc * 8;
+    t.hex.resize((size_t)nh);
     int64_t bad = nh;
 #pragma omp parallel for reduction(min : bad) schedule(static)
-    for (int64_t k = 0; k < nh; k++)
-      if (t.hex[(size_t)k] < 0 || t.hex[(size_t)k] >= nn) bad = std::min(bad, k);
+    for (int64_t k = 0; k < nh; k++) {
+      const int32_t q = m.hexes[k];
+      t.hex[(size_t)k] = q;
+      if (q < 0 || q >= nn) bad = std::min(bad, k);
+    }
     if (bad < nh)
       fail(PN_ERR_RANGE, "invalid node id: Node count: " + std::to_string(nn) +
                              ", provided index: " + std::to_string(t.hex[(size_t)bad]));
   }
-  t.owned.assign(nn, 1);
-  if (m.node_owner)
-    for (int32_t n = 0; n < nn; n++) t.owned[n] = (m.node_owner[n] == m.partition_id);
 
-  // buildLinks: corner k of cell c -> slot k^6 of that node; later cells win
-  t.ncc.assign((size_t)nn * 8, -1);
+  // buildLinks: corner k of cell c -> slot k^6 of that node; later cells win,
+  // i.e. every slot holds the highest cell index that names it
+  fill_par(t.ncc, (size_t)nn * 8, int32_t(-1));
+#pragma omp parallel for schedule(static)
   for (int32_t c = 0; c < nc; c++)
-    for (int k = 0; k < 8; k++) t.ncc[(size_t)t.hex[(size_t)c * 8 + k] * 8 + (k ^ 6)] = c;
+    for (int k = 0; k < 8; k++) atomic_max(&t.ncc[(size_t)t.hex[(size_t)c * 8 + k] * 8 + (k ^ 6)], c);
 
   // nodePrep (RightHex.hpp:272-309): per axis, the extent of every corner of
   // every incident cell around the node.  Min / max are exact, so taking them
@@ -113,7 +148,7 @@ void build_mesh_tables(const pn_mesh &m, MeshTables &t) {
   // gives the same numbers with 8 reads per node instead of 64.  Nodes are
   // independent; the first node (in order) with a non-positive spacing
   // decides the error, as in the reference's loop.
-  std::vector<double> box((size_t)nc * 6);
+  hvec<double> box((size_t)nc * 6);
 #pragma omp parallel for schedule(static)
   for (int32_t c = 0; c < nc; c++) {
     double lo[3] = {1e308, 1e308, 1e308}, hi[3] = {-1e308, -1e308, -1e308};
@@ -220,8 +255,10 @@ double at_node(const pn_field &f, const MeshTables &t, int32_t n) {
   return v / 8.0;
 }
 
+using Row = std::array<uint64_t, 21>;  // bit patterns of a cell's 21 stiffness values
+
 struct RowHash {
-  size_t operator()(const std::vector<uint64_t> &r) const {
+  size_t operator()(const Row &r) const {
     uint64_t h = 1469598103934665603ull;
     for (uint64_t w : r) { h ^= w; h *= 1099511628211ull; }
     return (size_t)h;
@@ -240,29 +277,70 @@ void build_material_from_fields(const pn_material &mat, const MeshTables &t, dou
   check_field(mat.density, t, "density");
   for (int k = 0; k < 21; k++) check_field(mat.cij[k], t, "stiffness");
   out.coef.resize(t.n_nodes);
+#pragma omp parallel for schedule(static)
   for (int32_t n = 0; n < t.n_nodes; n++)
     out.coef[n] = t.owned[n] ? dt / at_node(mat.density, t, n) : 0.;
-  // de-duplicate the per-cell stiffness rows (bit patterns) into a table
-  std::unordered_map<std::vector<uint64_t>, int32_t, RowHash> ids;
-  out.cell_mat.resize(t.n_cells);
+  // De-duplicate the per-cell stiffness rows (bit patterns) into a table,
+  // numbered in order of first appearance.  Each thread numbers the rows of
+  // its contiguous run of cells in their order of first appearance there;
+  // merging the runs in cell order then numbers every row as one pass over
+  // all cells would.
+  const int32_t nc = t.n_cells;
+  out.cell_mat.resize(nc);
+  std::vector<std::vector<Row>> seen;  // [run] rows in order of first appearance
+#pragma omp parallel
+  {
+#pragma omp single
+    seen.resize((size_t)omp_get_num_threads());
+    const int nt = omp_get_num_threads(), r = omp_get_thread_num();
+    const int32_t c0 = (int32_t)((int64_t)nc * r / nt), c1 = (int32_t)((int64_t)nc * (r + 1) / nt);
+    std::unordered_map<Row, int32_t, RowHash> ids;
+    std::vector<Row> &rows = seen[(size_t)r];
+    Row key{}, last{};
+    int32_t last_id = -1;
+    for (int32_t c = c0; c < c1; c++) {
+      for (int k = 0; k < 21; k++) {
+        const double v = at_cell(mat.cij[k], t, c);
+        std::memcpy(&key[k], &v, 8);
+      }
+      if (last_id < 0 || key != last) {  // neighbouring cells mostly share a row
+        auto it = ids.find(key);
+        if (it == ids.end()) {
+          last_id = (int32_t)rows.size();
+          ids.emplace(key, last_id);
+          rows.push_back(key);
+        } else {
+          last_id = it->second;
+        }
+        last = key;
+      }
+      out.cell_mat[c] = last_id;  // numbered within the run for now
+    }
+  }
+  std::unordered_map<Row, int32_t, RowHash> ids;
+  std::vector<std::vector<int32_t>> remap(seen.size());
   out.c36.clear();
-  std::vector<uint64_t> key(21);
-  double row[21];
-  for (int32_t c = 0; c < t.n_cells; c++) {
-    for (int k = 0; k < 21; k++) {
-      row[k] = at_cell(mat.cij[k], t, c);
-      std::memcpy(&key[k], &row[k], 8);
+  for (size_t r = 0; r < seen.size(); r++)
+    for (const Row &key : seen[r]) {
+      auto it = ids.find(key);
+      int32_t id;
+      if (it == ids.end()) {
+        id = (int32_t)ids.size();
+        ids.emplace(key, id);
+        double row[21];
+        std::memcpy(row, key.data(), sizeof(row));
+        out.c36.resize(out.c36.size() + 36);
+        expand36(row, &out.c36[(size_t)id * 36]);
+      } else {
+        id = it->second;
+      }
+      remap[r].push_back(id);
     }
-    auto it = ids.find(key);
-    if (it == ids.end()) {
-      const int32_t id = (int32_t)ids.size();
-      ids.emplace(key, id);
-      out.c36.resize(out.c36.size() + 36);
-      expand36(row, &out.c36[(size_t)id * 36]);
-      out.cell_mat[c] = id;
-    } else {
-      out.cell_mat[c] = it->second;
-    }
+  const int nt = (int)seen.size();
+#pragma omp parallel for schedule(static)
+  for (int r = 0; r < nt; r++) {
+    const int32_t c0 = (int32_t)((int64_t)nc * r / nt), c1 = (int32_t)((int64_t)nc * (r + 1) / nt);
+    for (int32_t c = c0; c < c1; c++) out.cell_mat[c] = remap[(size_t)r][(size_t)out.cell_mat[c]];
   }
   out.n_mat = (int32_t)ids.size();
 }
@@ -273,14 +351,20 @@ void build_material_from_table(const pn_material_table &mat, const MeshTables &t
     fail(PN_ERR_INVALID, "material table");
   if (!all_finite(mat.density, mat.n_materials) || !all_finite(mat.cij, (int64_t)mat.n_materials * 21))
     fail(PN_ERR_NOT_FINITE, "non-finite value in material table");
-  for (int32_t c = 0; c < t.n_cells; c++)
-    if (mat.cell_material[c] < 0 || mat.cell_material[c] >= mat.n_materials)
-      fail(PN_ERR_RANGE, "cell material id out of range");
+  out.cell_mat.resize(t.n_cells);
+  bool in_range = true;
+#pragma omp parallel for reduction(&& : in_range) schedule(static)
+  for (int32_t c = 0; c < t.n_cells; c++) {
+    const int32_t id = mat.cell_material[c];
+    out.cell_mat[c] = id;
+    in_range = in_range && id >= 0 && id < mat.n_materials;
+  }
+  if (!in_range) fail(PN_ERR_RANGE, "cell material id out of range");
   out.n_mat = mat.n_materials;
   out.c36.resize((size_t)out.n_mat * 36);
   for (int32_t i = 0; i < out.n_mat; i++) expand36(mat.cij + (size_t)i * 21, &out.c36[(size_t)i * 36]);
-  out.cell_mat.assign(mat.cell_material, mat.cell_material + t.n_cells);
   out.coef.resize(t.n_nodes);
+#pragma omp parallel for schedule(static)
   for (int32_t n = 0; n < t.n_nodes; n++) {
     double v = 0.0;
     for (int k = 0; k < 8; k++) {
@@ -486,12 +570,13 @@ void detect_grid(const MeshTables &t, GridMap &g, double max_void_fraction) {
     y0 = std::min(y0, t.y[n]);
     z0 = std::min(z0, t.z[n]);
   }
-  std::vector<int64_t> gi(t.n_nodes), gj(t.n_nodes), gk(t.n_nodes);
+  hvec<int32_t> gi(t.n_nodes), gj(t.n_nodes), gk(t.n_nodes);  // lattice coordinates, < 2^20
   int64_t mi = 0, mj = 0, mk = 0;
-  auto lattice = [](double v, double o, double h, int64_t &out) {
+  auto lattice = [](double v, double o, double h, int32_t &out) {
     const double f = (v - o) / h;
-    out = (int64_t)std::llround(f);
-    return std::fabs(f - (double)out) <= 1e-6 && out >= 0 && out < (1 << 20);
+    const int64_t q = (int64_t)std::llround(f);
+    out = (int32_t)q;
+    return std::fabs(f - (double)q) <= 1e-6 && q >= 0 && q < (1 << 20);
   };
   bool on = true;
 #pragma omp parallel for reduction(max : mi, mj, mk) reduction(&& : on) schedule(static)
@@ -500,9 +585,9 @@ void detect_grid(const MeshTables &t, GridMap &g, double max_void_fraction) {
                     lattice(t.z[n], z0, t.hz, gk[n]);
     on = on && ok;
     if (!ok) continue;
-    mi = std::max(mi, gi[n]);
-    mj = std::max(mj, gj[n]);
-    mk = std::max(mk, gk[n]);
+    mi = std::max<int64_t>(mi, gi[n]);
+    mj = std::max<int64_t>(mj, gj[n]);
+    mk = std::max<int64_t>(mk, gk[n]);
   }
   if (!on) {
     g.why = "node off the lattice";
@@ -513,7 +598,7 @@ void detect_grid(const MeshTables &t, GridMap &g, double max_void_fraction) {
     return;
   }
   const int64_t nx = mi, ny = mj, nz = mk;
-  const int64_t gnodes = (nx + 1) * (ny + 1) * (nz + 1), gcells = nx * ny * nz;
+  const int64_t gcells = nx * ny * nz;
   const int64_t pnx = GridMap::node_pitch(nx), pcx = GridMap::cell_pitch(nx);
   if (pnx * (ny + 1) * (nz + 1) >= (int64_t(1) << 31) - 1) {
     g.why = "lattice too large for 32-bit indices";
@@ -531,16 +616,39 @@ void detect_grid(const MeshTables &t, GridMap &g, double max_void_fraction) {
   g.node_grid.resize(t.n_nodes);
 #pragma omp parallel for schedule(static)
   for (int32_t n = 0; n < t.n_nodes; n++) g.node_grid[n] = g.node_at(gi[n], gj[n], gk[n]);
-  // the first node on a site keeps it; later ones get tail slots (split sites)
-  std::vector<int32_t> first((size_t)g.node_sites(), -1);
-  std::vector<uint8_t> split((size_t)g.node_sites(), 0);
-  for (int32_t n = 0; n < t.n_nodes; n++) {
-    const int64_t site = g.node_grid[n];
-    if (first[(size_t)site] < 0) {
-      first[(size_t)site] = n;
-    } else {
-      split[(size_t)site] = 1;
-      g.node_grid[n] = g.node_sites() + g.n_extra++;
+  // The first node (in node order) on a site keeps it; later ones get tail
+  // slots, numbered in node order (split sites).  Parallel: the lowest node
+  // per site, then per contiguous run of nodes the count of later ones, a
+  // prefix sum over the runs, and the numbering within each run.
+  hvec<int32_t> first;
+  fill_par(first, (size_t)g.node_sites(), INT32_MAX);
+  hvec<uint8_t> split;
+  fill_par(split, (size_t)g.node_sites(), uint8_t(0));
+  const int32_t nn = t.n_nodes;
+#pragma omp parallel for schedule(static)
+  for (int32_t n = 0; n < nn; n++) atomic_min(&first[(size_t)g.node_grid[n]], n);
+  const int runs = std::max(1, std::min(omp_get_max_threads() * 4, nn / 4096 + 1));
+  std::vector<int64_t> later((size_t)runs + 1, 0);
+#pragma omp parallel for schedule(static)
+  for (int r = 0; r < runs; r++) {
+    const int32_t n0 = (int32_t)((int64_t)nn * r / runs), n1 = (int32_t)((int64_t)nn * (r + 1) / runs);
+    int64_t cnt = 0;
+    for (int32_t n = n0; n < n1; n++) cnt += first[(size_t)g.node_grid[n]] != n;
+    later[(size_t)r + 1] = cnt;
+  }
+  for (int r = 0; r < runs; r++) later[(size_t)r + 1] += later[(size_t)r];
+  g.n_extra = later[(size_t)runs];
+  if (g.n_extra > 0) {
+#pragma omp parallel for schedule(static)
+    for (int r = 0; r < runs; r++) {
+      const int32_t n0 = (int32_t)((int64_t)nn * r / runs), n1 = (int32_t)((int64_t)nn * (r + 1) / runs);
+      int64_t e = later[(size_t)r];
+      for (int32_t n = n0; n < n1; n++) {
+        const int64_t site = g.node_grid[n];
+        if (first[(size_t)site] == n) continue;
+        __atomic_store_n(&split[(size_t)site], (uint8_t)1, __ATOMIC_RELAXED);
+        g.node_grid[n] = g.node_sites() + e++;
+      }
     }
   }
   if (g.n_extra > t.n_nodes / 8) {
@@ -565,14 +673,15 @@ void detect_grid(const MeshTables &t, GridMap &g, double max_void_fraction) {
     g.why = "cell is not a lattice box in corner order";
     return;
   }
-  std::vector<uint8_t> ctaken((size_t)g.cell_sites(), 0);
-  for (int32_t c = 0; c < t.n_cells; c++) {
-    uint8_t &site = ctaken[(size_t)g.cell_grid[c]];
-    if (site) {
-      g.why = "two cells on one lattice site";
-      return;
-    }
-    site = 1;
+  hvec<uint8_t> ctaken;
+  fill_par(ctaken, (size_t)g.cell_sites(), uint8_t(0));
+  bool twice = false;
+#pragma omp parallel for reduction(|| : twice) schedule(static)
+  for (int32_t c = 0; c < t.n_cells; c++)
+    twice = __atomic_exchange_n(&ctaken[(size_t)g.cell_grid[c]], (uint8_t)1, __ATOMIC_RELAXED) || twice;
+  if (twice) {
+    g.why = "two cells on one lattice site";
+    return;
   }
   if (g.n_extra > 0) {  // copies and fix cells
     g.copy_of_node.assign((size_t)t.n_nodes, -1);
@@ -601,10 +710,10 @@ void detect_grid(const MeshTables &t, GridMap &g, double max_void_fraction) {
     }
   }
   g.col_top.assign((size_t)nx * ny, 0);
+#pragma omp parallel for schedule(static)
   for (int32_t c = 0; c < t.n_cells; c++) {
     const int64_t q = g.cell_grid[c], i = q % pcx, j = (q / pcx) % ny, k = q / (pcx * ny);
-    int32_t &top = g.col_top[(size_t)(j * nx + i)];
-    top = std::max(top, (int32_t)k + 1);
+    atomic_max(&g.col_top[(size_t)(j * nx + i)], (int32_t)k + 1);
   }
   g.ok = true;
 }

@@ -14,7 +14,10 @@
 // predicates and spacings round exactly as the reference's C++ does.
 #pragma once
 #include <cstdint>
+#include <memory>
 #include <string>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "../../include/pannde_gb300.h"
@@ -26,6 +29,32 @@ struct SetupError {
   std::string msg;
 };
 
+// Allocator that leaves elements default-initialised (for numbers: not
+// written) when a vector is sized, so that the parallel loop filling a large
+// table is also the first to touch its pages: the page faults of a
+// multi-gigabyte table are then spread over the threads instead of taken by
+// one zero-filling thread.
+template <typename T>
+struct UninitAlloc : std::allocator<T> {
+  template <typename U>
+  struct rebind {
+    using other = UninitAlloc<U>;
+  };
+  UninitAlloc() noexcept = default;
+  template <typename U>
+  UninitAlloc(const UninitAlloc<U> &) noexcept {}
+  template <typename U>
+  void construct(U *p) noexcept(std::is_nothrow_default_constructible<U>::value) {
+    ::new ((void *)p) U;
+  }
+  template <typename U, typename... A>
+  void construct(U *p, A &&...a) {
+    ::new ((void *)p) U(std::forward<A>(a)...);
+  }
+};
+template <typename T>
+using hvec = std::vector<T, UninitAlloc<T>>;
+
 // Voigt (i,j) -> index into the 21 unique entries.
 inline int cij_index(int i, int j) {
   if (i > j) { int t = i; i = j; j = t; }
@@ -34,11 +63,11 @@ inline int cij_index(int i, int j) {
 
 struct MeshTables {
   int32_t n_nodes = 0, n_cells = 0;
-  std::vector<double> x, y, z;
-  std::vector<int32_t> hex;       // [n_cells*8]
-  std::vector<int32_t> ncc;       // [n_nodes*8], -1 = none
-  std::vector<uint8_t> owned;     // [n_nodes]
-  std::vector<double> dxc, dyc, dzc, dxn, dyn, dzn;
+  hvec<double> x, y, z;
+  hvec<int32_t> hex;       // [n_cells*8]
+  hvec<int32_t> ncc;       // [n_nodes*8], -1 = none
+  hvec<uint8_t> owned;     // [n_nodes]
+  hvec<double> dxc, dyc, dzc, dxn, dyn, dzn;
   bool uniform = false;
   double hx = 0, hy = 0, hz = 0;
 };
@@ -49,8 +78,8 @@ void build_mesh_tables(const pn_mesh &m, MeshTables &t);
 struct MaterialTables {
   int32_t n_mat = 0;
   std::vector<double> c36;        // [n_mat][36] raw stiffness (C[i][j])
-  std::vector<int32_t> cell_mat;  // [n_cells]
-  std::vector<double> coef;       // [n_nodes] dt / rho_node, 0 = not owned
+  hvec<int32_t> cell_mat;         // [n_cells]
+  hvec<double> coef;              // [n_nodes] dt / rho_node, 0 = not owned
 };
 
 // From reference-style fields (density + 21 Cij, NODE/CELL/CONSTANT).
@@ -114,8 +143,8 @@ struct GridMap {
   std::string why;               // reason when not a grid
   int32_t nx = 0, ny = 0, nz = 0;  // cells per axis
   int32_t pnx = 0, pcx = 0;        // row pitch (sites) of node / cell buffers
-  std::vector<int64_t> node_grid;  // mesh node -> grid node
-  std::vector<int64_t> cell_grid;  // mesh cell -> grid cell
+  hvec<int64_t> node_grid;         // mesh node -> grid node
+  hvec<int64_t> cell_grid;         // mesh cell -> grid cell
   std::vector<int32_t> col_top;    // [ny][nx] 1 + the highest solid cell layer of column (i, j), 0 if none
   int64_t n_extra = 0;                // extra copies (tail slots node_sites() + e)
   std::vector<int32_t> copy_node;     // mesh node of every copy (nodes of split sites), ascending

@@ -190,15 +190,17 @@ struct pn_solver {
   void upload_real(void *dst, const double *src_, size_t n) {
     if (n == 0) return;
     if (is_df64()) {
-      std::vector<float> tmp(2 * n);
-      for (size_t i = 0; i < n; i++) pn::split_df(src_[i], tmp[2 * i], tmp[2 * i + 1]);
+      pn::hvec<float> tmp(2 * n);
+#pragma omp parallel for schedule(static)
+      for (int64_t i = 0; i < (int64_t)n; i++) pn::split_df(src_[i], tmp[2 * i], tmp[2 * i + 1]);
       pn::ck(cudaMemcpyAsync(dst, tmp.data(), n * 8, cudaMemcpyHostToDevice, stream), "upload");
       pn::ck(cudaStreamSynchronize(stream), "upload sync");
     } else if (esz == 8) {
       pn::ck(cudaMemcpyAsync(dst, src_, n * 8, cudaMemcpyHostToDevice, stream), "upload");
     } else {
-      std::vector<float> tmp(n);
-      for (size_t i = 0; i < n; i++) tmp[i] = (float)src_[i];
+      pn::hvec<float> tmp(n);
+#pragma omp parallel for schedule(static)
+      for (int64_t i = 0; i < (int64_t)n; i++) tmp[i] = (float)src_[i];
       pn::ck(cudaMemcpyAsync(dst, tmp.data(), n * 4, cudaMemcpyHostToDevice, stream), "upload");
       pn::ck(cudaStreamSynchronize(stream), "upload sync");
     }

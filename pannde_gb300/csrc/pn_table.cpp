@@ -40,12 +40,14 @@ void table_create(pn_solver *s) {
     for (double &v : ct) v *= s->dt;  // fast forms fold dt into C
   s->upload_real(s->d_ctab, ct.data(), ct.size());
   if (per_elem) {
-    std::vector<double> g((size_t)nn * 3), h((size_t)nc * 3);
-    const std::vector<double> *dn[3] = {&s->mesh.dxn, &s->mesh.dyn, &s->mesh.dzn};
-    const std::vector<double> *dc[3] = {&s->mesh.dxc, &s->mesh.dyc, &s->mesh.dzc};
+    hvec<double> g((size_t)nn * 3), h((size_t)nc * 3);
+    const double *dn[3] = {s->mesh.dxn.data(), s->mesh.dyn.data(), s->mesh.dzn.data()};
+    const double *dc[3] = {s->mesh.dxc.data(), s->mesh.dyc.data(), s->mesh.dzc.data()};
     for (int a = 0; a < 3; a++) {
-      for (int32_t n = 0; n < nn; n++) g[(size_t)a * nn + n] = exact ? (*dn[a])[n] : 0.25 / (*dn[a])[n];
-      for (int32_t c = 0; c < nc; c++) h[(size_t)a * nc + c] = exact ? (*dc[a])[c] : 0.25 / (*dc[a])[c];
+#pragma omp parallel for schedule(static)
+      for (int32_t n = 0; n < nn; n++) g[(size_t)a * nn + n] = exact ? dn[a][n] : 0.25 / dn[a][n];
+#pragma omp parallel for schedule(static)
+      for (int32_t c = 0; c < nc; c++) h[(size_t)a * nc + c] = exact ? dc[a][c] : 0.25 / dc[a][c];
     }
     s->d_gnode = s->alloc<void>(g.size() * e);
     s->d_gcell = s->alloc<void>(h.size() * e);

@@ -1,0 +1,69 @@
+// setup_digest.cpp -- builds every host table of pn_setup.cpp (links,
+// spacings, material tables, voxel-grid map with split sites) for one mesh
+// and returns a 64-bit FNV-1a digest of each array, so that a test can check
+// the tables bit for bit across thread counts.  Compiled by
+// tests/test_setup_threads_cpu.py together with pn_setup.cpp.
+#include <cstdio>
+
+#include "pn_setup.hpp"
+
+namespace {
+uint64_t fnv(const void *p, size_t n, uint64_t h = 1469598103934665603ull) {
+  const unsigned char *b = (const unsigned char *)p;
+  for (size_t i = 0; i < n; i++) {
+    h ^= b[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+template <class V>
+uint64_t digest_of(const V &v) {
+  return fnv(v.data(), v.size() * sizeof(v[0]), 1469598103934665603ull ^ v.size());
+}
+}  // namespace
+
+// Returns the number of digests written to out (at most 40), or -1 with the
+// error code and message in msg when setup rejects the input.
+extern "C" int setup_digest(const pn_mesh *m, const pn_material *mat, const pn_material_table *tab,
+                            double dt, uint64_t *out, char *msg, int msg_len) {
+  int i = 0;
+  msg[0] = 0;
+  try {
+    pn::MeshTables t;
+    pn::MaterialTables mt;
+    pn::GridMap g;
+    pn::build_mesh_tables(*m, t);
+    if (mat) pn::build_material_from_fields(*mat, t, dt, mt);
+    else pn::build_material_from_table(*tab, t, dt, mt);
+    pn::detect_grid(t, g, 0.95);
+    for (const auto *v : {&t.x, &t.y, &t.z, &t.dxc, &t.dyc, &t.dzc, &t.dxn, &t.dyn, &t.dzn, &mt.coef})
+      out[i++] = digest_of(*v);
+    out[i++] = digest_of(t.hex);
+    out[i++] = digest_of(t.ncc);
+    out[i++] = digest_of(t.owned);
+    out[i++] = (uint64_t)t.uniform;
+    out[i++] = fnv(&t.hx, 8) ^ fnv(&t.hy, 8) ^ fnv(&t.hz, 8);
+    out[i++] = (uint64_t)mt.n_mat;
+    out[i++] = digest_of(mt.c36);
+    out[i++] = digest_of(mt.cell_mat);
+    out[i++] = (uint64_t)g.ok;
+    out[i++] = fnv(g.why.data(), g.why.size());
+    out[i++] = ((uint64_t)g.nx << 40) ^ ((uint64_t)g.ny << 20) ^ (uint64_t)g.nz;
+    if (g.ok) {
+      out[i++] = digest_of(g.node_grid);
+      out[i++] = digest_of(g.cell_grid);
+      out[i++] = digest_of(g.col_top);
+      out[i++] = (uint64_t)g.n_extra;
+      out[i++] = digest_of(g.copy_node);
+      out[i++] = digest_of(g.copy_site);
+      out[i++] = digest_of(g.copy_mask);
+      out[i++] = digest_of(g.copy_of_node);
+      out[i++] = digest_of(g.fix_cell);
+      out[i++] = digest_of(g.fix_of_cell);
+    }
+    return i;
+  } catch (const pn::SetupError &e) {
+    snprintf(msg, (size_t)msg_len, "%d %s", e.code, e.msg.c_str());
+    return -1;
+  }
+}
