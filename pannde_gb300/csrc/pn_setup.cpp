@@ -443,6 +443,26 @@ void push_entry(std::vector<SourceEntry> &out, bool exact, int32_t elem, int32_t
   out.push_back(SourceEntry{elem, comp, sig, 0.125});
 }
 
+// Runs body(e, list) for the elements e in [0, n) in contiguous runs on the
+// threads, each run appending to a list of its own, and concatenates the lists
+// in run order: the entries come out in element order, as from one serial
+// loop (push_entry only merges entries of the same element, which never
+// straddle two runs).
+template <typename F>
+void entries_by_runs(int32_t n, std::vector<SourceEntry> &out, F body) {
+  const int runs = std::max(1, std::min(omp_get_max_threads() * 4, n / 4096 + 1));
+  std::vector<std::vector<SourceEntry>> part((size_t)runs);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int r = 0; r < runs; r++) {
+    const int32_t e0 = (int32_t)((int64_t)n * r / runs), e1 = (int32_t)((int64_t)n * (r + 1) / runs);
+    for (int32_t e = e0; e < e1; e++) body(e, part[(size_t)r]);
+  }
+  size_t total = out.size();
+  for (auto &p : part) total += p.size();
+  out.reserve(total);
+  for (auto &p : part) out.insert(out.end(), p.begin(), p.end());
+}
+
 }  // namespace
 
 void build_source_entries(const MeshTables &t, const std::vector<pn_window_source> &src, bool exact,
@@ -464,7 +484,7 @@ void build_source_entries(const MeshTables &t, const std::vector<pn_window_sourc
 
   if (ngf > 0) {
     // cell centres, HostRSGTDUT::cellcenter order (corner order, += 0.125*pt)
-    std::vector<double> cc((size_t)t.n_cells * 3);
+    hvec<double> cc((size_t)t.n_cells * 3);
 #pragma omp parallel for schedule(static)
     for (int32_t c = 0; c < t.n_cells; c++) {
       double p[3] = {0., 0., 0.};
@@ -486,37 +506,39 @@ void build_source_entries(const MeshTables &t, const std::vector<pn_window_sourc
         fsrc.push_back((int32_t)i);
       }
     const size_t nf = fsrc.size();
-    std::vector<uint8_t> hit((size_t)t.n_cells * nf, 0);
-    std::vector<uint8_t> any_cell(t.n_cells, 0);
+    hvec<uint8_t> hit((size_t)t.n_cells * nf);
+    hvec<uint8_t> any_cell(t.n_cells);
 #pragma omp parallel for schedule(static)
-    for (int32_t c = 0; c < t.n_cells; c++)
+    for (int32_t c = 0; c < t.n_cells; c++) {
+      uint8_t any = 0;
       for (size_t l = 0; l < nf; l++) {
         const int32_t i = fsrc[l];
         const uint8_t *mk = mask_of(i);
-        if (mk ? mk[c] != 0 : window_at(src[i], &cc[(size_t)c * 3])) {
-          hit[(size_t)c * nf + l] = 1;
-          any_cell[c] = 1;
-        }
+        const uint8_t in = (mk ? mk[c] != 0 : window_at(src[i], &cc[(size_t)c * 3])) ? 1 : 0;
+        hit[(size_t)c * nf + l] = in;
+        any |= in;
       }
+      any_cell[c] = any;
+    }
     // evalXds loop order per node: dir, then slot kb, then transducer g
-    for (int32_t n = 0; n < t.n_nodes; n++) {
-      if (!t.owned[n]) continue;
+    entries_by_runs(t.n_nodes, force, [&](int32_t n, std::vector<SourceEntry> &list) {
+      if (!t.owned[n]) return;
       bool any = false;
       for (int kb = 0; kb < 8 && !any; kb++) {
         const int32_t c = t.ncc[(size_t)n * 8 + kb];
         any = (c != -1) && any_cell[c];
       }
-      if (!any) continue;
+      if (!any) return;
       for (int dir = 0; dir < 3; dir++)
         for (int kb = 0; kb < 8; kb++) {
           const int32_t c = t.ncc[(size_t)n * 8 + kb];
           if (c == -1 || !any_cell[c]) continue;
           for (int32_t gi = 0; gi < ngf; gi++) {
             const int32_t si = fslot[(size_t)gi * 3 + dir];
-            if (si >= 0 && hit[(size_t)c * nf + flocal[si]]) push_entry(force, exact, n, dir, si);
+            if (si >= 0 && hit[(size_t)c * nf + flocal[si]]) push_entry(list, exact, n, dir, si);
           }
         }
-    }
+    });
   }
   if (ngm > 0) {
     std::vector<int32_t> msrc, mlocal(src.size(), -1);
@@ -526,34 +548,36 @@ void build_source_entries(const MeshTables &t, const std::vector<pn_window_sourc
         msrc.push_back((int32_t)i);
       }
     const size_t nm = msrc.size();
-    std::vector<uint8_t> hit((size_t)t.n_nodes * nm, 0);
-    std::vector<uint8_t> any_node(t.n_nodes, 0);
+    hvec<uint8_t> hit((size_t)t.n_nodes * nm);
+    hvec<uint8_t> any_node(t.n_nodes);
+#pragma omp parallel for schedule(static)
     for (int32_t n = 0; n < t.n_nodes; n++) {
       const double r[3] = {t.x[n], t.y[n], t.z[n]};
+      uint8_t any = 0;
       for (size_t l = 0; l < nm; l++) {
         const int32_t i = msrc[l];
         const uint8_t *mk = mask_of(i);
-        if (mk ? mk[n] != 0 : window_at(src[i], r)) {
-          hit[(size_t)n * nm + l] = 1;
-          any_node[n] = 1;
-        }
+        const uint8_t in = (mk ? mk[n] != 0 : window_at(src[i], r)) ? 1 : 0;
+        hit[(size_t)n * nm + l] = in;
+        any |= in;
       }
+      any_node[n] = any;
     }
     // evalMoments loop order per cell: component, then corner kb, then tensor g
-    for (int32_t c = 0; c < t.n_cells; c++) {
+    entries_by_runs(t.n_cells, moment, [&](int32_t c, std::vector<SourceEntry> &list) {
       bool any = false;
       for (int kb = 0; kb < 8 && !any; kb++) any = any_node[t.hex[(size_t)c * 8 + kb]];
-      if (!any) continue;
+      if (!any) return;
       for (int comp = 0; comp < 6; comp++)
         for (int kb = 0; kb < 8; kb++) {
           const int32_t q = t.hex[(size_t)c * 8 + kb];
           if (!any_node[q]) continue;
           for (int32_t gi = 0; gi < ngm; gi++) {
             const int32_t si = mslot[(size_t)gi * 6 + comp];
-            if (si >= 0 && hit[(size_t)q * nm + mlocal[si]]) push_entry(moment, exact, c, comp, si);
+            if (si >= 0 && hit[(size_t)q * nm + mlocal[si]]) push_entry(list, exact, c, comp, si);
           }
         }
-    }
+    });
   }
 }
 

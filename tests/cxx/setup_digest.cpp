@@ -1,7 +1,7 @@
 // setup_digest.cpp -- builds every host table of pn_setup.cpp (links,
-// spacings, material tables, voxel-grid map with split sites) for one mesh
-// and returns a 64-bit FNV-1a digest of each array, so that a test can check
-// the tables bit for bit across thread counts.  Compiled by
+// spacings, material tables, voxel-grid map with split sites, source
+// entries) for one mesh and returns a 64-bit FNV-1a digest of each array, so
+// that a test can check the tables bit for bit across thread counts.  Compiled by
 // tests/test_setup_threads_cpu.py together with pn_setup.cpp.
 #include <cstdio>
 
@@ -62,6 +62,39 @@ extern "C" int setup_digest(const pn_mesh *m, const pn_material *mat, const pn_m
       out[i++] = digest_of(g.fix_of_cell);
     }
     return i;
+  } catch (const pn::SetupError &e) {
+    snprintf(msg, (size_t)msg_len, "%d %s", e.code, e.msg.c_str());
+    return -1;
+  }
+}
+
+// Source entries (build_source_entries) of n window sources: the force and
+// moment entry counts and a digest of each list (element, component, source,
+// weight); -1 with the error in msg when setup rejects the input.
+extern "C" int setup_digest_sources(const pn_mesh *m, const pn_window_source *src, int n, int exact,
+                                    uint64_t *out, char *msg, int msg_len) {
+  msg[0] = 0;
+  try {
+    pn::MeshTables t;
+    pn::build_mesh_tables(*m, t);
+    std::vector<pn_window_source> all(src, src + n);
+    std::vector<pn::SourceEntry> fe, me;
+    pn::build_source_entries(t, all, exact != 0, fe, me);
+    auto digest_entries = [](const std::vector<pn::SourceEntry> &v) {
+      uint64_t h = 1469598103934665603ull;
+      for (const pn::SourceEntry &e : v) {
+        h = fnv(&e.elem, 4, h);
+        h = fnv(&e.comp, 4, h);
+        h = fnv(&e.sig, 4, h);
+        h = fnv(&e.w, 8, h);
+      }
+      return h;
+    };
+    out[0] = fe.size();
+    out[1] = me.size();
+    out[2] = digest_entries(fe);
+    out[3] = digest_entries(me);
+    return 4;
   } catch (const pn::SetupError &e) {
     snprintf(msg, (size_t)msg_len, "%d %s", e.code, e.msg.c_str());
     return -1;

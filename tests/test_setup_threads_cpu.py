@@ -3,7 +3,8 @@
 pn_setup.cpp builds the links (HexMesh::buildLinks, "later cells win"), the
 spacings (RightHex nodePrep / cellPrep, first bad node reported), the
 de-duplicated material table (rows numbered in order of first appearance)
-and the voxel-grid map (split sites numbered in node order) with OpenMP
+the voxel-grid map (split sites numbered in node order) and the source
+entries (concatenated per run of elements, in element order) with OpenMP
 loops.  tests/cxx/setup_digest.cpp digests every table; the digests and the
 error messages must be identical with 1 thread and with several, on voxel
 meshes with cracks as disconnected faces, fluid columns, removed slabs,
@@ -40,6 +41,13 @@ def digest(c, fields, mesh=None):
                          ctypes.byref(tab) if tab else None, ctypes.c_double(c.dt), out, msg, 256)
     return [n, [str(v) for v in out[:max(n, 0)]], msg.value.decode()]
 
+def digest_sources(mesh, srcs, exact):
+    m, k1 = mesh.as_struct()
+    st, k2 = cases.sources_struct(srcs)
+    out = (ctypes.c_uint64 * 4)(); msg = ctypes.create_string_buffer(256)
+    n = lib.setup_digest_sources(ctypes.byref(m), st, len(srcs), exact, out, msg, 256)
+    return [n, [str(v) for v in out[:max(n, 0)]], msg.value.decode()]
+
 res = {}
 small = cases.al_plate_case(nx=24, ny=20, nz=6, nsteps=4)
 m = small.mesh
@@ -70,6 +78,17 @@ for fields in (0, 1):
     res[f"owners-{fields}"] = digest(small, fields, owners)
     res[f"isolated-{fields}"] = digest(small, fields, iso)
     res[f"bad-id-{fields}"] = digest(small, fields, cases.HexMesh(m.x, m.y, m.z, bad_id))
+F, M = cases.N.PN_SOURCE_FORCE, cases.N.PN_SOURCE_MOMENT
+zt, h, s0 = m.z.max(), 0.1e-3, small.sources[0]
+mixed = [cases.WindowSource(F, g, d, (1e-3 + g * 0.8e-3, 1e-3, zt), 0.9e-3, h, s0.times, s0.values)
+         for g in range(2) for d in range(3)]
+mixed += [cases.WindowSource(M, 0, k, (1.2e-3, 1e-3, zt), 0.7e-3, h, s0.times, s0.values) for k in range(6)]
+for exact in (0, 1):
+    res[f"sources-mixed-{exact}"] = digest_sources(m, mixed, exact)
+    res[f"sources-owners-{exact}"] = digest_sources(owners, mixed, exact)
+    for wc in (False, True):
+        c = cases.bracket_case(200, nsteps=4, water_column=wc, scale=0.4)
+        res[f"sources-bracket-{wc}-{exact}"] = digest_sources(c.mesh, c.sources, exact)
 print(json.dumps(res))
 '''
 
@@ -101,5 +120,6 @@ def test_host_tables_independent_of_thread_count(digest_lib):
     assert any(int(v[1][-7]) > 0 for k, v in one.items() if "faces" in k and v[0] > 30)
     assert one["isolated-0"][2].startswith("2 DX") and one["bad-id-1"][2].startswith("3 invalid node id")
     assert one["duplicated-0"][0] > 0 and one["materials-1"][0] > 0
+    assert all(int(v[1][0]) > 0 and int(v[1][1]) > 0 for k, v in one.items() if k.startswith("sources-mixed"))
     for threads in (3, 8):
         assert run_with_threads(digest_lib, threads) == one
