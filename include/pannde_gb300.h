@@ -77,7 +77,8 @@ enum pn_form {
      table form */
   PN_FORM_AUTO = 0,
   /* connectivity tables on the device (cell -> 8 nodes, node -> 8 cell
-     slots), two kernels per step; any hex mesh */
+     slots), two kernels per step; any hex mesh of at most 715,827,882 nodes
+     and cells (PN_ERR_INVALID above that) */
   PN_FORM_TABLE = 0x100,
   /* implicit lattice indices, one fused kernel per step, double-buffered
      state; PN_ERR_INVALID when the mesh is not a voxel grid */

@@ -114,12 +114,18 @@ bool split_mode(int32_t mode, int &precision, int &form) {
 // the form a mesh gets; throws when PN_FORM_GRID is asked of a non-grid mesh
 int choose_form(const pn::MeshTables &m, const pn::MaterialTables &mt, int precision, int form,
                 pn::GridMap &g) {
-  if (form == PN_FORM_TABLE) return PN_FORM_TABLE;
+  auto table = [&]() {
+    if (m.n_nodes > pn::kTableMaxElems || m.n_cells > pn::kTableMaxElems)
+      throw pn::SetupError{PN_ERR_INVALID, "mesh too large for the connectivity-table form (at most " +
+                                               std::to_string(pn::kTableMaxElems) + " nodes and cells)"};
+    return PN_FORM_TABLE;
+  };
+  if (form == PN_FORM_TABLE) return table();
   pn::detect_grid(m, g);
   std::string why;
   if (pn::grid_eligible(m, mt, precision, g, &why)) return PN_FORM_GRID;
   if (form == PN_FORM_GRID) throw pn::SetupError{PN_ERR_INVALID, "grid form unavailable: " + why};
-  return PN_FORM_TABLE;
+  return table();
 }
 
 int create_common(const pn_mesh *mesh, double dt, int32_t mode, pn_solver **out,

@@ -579,6 +579,10 @@ void build_source_entries(const MeshTables &t, const std::vector<pn_window_sourc
         }
     });
   }
+  if ((int64_t)force.size() > kMaxSourceEntries || (int64_t)moment.size() > kMaxSourceEntries)
+    fail(PN_ERR_INVALID, "too many source entries (" + std::to_string(force.size()) + " force, " +
+                             std::to_string(moment.size()) + " moment; at most " +
+                             std::to_string(kMaxSourceEntries) + " each)");
 }
 
 void detect_grid(const MeshTables &t, GridMap &g, double max_void_fraction) {
@@ -662,6 +666,10 @@ void detect_grid(const MeshTables &t, GridMap &g, double max_void_fraction) {
   }
   for (int r = 0; r < runs; r++) later[(size_t)r + 1] += later[(size_t)r];
   g.n_extra = later[(size_t)runs];
+  if (g.node_len() >= (int64_t(1) << 31) - 1) {
+    g.why = "lattice too large for 32-bit indices";
+    return;
+  }
   if (g.n_extra > 0) {
 #pragma omp parallel for schedule(static)
     for (int r = 0; r < runs; r++) {

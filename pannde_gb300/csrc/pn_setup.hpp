@@ -55,6 +55,14 @@ struct UninitAlloc : std::allocator<T> {
 template <typename T>
 using hvec = std::vector<T, UninitAlloc<T>>;
 
+// Largest node or cell count of the connectivity-table form: its kernels
+// address the spacing rows of a non-uniform mesh as a*n + i (a < 3) and the
+// two int4 halves of a connectivity row as 2*i + h in 32-bit arithmetic.
+constexpr int32_t kTableMaxElems = 715827882;  // (2^31 - 1) / 3
+// Largest number of force or moment entries of one solver: 32-bit offsets,
+// and the grid form hands an entry to up to four blocks.
+constexpr int64_t kMaxSourceEntries = (int64_t(1) << 29) - 1;
+
 // Voigt (i,j) -> index into the 21 unique entries.
 inline int cij_index(int i, int j) {
   if (i > j) { int t = i; i = j; j = t; }
