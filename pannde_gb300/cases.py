@@ -116,18 +116,27 @@ def voxel_mesh(solid: np.ndarray, h, origin=(0.0, 0.0, 0.0)) -> HexMesh:
             for dk in (0, 1):
                 used |= pad[di:di + nx + 1, dj:dj + ny + 1, dk:dk + nz + 1]
     flat = np.flatnonzero(used.reshape(-1))
-    nid = np.full(used.size, -1, dtype=np.int64)
-    nid[flat] = np.arange(flat.size)
-    nid = nid.reshape(used.shape)
+    nid = np.full(used.size, -1, dtype=np.int32)  # lattice point (flat) -> node id
+    nid[flat] = np.arange(flat.size, dtype=np.int32)
     ii, jj, kk = np.unravel_index(flat, used.shape)
     x = origin[0] + ii * hx
     y = origin[1] + jj * hy
     z = origin[2] + kk * hz
-    ci, cj, ck = np.nonzero(solid)  # C order: x slowest, z fastest
+    cells = np.flatnonzero(solid.reshape(-1))  # C order: x slowest, z fastest
+    ci, cj, ck = np.unravel_index(cells, solid.shape)
+    # flat lattice point of each cell's corner 0, then the corners' offsets
+    sj, si = nz + 1, (ny + 1) * (nz + 1)
+    base = ci * si + cj * sj + ck
     corners = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
-    hexes = np.stack([nid[ci + a, cj + b, ck + c] for a, b, c in corners], axis=1).astype(np.int32)
+    hexes = np.empty((cells.size, 8), dtype=np.int32)
+    for q, (a, b, c) in enumerate(corners):
+        hexes[:, q] = nid[base + (a * si + b * sj + c)]
+    node_ijk = np.empty((flat.size, 3), dtype=np.int64)
+    node_ijk[:, 0], node_ijk[:, 1], node_ijk[:, 2] = ii, jj, kk
+    cell_ijk = np.empty((cells.size, 3), dtype=np.int64)
+    cell_ijk[:, 0], cell_ijk[:, 1], cell_ijk[:, 2] = ci, cj, ck
     return HexMesh(x.astype(np.float64), y.astype(np.float64), z.astype(np.float64), hexes,
-                   node_ijk=np.stack([ii, jj, kk], axis=1), cell_ijk=np.stack([ci, cj, ck], axis=1))
+                   node_ijk=node_ijk, cell_ijk=cell_ijk)
 
 
 # ---- materials --------------------------------------------------------------
