@@ -29,8 +29,9 @@
  * hit lists are independent per element, so they run under OpenMP when
  * compiled with -fopenmp; the hit lists are built in two passes (count,
  * prefix sum, fill) and the spacing check reports the first bad node in node
- * order, so results and errors do not depend on the thread count.  Only
- * buildLinks stays serial: a later cell overwrites an earlier one's link.
+ * order, so results and errors do not depend on the thread count.
+ * buildLinks' "a later cell overwrites an earlier one's link" is kept as an
+ * atomic maximum of the cell index per slot.
  */
 #include <math.h>
 #include <stdint.h>
@@ -51,13 +52,23 @@ static int or_fail(int code, const char *msg) {
 }
 
 /* ---- mesh links: HexMesh::buildLinks (HexMesh.hpp:300-313) ------------- */
+/* Later cells win: every slot ends up holding the highest cell index that
+   names it, which lets the cells be linked in parallel (an atomic maximum). */
 static int build_links(const pn_mesh *m, int32_t *ncc) {
+  const int64_t nh = (int64_t)m->n_cells * 8;
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+  for (int64_t k = 0; k < nh; k++) bad |= m->hexes[k] < 0 || m->hexes[k] >= m->n_nodes;
+  if (bad) return or_fail(PN_ERR_RANGE, "invalid node id");
+#pragma omp parallel for schedule(static)
   for (int64_t k = 0; k < (int64_t)m->n_nodes * 8; k++) ncc[k] = -1;
+#pragma omp parallel for schedule(static)
   for (int32_t c = 0; c < m->n_cells; c++) {
     for (int k = 0; k < 8; k++) {
-      int32_t n = m->hexes[(int64_t)c * 8 + k];
-      if (n < 0 || n >= m->n_nodes) return or_fail(PN_ERR_RANGE, "invalid node id");
-      ncc[(int64_t)n * 8 + (k ^ 6)] = c;
+      int32_t *slot = &ncc[(int64_t)m->hexes[(int64_t)c * 8 + k] * 8 + (k ^ 6)];
+      int32_t cur = __atomic_load_n(slot, __ATOMIC_RELAXED);
+      while (cur < c && !__atomic_compare_exchange_n(slot, &cur, c, 1, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {
+      }
     }
   }
   return PN_OK;
