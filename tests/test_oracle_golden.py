@@ -265,10 +265,16 @@ def _random_cases():
     g.x = g.x * (1 + 80.0 * g.x)
     gc = cases.Case("graded", g, np.array([2700.0]), cij[:1], np.zeros(g.n_cells, np.int32), 2e-9)
     out.append((gc, [], 0))
+    # duplicated cells of the other material: a node's slot keeps the later
+    # cell (HexMesh::buildLinks), which then sets its density and differences
+    dup = rng.choice(m.n_cells, size=12, replace=False)
+    md = cases.HexMesh(m.x, m.y, m.z, np.concatenate([m.hexes, m.hexes[dup]]).astype(np.int32))
+    dc = cases.Case("duplicated", md, c.density, cij, np.concatenate([mat, 1 - mat[dup]]).astype(np.int32), 4e-9)
+    out.append((dc, src, 0))
     return [(c, s, k, rng.integers(1 << 30)) for c, s, k in out]
 
 
-@pytest.mark.parametrize("idx", range(4), ids=["holes", "moments", "crack", "graded"])
+@pytest.mark.parametrize("idx", range(5), ids=["holes", "moments", "crack", "graded", "duplicated"])
 def test_port_matches_compiled_reference(idx):
     """The C restatement against the reference HostSolver compiled from its own
     sources, on seeded cases from a random state: every field, trace and the
