@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <new>
 #include <unordered_map>
 
 namespace pn {
@@ -287,12 +288,13 @@ void build_material_from_fields(const pn_material &mat, const MeshTables &t, dou
   // all cells would.
   const int32_t nc = t.n_cells;
   out.cell_mat.resize(nc);
-  std::vector<std::vector<Row>> seen;  // [run] rows in order of first appearance
-#pragma omp parallel
-  {
-#pragma omp single
-    seen.resize((size_t)omp_get_num_threads());
+  std::vector<std::vector<Row>> seen((size_t)omp_get_max_threads());  // [run] rows, first appearance order
+  int team = 1;  // runs = threads the region actually got
+  bool out_of_memory = false;
+#pragma omp parallel num_threads((int)seen.size()) reduction(|| : out_of_memory)
+  try {
     const int nt = omp_get_num_threads(), r = omp_get_thread_num();
+    if (r == 0) team = nt;
     const int32_t c0 = (int32_t)((int64_t)nc * r / nt), c1 = (int32_t)((int64_t)nc * (r + 1) / nt);
     std::unordered_map<Row, int32_t, RowHash> ids;
     std::vector<Row> &rows = seen[(size_t)r];
@@ -316,7 +318,11 @@ void build_material_from_fields(const pn_material &mat, const MeshTables &t, dou
       }
       out.cell_mat[c] = last_id;  // numbered within the run for now
     }
+  } catch (const std::bad_alloc &) {  // no exception may leave a parallel region
+    out_of_memory = true;
   }
+  if (out_of_memory) throw std::bad_alloc();
+  seen.resize((size_t)team);
   std::unordered_map<Row, int32_t, RowHash> ids;
   std::vector<std::vector<int32_t>> remap(seen.size());
   out.c36.clear();
@@ -452,11 +458,17 @@ template <typename F>
 void entries_by_runs(int32_t n, std::vector<SourceEntry> &out, F body) {
   const int runs = std::max(1, std::min(omp_get_max_threads() * 4, n / 4096 + 1));
   std::vector<std::vector<SourceEntry>> part((size_t)runs);
-#pragma omp parallel for schedule(dynamic, 1)
+  bool out_of_memory = false;
+#pragma omp parallel for schedule(dynamic, 1) reduction(|| : out_of_memory)
   for (int r = 0; r < runs; r++) {
     const int32_t e0 = (int32_t)((int64_t)n * r / runs), e1 = (int32_t)((int64_t)n * (r + 1) / runs);
-    for (int32_t e = e0; e < e1; e++) body(e, part[(size_t)r]);
+    try {
+      for (int32_t e = e0; e < e1; e++) body(e, part[(size_t)r]);
+    } catch (const std::bad_alloc &) {  // no exception may leave a parallel region
+      out_of_memory = true;
+    }
   }
+  if (out_of_memory) throw std::bad_alloc();
   size_t total = out.size();
   for (auto &p : part) total += p.size();
   out.reserve(total);

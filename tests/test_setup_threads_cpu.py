@@ -106,8 +106,8 @@ def digest_lib(tmp_path_factory):
     return out
 
 
-def run_with_threads(lib, threads):
-    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+def run_with_threads(lib, threads, **extra):
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads), **extra)
     r = subprocess.run([sys.executable, "-c", SCRIPT, str(lib), str(ROOT)], capture_output=True,
                        text=True, env=env, timeout=300)
     assert r.returncode == 0, r.stderr
@@ -123,3 +123,5 @@ def test_host_tables_independent_of_thread_count(digest_lib):
     assert all(int(v[1][0]) > 0 and int(v[1][1]) > 0 for k, v in one.items() if k.startswith("sources-mixed"))
     for threads in (3, 8):
         assert run_with_threads(digest_lib, threads) == one
+    # teams smaller than asked for (a thread limit below the thread count)
+    assert run_with_threads(digest_lib, 8, OMP_THREAD_LIMIT="3") == one
