@@ -9,7 +9,7 @@
  * no torch and no CUDA types cross this line (streams are passed as void*).
  * Every call returns an int status (PN_OK on success); on failure
  * pn_last_error() returns a message for the calling thread.  No exception
- * ever crosses the ABI; the C++ adapter (pannde/DeviceSolver.hpp) rethrows
+ * ever crosses the ABI; the C++ adapter (include/DeviceSolver.hpp) rethrows
  * the exception type the reference would have thrown, keyed on the status.
  *
  * All host-side floating-point inputs and outputs are IEEE double, as in the
