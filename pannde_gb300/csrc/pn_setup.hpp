@@ -12,6 +12,8 @@
 //   signals    HostUnivariate::evalAt         HostUnivariate.hpp:109-142
 // This file must be compiled with -ffp-contract=off so that the window
 // predicates and spacings round exactly as the reference's C++ does.
+// The loops over nodes and cells run under OpenMP; every table, and every
+// error reported, is the same with any number of threads.
 #pragma once
 #include <cstdint>
 #include <memory>
