@@ -41,6 +41,15 @@ def digest(c, fields, mesh=None):
                          ctypes.byref(tab) if tab else None, ctypes.c_double(c.dt), out, msg, 256)
     return [n, [str(v) for v in out[:max(n, 0)]], msg.value.decode()]
 
+def plan(c, mode):
+    """pn_plan_solver of the library itself (host-only): form, footprint, lattice."""
+    from pannde_gb300 import _native as N
+    m, k1 = c.mesh.as_struct()
+    tab, k2 = c.material_table()
+    out = N.PnPlan()
+    rc = N.load().pn_plan_solver(ctypes.byref(m), None, ctypes.byref(tab), c.dt, mode, ctypes.byref(out))
+    return [rc, out.n_materials, out.form, out.device_bytes, out.algorithmic_bytes_per_step, list(out.grid)]
+
 def digest_sources(mesh, srcs, exact):
     m, k1 = mesh.as_struct()
     st, k2 = cases.sources_struct(srcs)
@@ -72,6 +81,9 @@ for fields in (0, 1):
             for crack in ("faces", "slab"):
                 c = cases.bracket_case(100 + seed, nsteps=4, water_column=wc, scale=0.3, crack=crack)
                 res[f"bracket{seed}-{wc}-{crack}-{fields}"] = digest(c, fields)
+                if fields:
+                    for mode in (1, 2, 3):  # f64, f32, df64; form chosen automatically
+                        res[f"plan-bracket{seed}-{wc}-{crack}-{mode}"] = plan(c, mode)
     res[f"shuffled-{fields}"] = digest(shuffled, fields)
     res[f"materials-{fields}"] = digest(many, fields)
     res[f"duplicated-{fields}"] = digest(dup, fields)
@@ -120,6 +132,7 @@ def test_host_tables_independent_of_thread_count(digest_lib):
     assert any(int(v[1][-7]) > 0 for k, v in one.items() if "faces" in k and v[0] > 30)
     assert one["isolated-0"][2].startswith("2 DX") and one["bad-id-1"][2].startswith("3 invalid node id")
     assert one["duplicated-0"][0] > 0 and one["materials-1"][0] > 0
+    assert all(v[0] == 0 for k, v in one.items() if k.startswith("plan-"))
     assert all(int(v[1][0]) > 0 and int(v[1][1]) > 0 for k, v in one.items() if k.startswith("sources-mixed"))
     for threads in (3, 8):
         assert run_with_threads(digest_lib, threads) == one
