@@ -69,6 +69,7 @@ def parse():
     p.add_argument("--batch-form", default="auto", choices=["auto", "table", "grid"],
                    help="device form of the batch members (auto: grid, the brackets are lattices)")
     p.add_argument("--no-serving", action="store_true", help="skip the serving leg")
+    p.add_argument("--no-pipes", action="store_true", help="skip the arithmetic pipe-rate leg")
     p.add_argument("--serving-requests", type=int, default=8)
     p.add_argument("--serving-rate", type=float, default=1.0, help="Poisson arrivals per second")
     return p.parse_args()
@@ -497,6 +498,11 @@ def main():
             line["batch"] = batch_leg(args.batch_members, args.batch_sample_steps, torch, form=args.batch_form)
         if ws == 1 and not args.no_serving:
             line["serving"] = serving_leg(args.serving_requests, args.serving_rate, torch)
+        if ws == 1 and not args.no_pipes:
+            from pannde_gb300.solver import measure_pipe_rates
+            line["pipes"] = {"ops_per_s": {k: float(f"{v:.4g}") for k, v in measure_pipe_rates().items()},
+                             "how": "pn_measure_pipe_rates: 8 independent chains per thread, full grid of "
+                                    "resident blocks, CUDA events, best of 3; thread-level operations/s"}
         if ws == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_reference(case, args.cpu_seconds)
         print(json.dumps(line))

@@ -54,6 +54,14 @@
 #include "StandardNames.hpp"
 #include "pannde_gb300.h"
 
+/* Precision of models built without an explicit precision argument -- the
+   runners name HostSolver::HostRSGTDUT / HostUTModel and never pass one.
+   Define PN_DEFAULT_PRECISION (e.g. -DPN_DEFAULT_PRECISION=PN_PREC_F64_EXACT
+   for results bit-identical to HostSolver) to choose another form. */
+#ifndef PN_DEFAULT_PRECISION
+#define PN_DEFAULT_PRECISION PN_PREC_F64
+#endif
+
 namespace DeviceSolver {
 
 /* Rethrow a C-ABI status as the exception type the reference raises. */
@@ -263,7 +271,7 @@ class DeviceRSGTDUT : public DeviceModel {
       double dt, std::shared_ptr<PanNDE::FieldBundle> domain,
       std::shared_ptr<PanNDE::FieldBundle> initial_condition,
       std::shared_ptr<PanNDE::MultiVariate> transducers[][3], int Nxducers = 0,
-      std::shared_ptr<PanNDE::Communicator> comm = nullptr, int32_t precision = PN_PREC_F64) {
+      std::shared_ptr<PanNDE::Communicator> comm = nullptr, int32_t precision = PN_DEFAULT_PRECISION) {
     return std::make_shared<DeviceRSGTDUT>(dt, domain, initial_condition, transducers, Nxducers, comm,
                                            precision);
   }
@@ -272,7 +280,7 @@ class DeviceRSGTDUT : public DeviceModel {
                 std::shared_ptr<PanNDE::FieldBundle> initial_condition,
                 std::shared_ptr<PanNDE::MultiVariate> transducer[3],
                 std::shared_ptr<PanNDE::Communicator> comm = nullptr,
-                int32_t precision = PN_PREC_F64)
+                int32_t precision = PN_DEFAULT_PRECISION)
       : DeviceModel(dt, domain, initial_condition, comm, precision) {
     addTransducer(transducer);
   }
@@ -281,7 +289,7 @@ class DeviceRSGTDUT : public DeviceModel {
                 std::shared_ptr<PanNDE::FieldBundle> initial_condition,
                 std::shared_ptr<PanNDE::MultiVariate> transducers[][3], int Nxducers = 0,
                 std::shared_ptr<PanNDE::Communicator> comm = nullptr,
-                int32_t precision = PN_PREC_F64)
+                int32_t precision = PN_DEFAULT_PRECISION)
       : DeviceModel(dt, domain, initial_condition, comm, precision) {
     for (int k = 0; k < Nxducers; k++) addTransducer(transducers[k]);
   }
@@ -300,14 +308,14 @@ class DeviceUTModel : public DeviceModel {
   static std::shared_ptr<DeviceUTModel> makeShared(
       double dt, std::shared_ptr<PanNDE::FieldBundle> domain,
       std::shared_ptr<PanNDE::FieldBundle> initial_condition,
-      std::shared_ptr<PanNDE::Communicator> comm = nullptr, int32_t precision = PN_PREC_F64) {
+      std::shared_ptr<PanNDE::Communicator> comm = nullptr, int32_t precision = PN_DEFAULT_PRECISION) {
     return std::make_shared<DeviceUTModel>(dt, domain, initial_condition, comm, precision);
   }
 
   DeviceUTModel(double dt, std::shared_ptr<PanNDE::FieldBundle> domain,
                 std::shared_ptr<PanNDE::FieldBundle> initial_condition,
                 std::shared_ptr<PanNDE::Communicator> comm = nullptr,
-                int32_t precision = PN_PREC_F64)
+                int32_t precision = PN_DEFAULT_PRECISION)
       : DeviceModel(dt, domain, initial_condition, comm, precision) {}
 
   /* HostUTModel::applyTransducer (HostUTModel.hpp:138-141) */

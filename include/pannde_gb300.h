@@ -392,7 +392,12 @@ int pn_batch_solve(pn_batch *b, int32_t nsteps);
    compiled into the library (room for about 270 grid-form or 550
    table-form members), looked up with
    cudaGetSymbolAddress on the first call on each device -- make that first
-   call before any stream capture starts on the device.  Batches whose
+   call before any stream capture starts on the device.  The first call on a
+   device may also load kernels the process has not launched yet (CUDA's lazy
+   module loading), which the driver backs with memory of its own; later calls
+   load nothing.  The looked-up address is kept for the life of the process's
+   context on the device: do not call this again on a device after
+   cudaDeviceReset.  Batches whose
    staging does not fit return PN_ERR_INVALID with the sizes, and so do
    members whose source tables or signal table have not been built yet (any
    one pn_batch_solve or pn_solver_solve step builds them; signal rows are
@@ -441,6 +446,17 @@ int pn_partitioned_get_traces(pn_partitioned *p, double *out, int64_t max_record
 /* partitions, halo node copies, local cells summed over partitions */
 int pn_partitioned_info(pn_partitioned *p, int32_t *n_parts, int64_t *halo_nodes, int64_t *local_cells);
 int pn_partitioned_destroy(pn_partitioned *p);
+
+/* ---- diagnostics -------------------------------------------------------------
+   Issue rates of the arithmetic pipes the step kernels lean on, measured on
+   the current device (no counterpart in the reference; a measurement aid for
+   choosing an arithmetic form).  Fills min(n, 6) rates in thread-level
+   operations per second: [0] FP64 fused multiply-add, [1] FP64 add, [2] FP32
+   fused multiply-add, [3] conversion double -> float, [4] conversion float ->
+   double (each of [3], [4] alongside two integer instructions), [5] a
+   32-bit integer xor + add pair.  Takes about a second and a few MB of
+   device memory. */
+int pn_measure_pipe_rates(double *rates, int32_t n);
 
 /* Free all device memory of the solver. */
 int pn_solver_destroy(pn_solver *s);

@@ -29,7 +29,9 @@ from pannde_gb300 import _native as N
 HERE = Path(__file__).resolve().parent
 PORT_LIB = HERE / "_build" / "libpn_oracle.so"
 REF_LIB = HERE / "_ref" / "libpannde_ref.so"
-REF_SRC = Path(os.environ.get("PANNDE_REFERENCE", "/root/reference"))
+# the PanNDE sources: $PANNDE_REFERENCE, else a "reference" directory beside
+# this repository's root
+REF_SRC = Path(os.environ.get("PANNDE_REFERENCE") or (HERE.parent.parent / "reference"))
 
 _RUN_ARGS = [POINTER(N.PnMesh), POINTER(N.PnMaterial), c_double, POINTER(N.P_double),
              POINTER(N.P_double), POINTER(N.PnWindowSource), c_int32, c_int32, N.P_int32, c_int32,

@@ -9,6 +9,7 @@ Sources (``pannde_gb300/csrc``):
   rsg_split.cu  grid form: fix-up of split lattice sites (cracks)  nvcc, sm_103a
   pn_noalloc.cu fixed scratch of the allocation-free batch solve   nvcc
   rsg_energy.cu FP64 energy audit             nvcc, sm_103a
+  rsg_pipes.cu  pipe issue-rate measurement   nvcc, sm_103a
   pn_energy.cpp energy audit tables           g++
   pn_partition.cpp partitioned solve (halo exchange on one device)  g++
   pn_setup.cpp  host table construction       g++, -ffp-contract=off, OpenMP loops
@@ -63,6 +64,7 @@ def _jobs() -> list[tuple[list[str], Path]]:
         (common_cu + ["-c", str(CSRC / "rsg_split.cu")], OUT / "rsg_split.o"),
         (common_cu + ["-c", str(CSRC / "pn_noalloc.cu")], OUT / "pn_noalloc.o"),
         (common_cu + ["-c", str(CSRC / "rsg_energy.cu")], OUT / "rsg_energy.o"),
+        (common_cu + ["-c", str(CSRC / "rsg_pipes.cu")], OUT / "rsg_pipes.o"),
         (common_cc + ["-c", str(CSRC / "pn_energy.cpp")], OUT / "pn_energy.o"),
         (common_cc + ["-c", str(CSRC / "pn_partition.cpp")], OUT / "pn_partition.o"),
         (common_cc + ["-c", str(CSRC / "pn_setup.cpp")], OUT / "pn_setup.o"),

@@ -551,7 +551,14 @@ int pn_batch_solve_noalloc(pn_batch *b, int32_t nsteps) {
     void *scratch = nullptr;
     pn::ck(pn::noalloc_scratch(&scratch), "scratch symbol address");
     for (pn_solver *s : b->members) pn::ck(cudaStreamSynchronize(s->stream), "member sync");
-    solve_members(b, nsteps, ScratchStaging{(unsigned char *)scratch}, false);
+    try {
+      solve_members(b, nsteps, ScratchStaging{(unsigned char *)scratch}, false);
+    } catch (...) {
+      // steps queued before the failure may still read the scratch: let them
+      // finish before the lock lets another call restage it
+      cudaStreamSynchronize(b->stream);
+      throw;
+    }
     return PN_OK;
   });
 }

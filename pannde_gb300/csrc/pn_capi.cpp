@@ -552,6 +552,14 @@ int pn_solver_energy(pn_solver *s, double *kinetic, double *strain) {
   });
 }
 
+int pn_measure_pipe_rates(double *rates, int32_t n) {
+  return guarded([&]() -> int {
+    if (!rates || n < 0) return set_err(PN_ERR_INVALID, "null rates or negative count");
+    pn::ck(pn::measure_pipe_rates(rates, n), "pipe-rate kernels");
+    return PN_OK;
+  });
+}
+
 int pn_solver_synchronize(pn_solver *s) {
   return guarded([&]() -> int {
     if (!s) return set_err(PN_ERR_INVALID, "null solver");

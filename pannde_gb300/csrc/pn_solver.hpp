@@ -333,4 +333,8 @@ void energy(pn_solver *s, double &kinetic, double &strain);
 // in the solver's device error word; the stream must be synchronised
 int device_check(pn_solver *s);
 
+// issue rates of the arithmetic pipes on the current device (rsg_pipes.cu):
+// FP64 FMA, FP64 add, FP32 FMA, double->float, float->double, integer pair
+cudaError_t measure_pipe_rates(double *rates, int n);
+
 }  // namespace pn

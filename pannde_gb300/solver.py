@@ -316,3 +316,15 @@ class Partitioned:
 
     def __exit__(self, *exc):
         self.close()
+
+
+PIPE_RATE_NAMES = ("fp64_fma", "fp64_add", "fp32_fma", "cvt_f64_to_f32", "cvt_f32_to_f64", "int_xor_add")
+
+
+def measure_pipe_rates() -> dict:
+    """Thread-level operations per second of the arithmetic pipes on the
+    current device (pn_measure_pipe_rates), keyed by PIPE_RATE_NAMES."""
+    lib = N.load()
+    out = np.zeros(len(PIPE_RATE_NAMES), np.float64)
+    N.check(lib.pn_measure_pipe_rates(out.ctypes.data_as(N.P_double), len(PIPE_RATE_NAMES)))
+    return dict(zip(PIPE_RATE_NAMES, out.tolist()))

@@ -4,14 +4,15 @@ HostSolver headers, links the library, and behaves like HostRSGTDUT /
 HostUTModel (bit-identical in the exact FP64 form, <= 1e-10 otherwise) when a
 GPU is present; without one, device creation raises std::runtime_error.
 Skipped where the reference sources are absent."""
-import os
 import subprocess
 from pathlib import Path
 
 import pytest
 
+import oracle
+
 ROOT = Path(__file__).resolve().parent.parent
-REF = Path(os.environ.get("PANNDE_REFERENCE", "/root/reference"))
+REF = oracle.REF_SRC
 LIB = ROOT / "pannde_gb300" / "_build"
 
 

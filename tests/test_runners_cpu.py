@@ -8,17 +8,18 @@ excitations and timing through the stand-in gateway and reaches model
 construction; with a GPU it runs and writes <out>_<k>.vtu and
 velocities_<k>.vtt, without one model construction reports that no CUDA
 device is usable.  Skipped where the reference sources are absent."""
-import os
 import shutil
 import subprocess
 from pathlib import Path
 
 import pytest
 
+import oracle
+
 from pannde_gb300 import cases, vtu
 
 ROOT = Path(__file__).resolve().parent.parent
-REF = Path(os.environ.get("PANNDE_REFERENCE", "/root/reference"))
+REF = oracle.REF_SRC
 LIB = ROOT / "pannde_gb300" / "_build"
 RUNNERS = REF / "applications" / "source" / "CaseRunners"
 

@@ -9,6 +9,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
+import oracle
 from pannde_gb300 import cases, vtu
 
 ROOT = Path(__file__).resolve().parent.parent
@@ -98,8 +99,7 @@ def test_transducer_job_keys(tmp_path):
 
 def test_standin_gateway_reads_and_writes(tmp_path):
     """include/standin/VTKGateway.hpp over the reference's HostData factories."""
-    import os
-    ref = Path(os.environ.get("PANNDE_REFERENCE", "/root/reference"))
+    ref = oracle.REF_SRC
     if not (ref / "modules" / "HostData" / "include" / "HostField.hpp").exists():
         pytest.skip("reference headers not present")
     inc = ["-I", str(ROOT / "include" / "standin"), "-I", str(ROOT / "include")]

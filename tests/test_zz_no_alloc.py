@@ -84,6 +84,29 @@ def test_members_with_split_sites(cuda_device):
         y.close()
 
 
+def test_second_call_takes_no_device_memory(cuda_device):
+    """After one warm call (which may load kernels lazily), a further call
+    leaves the device's free memory where it was: nothing is allocated."""
+    import torch
+    cs = members()
+    sv = [Solver.from_case(c, precision="f32", form="grid", capacity=40) for c in cs]
+    try:
+        with Batch() as b:
+            for s in sv:
+                b.add(s)
+            b.solve(1)
+            b.solve_noalloc(5)
+            torch.cuda.synchronize()
+            free0, _ = torch.cuda.mem_get_info()
+            b.solve_noalloc(9)
+            torch.cuda.synchronize()
+            free1, _ = torch.cuda.mem_get_info()
+        assert free1 >= free0, (free0, free1)
+    finally:
+        for s in sv:
+            s.close()
+
+
 def test_members_without_tables_are_refused(cuda_device):
     c = members()[0]
     with Solver.from_case(c, precision="f32", capacity=10) as s, Batch() as b:
