@@ -52,7 +52,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--case", default="laminate", choices=["laminate", "plate", "holes"])
-    p.add_argument("--nx", type=int, default=None, help="laminate size override (profiling)")
+    p.add_argument("--nx", type=int, default=None, help="laminate / holed-plate size override (profiling)")
     p.add_argument("--ny", type=int, default=None)
     p.add_argument("--nz", type=int, default=None)
     p.add_argument("--precisions", default="f64,df64,f32",
@@ -70,8 +70,12 @@ def parse():
                    help="device form of the batch members (auto: grid, the brackets are lattices)")
     p.add_argument("--no-serving", action="store_true", help="skip the serving leg")
     p.add_argument("--no-pipes", action="store_true", help="skip the arithmetic pipe-rate leg")
-    p.add_argument("--serving-requests", type=int, default=8)
-    p.add_argument("--serving-rate", type=float, default=1.0, help="Poisson arrivals per second")
+    p.add_argument("--no-holes", action="store_true",
+                   help="skip the FP32 holed-plate (1024x1024x24, 12 holes) bandwidth leg")
+    p.add_argument("--serving-requests", type=int, default=32)
+    p.add_argument("--serving-rate", type=float, default=4.0, help="Poisson arrivals per second")
+    p.add_argument("--serving-fp64-subset", type=int, default=8,
+                   help="requests of the serving run also solved in sequential FP64")
     return p.parse_args()
 
 
@@ -86,8 +90,9 @@ def make_case(name, nx=None, ny=None, nz=None):
         c = cases.al_plate_case()
         desc = "aluminium plate 64x64x8 cells (0.1 mm), 1 MHz tone burst, 16 sensors"
     else:
-        c = cases.holed_plate_case()
-        desc = "aluminium plate 1024x1024x24 cells (0.1 mm), 12 holes, 1 MHz tone burst, 128 sensors"
+        nx, ny, nz = nx or 1024, ny or 1024, nz or 24
+        c = cases.holed_plate_case(nx=nx, ny=ny, nz=nz)
+        desc = f"aluminium plate {nx}x{ny}x{nz} cells (0.1 mm), 12 holes, 1 MHz tone burst, 128 sensors"
     return c, desc
 
 
@@ -202,7 +207,7 @@ def whole_job_rate(units_per_rank, seconds, ws):
     return ws * units_per_rank / seconds
 
 
-def time_device(case, prec, steps, warmup, torch, dist):
+def time_device(case, prec, steps, warmup, torch, dist, energy=False):
     """Device throughput of the hot path with inputs resident in HBM."""
     from pannde_gb300.solver import Solver
     s = Solver.from_case(case, precision=prec, capacity=warmup + steps, form=FORM)
@@ -223,6 +228,8 @@ def time_device(case, prec, steps, warmup, torch, dist):
     ms = reduce_max(e0.elapsed_time(e1), dist, torch)
     kt = s.kernel_times()
     info = s.info()
+    if energy:  # FP64 energy audit of the final state
+        info["energy"] = s.energy()
     s.close()
     return ms, kt, info
 
@@ -359,13 +366,16 @@ def batch_leg(n_members, sample_steps, torch, steps_total=3000, form="auto"):
                         "water column (pressure source), FP32, one pn_batch_solve over all members"}
 
 
-def serving_leg(n_requests, rate, torch, seed=7):
+def serving_leg(n_requests, rate, torch, seed=7, subset=8):
     """Serving: Poisson arrivals (rate per second, seeded); each request an
     aluminium or laminate plate, cells log-uniform 0.2 M - 20 M, transducer
     position, 0.25-2 MHz, +-5% stiffness, 1000-8000 steps.  Continuous
-    batching in FP32 (pannde_gb300.serving.Server) against the same requests
-    solved one after another in plain FP64 on the same GPU; the FP64 traces
-    are also the spot check of every FP32 trace (relative L2 per request)."""
+    batching in FP32 (pannde_gb300.serving.Server) with the admission queue
+    depth sampled along the run.  The baseline is the same requests solved
+    one after another in plain FP64 on the same GPU: `subset` of them, drawn
+    by the seed, are solved (set-up included) and their seconds per cell-step
+    extrapolate the sequential run of all requests; the same FP64 solves are
+    the spot check of those requests' FP32 traces (relative L2 per request)."""
     from pannde_gb300 import serving
     t0 = time.perf_counter()
     reqs = serving.poisson_requests(n_requests, rate, seed)
@@ -373,22 +383,59 @@ def serving_leg(n_requests, rate, torch, seed=7):
     free, _ = torch.cuda.mem_get_info()
     srv = serving.Server(hbm_budget_bytes=int(0.7 * free), precision="f32", quantum=250)
     res, st = srv.run(reqs)
-    seq, sst = serving.run_sequential(reqs, precision="f64")
+    rng = np.random.default_rng(seed + 1)
+    pick = sorted(rng.choice(len(reqs), size=min(subset, len(reqs)), replace=False).tolist())
+    sub = [serving.Request(reqs[i].rid, 0.0, reqs[i].case, reqs[i].nsteps, reqs[i].meta) for i in pick]
+    seq, sst = serving.run_sequential(sub, precision="f64")
+    by_rid = {r.rid: r for r in res}
     errs = []
-    for r, q in zip(res, seq):
+    for q in seq:
         d = np.linalg.norm(q.traces)
-        errs.append(float(np.linalg.norm(r.traces - q.traces) / (d if d > 0 else 1.0)))
+        errs.append(float(np.linalg.norm(by_rid[q.rid].traces - q.traces) / (d if d > 0 else 1.0)))
+    cs = {r.rid: r.case.mesh.n_cells * r.nsteps for r in reqs}
+    s_per_cs = sst["elapsed_s"] / sum(cs[i] for i in (reqs[k].rid for k in pick))
+    seq_est_s = s_per_cs * sum(cs.values())
+    seq_sph = len(reqs) / seq_est_s * 3600.0
     return {"sims_per_hour": round(st["sims_per_hour"], 1), "p50_s": round(st["p50_s"], 3),
             "p99_s": round(st["p99_s"], 3), "gcell_steps_per_s": round(st["gcell_steps_per_s"], 3),
             "max_in_flight": st["max_active"], "requests": st["requests"], "rate_per_s": rate,
-            "sequential_fp64": {"sims_per_hour": round(sst["sims_per_hour"], 1), "p50_s": round(sst["p50_s"], 3),
-                                "p99_s": round(sst["p99_s"], 3)},
-            "sims_per_hour_vs_sequential_fp64": round(st["sims_per_hour"] / max(sst["sims_per_hour"], 1e-9), 2),
+            "elapsed_s": round(st["elapsed_s"], 2),
+            "queue": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in st["queue"].items()},
+            "sequential_fp64": {"sims_per_hour": round(seq_sph, 1), "measured_requests": len(pick),
+                                "measured_s": round(sst["elapsed_s"], 2),
+                                "s_per_gcell_step": round(s_per_cs * 1e9, 4),
+                                "how": "FP64 solves (set-up included) of a seeded subset, one after another; "
+                                       "their seconds per cell-step times all requests' cell-steps"},
+            "sims_per_hour_vs_sequential_fp64": round(st["sims_per_hour"] / max(seq_sph, 1e-9), 2),
             "fp32_trace_rel_l2_vs_fp64_max": max(errs) if errs else None,
+            "fp64_spot_checked_requests": len(errs),
             "request_generation_s": round(gen_s, 1),
             "workload": "Poisson arrivals; Al or laminate plates 0.2-20 M cells (log-uniform), "
                         "1000-8000 steps, 0.25-2 MHz; FP32 continuous batching vs sequential plain FP64; "
                         "latency = arrival to traces"}
+
+
+def holes_leg(steps, warmup, torch, peak, peak_kind):
+    """The FP32 large-mesh bandwidth workload: aluminium plate 1024x1024x24
+    cells (0.1 mm voxels) with 12 seeded through-thickness holes of 1-4 mm
+    radius (24.4 M cells left), a 2 mm radius 1 MHz transducer on the top
+    face, 128 seeded sensors recorded every step; FP32 state and material
+    rows.  Device throughput over `steps` steps after `warmup` (each step moves
+    far more than the L2), the tensor-copy kernel's HBM roofline over the
+    lattice it marches (each tile to its top solid layer), and the FP64
+    energy audit of the final state."""
+    case, desc = make_case("holes")
+    t0 = time.perf_counter()
+    ms, kt, info = time_device(case, "f32", steps, warmup, torch, None, energy=True)
+    cells = info["n_cells"]
+    kin, strain = info["energy"]
+    return {"workload": desc + " (FP32 form)", "cells": cells, "nodes": info["n_nodes"],
+            "lattice": info["grid"], "value": round(cells * steps / (ms * 1e-3) / 1e9, 4), "unit": UNIT,
+            "ms_per_step": round(ms / steps, 4), "steps": steps, "warmup": warmup, "dtype": "f32",
+            "algorithmic_bytes_per_step": info["algorithmic_bytes_per_step"],
+            "roofline": roofline("holes", info, kt, "f32", peak, peak_kind),
+            "energy_audit_fp64": {"after_steps": warmup + steps, "kinetic_J": kin, "strain_J": strain},
+            "setup_and_run_s": round(time.perf_counter() - t0, 1)}
 
 
 def cpu_reference(case, budget_s):
@@ -494,10 +541,13 @@ def main():
                               "pn_solver_get_traces + pn_solver_get_state to pinned host; wall clock, "
                               "max over ranks; bytes summed over ranks"}
     if rank == 0:
+        if ws == 1 and not args.no_holes:
+            line["configs"] = {"holes": holes_leg(args.steps, args.warmup, torch, peak, peak_kind)}
         if ws == 1 and not args.no_batch:
             line["batch"] = batch_leg(args.batch_members, args.batch_sample_steps, torch, form=args.batch_form)
         if ws == 1 and not args.no_serving:
-            line["serving"] = serving_leg(args.serving_requests, args.serving_rate, torch)
+            line["serving"] = serving_leg(args.serving_requests, args.serving_rate, torch,
+                                         subset=args.serving_fp64_subset)
         if ws == 1 and not args.no_pipes:
             from pannde_gb300.solver import measure_pipe_rates
             line["pipes"] = {"ops_per_s": {k: float(f"{v:.4g}") for k, v in measure_pipe_rates().items()},

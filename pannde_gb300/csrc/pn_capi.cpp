@@ -65,9 +65,12 @@ int64_t sig_row(const pn_solver *s, int64_t k) {
 
 int64_t step_bytes(const pn_solver *s) {
   const int64_t e = (int64_t)s->esz;
-  if (s->form == PN_FORM_GRID)
-    // S read + write, material byte per lattice cell; V read + write, dt/rho per node
-    return s->grid.grid_cells() * (12 * e + 1) + s->grid.grid_nodes() * 7 * e;
+  if (s->form == PN_FORM_GRID) {
+    // S read + write, material byte per marched lattice cell; V read + write,
+    // dt/rho per marched node (fixed at creation)
+    if (s->step_bytes_cached == 0) s->step_bytes_cached = grid_step_bytes(s->grid, s->mat.n_mat, e);
+    return s->step_bytes_cached;
+  }
   // per cell: S read in the velocity step, S read+write in the stress step,
   // material id, cell->node table; per node: V read+write in the velocity
   // step, V read in the stress step, dt/rho, node->cell slots
@@ -195,7 +198,7 @@ int pn_plan_solver(const pn_mesh *mesh, const pn_material *material, const pn_ma
     const int64_t e = precision == PN_PREC_F32 ? 4 : 8;
     if (f == PN_FORM_GRID) {
       out->device_bytes = pn::grid_footprint(g, mt, precision);
-      out->algorithmic_bytes_per_step = g.grid_cells() * (12 * e + 1) + g.grid_nodes() * 7 * e;
+      out->algorithmic_bytes_per_step = pn::grid_step_bytes(g, mt.n_mat, e);
       out->grid[0] = g.nx;
       out->grid[1] = g.ny;
       out->grid[2] = g.nz;

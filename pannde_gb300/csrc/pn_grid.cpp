@@ -166,6 +166,30 @@ bool grid_eligible(const MeshTables &m, const MaterialTables &mt, int precision,
   return true;
 }
 
+// Algorithmic HBM bytes of one grid step, e bytes per value: S read + write
+// and the material byte per marched lattice cell, V read + write and dt/rho
+// per marched lattice node.  The tensor-copy kernel marches each tile's owned
+// columns up to its top solid layer (node layers 0..top; nothing when top is
+// 0), the classic kernel the whole box.
+int64_t grid_step_bytes(const GridMap &g, int32_t n_mat, int64_t e) {
+  if (!want_tma(n_mat)) return g.grid_cells() * (12 * e + 1) + g.grid_nodes() * 7 * e;
+  const Tiles T = tiles_of(g);
+  const std::vector<int32_t> top = grid_tile_tops(g);
+  int64_t cells = 0, nodes = 0;
+  for (int by = 0; by < T.by_count; by++)
+    for (int bx = 0; bx < T.bx_count; bx++) {
+      const int64_t i0 = (int64_t)bx * (T.tx - 1), j0 = (int64_t)by * (T.ty - 1);
+      const int64_t ccols = std::max<int64_t>(0, std::min<int64_t>(T.tx - 1, g.nx - i0)) *
+                            std::max<int64_t>(0, std::min<int64_t>(T.ty - 1, g.ny - j0));
+      const int64_t ncols = std::max<int64_t>(0, std::min<int64_t>(T.tx - 1, g.nx + 1 - i0)) *
+                            std::max<int64_t>(0, std::min<int64_t>(T.ty - 1, g.ny + 1 - j0));
+      const int64_t t = top[(size_t)by * T.bx_count + bx];
+      cells += ccols * t;
+      nodes += t > 0 ? ncols * (t + 1) : 0;
+    }
+  return cells * (12 * e + 1) + nodes * 7 * e;
+}
+
 int64_t grid_footprint(const GridMap &g, const MaterialTables &mt, int precision) {
   const int64_t e = precision == PN_PREC_F32 ? 4 : 8;
   const int64_t gn = g.node_len(), gc = g.cell_sites();

@@ -86,6 +86,7 @@ struct pn_solver {
   uint8_t *d_gmat = nullptr;
   void *d_tmaps = nullptr;   // tensor maps [2 input parities] (null: classic kernel)
   int32_t *d_ktop = nullptr; // [tiles] cell layers the tensor-copy kernel marches per tile
+  mutable int64_t step_bytes_cached = 0;  // grid form: algorithmic bytes of one step (0: not yet)
   // cubic lattice with the tensor-copy kernel: 0.25/h folded into dt/rho, dt*C
   // and the force weights (the kernel's g is then 1); 1.0 when not folded
   double gfold = 1.0;
@@ -299,6 +300,8 @@ bool grid_eligible(const MeshTables &m, const MaterialTables &mt, int precision,
 // with the apron, i.e. the cell layers the tensor-copy kernel marches
 std::vector<int32_t> grid_tile_tops(const GridMap &g);
 int64_t grid_footprint(const GridMap &g, const MaterialTables &mt, int precision);
+// algorithmic HBM bytes of one grid step over the lattice the kernel marches
+int64_t grid_step_bytes(const GridMap &g, int32_t n_mat, int64_t e);
 void grid_create(pn_solver *s);
 void grid_sources(pn_solver *s);
 void grid_sensors(pn_solver *s, const std::vector<std::pair<int32_t, int32_t>> &sorted);

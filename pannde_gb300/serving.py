@@ -142,6 +142,15 @@ class Server:
         cell_steps = 0
         max_active = 0
         done = 0
+        admitted = 0
+        arrivals = [r.arrival for r in pending]
+        queue_log: list[tuple[float, int]] = []  # (time, requests arrived and not yet admitted)
+
+        def log_queue():
+            now = self.clock() - t0
+            arrived = int(np.searchsorted(arrivals, now, side="right"))
+            queue_log.append((now, arrived - admitted))
+
         with Batch() as batch:
             stream = _new_stream()
             if stream is not None:  # a created stream: repeated quanta replay as CUDA graphs
@@ -160,6 +169,7 @@ class Server:
                         raise state["error"]
                     r, s, need = item
                     batch.add(s)
+                    admitted += 1
                     now = self.clock() - t0
                     active[r.rid] = dict(req=r, solver=s, left=r.nsteps, need=need, admitted=now)
                     with lock:
@@ -167,6 +177,7 @@ class Server:
                         lock.notify_all()
                     if on_admit:
                         on_admit(r, now)
+                log_queue()
                 if not active:
                     continue
                 max_active = max(max_active, len(active))
@@ -196,8 +207,23 @@ class Server:
                      sims_per_hour=len(results) / elapsed * 3600.0 if elapsed > 0 else 0.0,
                      p50_s=float(np.percentile(lat, 50)), p99_s=float(np.percentile(lat, 99)),
                      gcell_steps_per_s=cell_steps / elapsed / 1e9 if elapsed > 0 else 0.0,
-                     max_active=max_active)
+                     max_active=max_active, queue=queue_stats(queue_log, elapsed))
         return sorted(results, key=lambda r: r.rid), stats
+
+
+def queue_stats(log: list[tuple[float, int]], elapsed: float) -> dict:
+    """Admission queue depth (requests arrived and not yet admitted) from
+    (time, depth) samples taken at every pass of the GPU loop, each held until
+    the next sample: time-weighted mean, the share of the run with a
+    non-empty queue, and the largest depth."""
+    if not log or elapsed <= 0:
+        return dict(mean_depth=0.0, nonempty_frac=0.0, max_depth=0, samples=0)
+    t = np.array([x[0] for x in log] + [elapsed])
+    d = np.array([x[1] for x in log], dtype=np.float64)
+    w = np.clip(np.diff(t), 0.0, None)
+    span = max(float(w.sum()), 1e-12)
+    return dict(mean_depth=float((w * d).sum() / span), nonempty_frac=float(w[d > 0].sum() / span),
+                max_depth=int(d.max()), samples=len(log))
 
 
 def _current_device():

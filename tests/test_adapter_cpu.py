@@ -23,7 +23,8 @@ def build_and_run(tmp_path):
     inc = ["-I", str(ROOT / "include")]
     for m in ("PanNDE", "HostData", "HostSolver", "Stubs"):
         inc += ["-I", str(REF / "modules" / m / "include")]
-    cmd = ["g++", "-std=c++14", "-O1", "-w", *inc, str(ROOT / "tests" / "cxx" / "adapter_check.cpp"),
+    # -ffp-contract=off: the reference's arithmetic as written, no fused a*b+c
+    cmd = ["g++", "-std=c++14", "-O1", "-ffp-contract=off", "-w", *inc, str(ROOT / "tests" / "cxx" / "adapter_check.cpp"),
            "-L", str(LIB), "-lpannde_gb300", f"-Wl,-rpath,{LIB}", "-o", str(exe)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
@@ -41,7 +42,7 @@ def test_runner_statements_compile_unchanged_with_standins(tmp_path):
     inc = ["-I", str(ROOT / "include" / "standin"), "-I", str(ROOT / "include")]
     for m in ("PanNDE", "HostData", "Stubs", "HostSolver"):
         inc += ["-I", str(REF / "modules" / m / "include")]
-    cmd = ["g++", "-std=c++14", "-O1", "-w", *inc, str(ROOT / "tests" / "cxx" / "standin_check.cpp"),
+    cmd = ["g++", "-std=c++14", "-O1", "-ffp-contract=off", "-w", *inc, str(ROOT / "tests" / "cxx" / "standin_check.cpp"),
            "-L", str(LIB), "-lpannde_gb300", f"-Wl,-rpath,{LIB}", "-o", str(exe)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
@@ -56,6 +57,7 @@ def test_runner_statements_compile_unchanged_with_standins(tmp_path):
 
 def test_adapter_builds_against_reference_and_runs(tmp_path):
     out = build_and_run(tmp_path)
+    print(out)
     lines = out.strip().splitlines()
     assert lines, out
     if lines[0].startswith("no-device"):

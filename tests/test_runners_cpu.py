@@ -32,7 +32,7 @@ def build(tmp_path, name):
         inc += ["-I", str(REF / "modules" / m / "include")]
     inc += ["-I", str(REF / "applications" / "include")]
     exe = tmp_path / name
-    r = subprocess.run(["g++", "-std=c++14", "-O1", "-w", *inc, str(RUNNERS / f"{name}.cpp"), "-L", str(LIB),
+    r = subprocess.run(["g++", "-std=c++14", "-O1", "-ffp-contract=off", "-w", *inc, str(RUNNERS / f"{name}.cpp"), "-L", str(LIB),
                         "-lpannde_gb300", f"-Wl,-rpath,{LIB}", "-lz", "-o", str(exe)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]

@@ -59,7 +59,11 @@ def build(tmp_path, name, variant):
     for m in ("PanNDE", "Controller", "HostData", "HostSolver", "Stubs"):
         inc += ["-I", str(REF / "modules" / m / "include")]
     inc += ["-I", str(REF / "applications" / "include")]
-    cmd = ["g++", "-std=c++14", "-O2", "-w", *defs, *inc, str(RUNNERS / f"{name}.cpp"), "-L", str(LIB),
+    # -ffp-contract=off: every product and sum rounded on its own, as written
+    # (g++ fuses a*b+c into one FMA on aarch64 at -O2 otherwise, which is not
+    # the reference's source-level arithmetic; the oracle builds the same way)
+    cmd = ["g++", "-std=c++14", "-O2", "-ffp-contract=off", "-w", *defs, *inc, str(RUNNERS / f"{name}.cpp"),
+           "-L", str(LIB),
            "-lpannde_gb300", f"-Wl,-rpath,{LIB}", "-lz", "-o", str(out)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
@@ -82,8 +86,10 @@ def arrays(path):
 
 
 def compare_dirs(host_dir, dev_dir, files, exact):
-    """Worst relative L2 over every array of every output file."""
+    """Worst relative L2 over every array of every output file (exact: every
+    array bit-identical, the differing ones listed)."""
     worst = 0.0
+    bad = []
     for f in files:
         a, b = arrays(dev_dir / f), arrays(host_dir / f)
         assert a.keys() == b.keys()
@@ -96,11 +102,13 @@ def compare_dirs(host_dir, dev_dir, files, exact):
                 ha = np.asarray(a[kind][name], np.float64)
                 assert ha.shape == hb.shape, (f, name)
                 if exact:
-                    assert np.array_equal(ha, hb), (f, name)
+                    if not np.array_equal(ha, hb):
+                        bad.append((f, name, int((ha != hb).sum()), float(np.abs(ha - hb).max())))
                     continue
                 d = max(np.linalg.norm(hb), floor)
                 if d > 0:
                     worst = max(worst, float(np.linalg.norm(ha - hb) / d))
+    assert not bad, f"arrays that differ (file, array, values, max abs): {bad[:12]}"
     return worst
 
 
