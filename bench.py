@@ -325,7 +325,7 @@ def batch_leg(n_members, sample_steps, torch, steps_total=3000, form="auto"):
     batch's stream; the per-step cost does not change along the run."""
     from pannde_gb300 import cases
     from pannde_gb300.solver import Batch, Solver
-    warm = 20  # long enough for the launch-shape tuning (2 rounds x up to 4 shapes x 2 steps) to run untimed
+    warm = 25  # long enough for the launch-shape tuning (2 rounds x up to 6 shapes x 2 steps + 1) to run untimed
     quantum = 25  # steps per pn_batch_solve call: equal calls replay a captured CUDA graph
     sample_steps = max(quantum, sample_steps // quantum * quantum)
     t0 = time.perf_counter()
@@ -361,6 +361,7 @@ def batch_leg(n_members, sample_steps, torch, steps_total=3000, form="auto"):
             "members": n_members, "cells_total": cells, "steps_per_sim": steps_total,
             "timed_steps": sample_steps, "ms_per_batch_step": round(ms / sample_steps, 4),
             "steps_per_call": quantum, "graph_launches": plan["graph_launches"],
+            "tuned_shape": {"tile": f"32x{plan['tile_rows']}", "z_chunks_per_column": plan["shape"] or "launcher"},
             "dtype": "f32", "form": ",".join(forms), "setup_s": round(setup_s, 1),
             "workload": f"{n_members} seeded L-brackets with a disconnected-face crack, every sixth with a "
                         "water column (pressure source), FP32, one pn_batch_solve over all members"}

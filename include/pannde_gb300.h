@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define PN_ABI_VERSION 2
+#define PN_ABI_VERSION 3
 
 /* ---- status codes ------------------------------------------------------ */
 enum pn_status {
@@ -415,9 +415,16 @@ int pn_batch_synchronize(pn_batch *b);
    precision, member count and work size) by timing candidates on real steps,
    and a chunk of steps whose launch sequence repeats the previous chunk's is
    captured as a CUDA graph and replayed (work on a created stream only).
-   Neither changes results.  Reports the graph replays and captures so far
-   and the number of tuned classes (any pointer may be NULL). */
-int pn_batch_plan_stats(pn_batch *b, int64_t *graph_launches, int64_t *graph_captures, int32_t *tuned_classes);
+   Grid-form shapes are a block tile of 32 x tile_rows threads (rows 8, or 16
+   with FP32 storage and the tensor-copy kernel; the members are re-tiled to
+   try and to keep a shape) times z chunks per tile column (0: as many as
+   one wave of resident blocks needs); table-form shapes are resident blocks
+   per SM.  Neither changes results.  Reports the graph replays and captures
+   so far, the number of tuned classes, and the shape of the last chunk run:
+   tile_rows (0 for the table form) and shape (grid: z chunks per column, 0 =
+   the launcher's choice; table: blocks per SM).  Any pointer may be NULL. */
+int pn_batch_plan_stats(pn_batch *b, int64_t *graph_launches, int64_t *graph_captures, int32_t *tuned_classes,
+                        int32_t *tile_rows, int32_t *shape);
 int pn_batch_destroy(pn_batch *b);
 
 /* ---- partitioned solve ----------------------------------------------------

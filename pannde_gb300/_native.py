@@ -12,7 +12,7 @@ from pathlib import Path
 import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "_build" / "libpannde_gb300.so"
-ABI_VERSION = 2  # PN_ABI_VERSION of include/pannde_gb300.h these declarations follow
+ABI_VERSION = 3  # PN_ABI_VERSION of include/pannde_gb300.h these declarations follow
 
 # status codes (enum pn_status)
 PN_OK = 0
@@ -137,7 +137,7 @@ SIGNATURES = {
     "pn_batch_set_stream": (c_int, [c_void_p, c_void_p]),
     "pn_batch_solve": (c_int, [c_void_p, c_int32]),
     "pn_batch_solve_noalloc": (c_int, [c_void_p, c_int32]),
-    "pn_batch_plan_stats": (c_int, [c_void_p, POINTER(c_int64), POINTER(c_int64), P_int32]),
+    "pn_batch_plan_stats": (c_int, [c_void_p, POINTER(c_int64), POINTER(c_int64), P_int32, P_int32, P_int32]),
     "pn_batch_synchronize": (c_int, [c_void_p]),
     "pn_batch_destroy": (c_int, [c_void_p]),
     "pn_partitioned_create": (c_int, [POINTER(PnMesh), POINTER(PnMaterialTable), c_double, c_int32, c_int32,

@@ -22,7 +22,7 @@
 // (kernel arguments are device pointers to the staged blocks plus the step).
 struct ChunkSignature {
   int form, precision, n, shape, chunk, total0, total1, sym, tma;
-  int reserved;  // keeps the pointers 8-byte aligned with no padding bytes (memcmp below)
+  int rows;  // grid form: tile rows (also keeps the pointers 8-byte aligned with no padding bytes)
   const void *p[4];
   bool operator==(const ChunkSignature &o) const { return std::memcmp(this, &o, sizeof(*this)) == 0; }
 };
@@ -39,6 +39,9 @@ struct pn_batch {
   // autotuner: launch shape chosen per (form, precision, member-count and
   // work-size class), by timing the candidates on real steps
   std::map<std::tuple<int, int, int, int>, int> tuned;
+  // launch shape of the last chunk (grid form: tile rows, z chunks per column
+  // with 0 = the launcher's choice; table form: 0, resident blocks per SM)
+  int last_rows = 0, last_shape = 0;
   // CUDA graph of the last chunk whose launch sequence repeated
   bool seen = false;
   ChunkSignature last{};
@@ -144,7 +147,9 @@ int32_t common_chunk(pn_batch *b, int32_t want, bool may_alloc = true) {
 // changes what a member computes (every node and cell is updated by one
 // thread with the same arithmetic), only how fast:
 //   table form  resident blocks per SM of the tile-walking kernels
-//   grid form   z chunks per tile column (blocks = tiles x chunks)
+//   grid form   tile rows (32 x 8 or, FP32 with the tensor-copy kernel, 32 x 16
+//               block tiles: members are re-tiled to try them) x z chunks per
+//               tile column (blocks = tiles x chunks)
 // The first chunk of a new (form, precision, members, work) class long
 // enough for it runs two steps with each candidate, twice in interleaved
 // rounds, timed with CUDA events on the batch stream, and keeps the candidate
@@ -154,7 +159,8 @@ int32_t common_chunk(pn_batch *b, int32_t want, bool may_alloc = true) {
 // (work on a created stream only; the legacy default stream cannot be
 // captured).  Neither runs in the allocation-free solve.
 constexpr int kTableShapes[] = {8, 4, 16, 2};  // blocks per SM
-constexpr int kGridShapes[] = {0, 1, 2};       // 0: the launcher's choice; else chunks per column
+constexpr int kGridChunkShapes[] = {0, 1, 2};  // 0: the launcher's choice; else chunks per column
+constexpr int kGridRowShapes[] = {8, 16};       // tile rows, where the storage has them
 constexpr int kTunePerShape = 2;               // timed steps per candidate and round
 constexpr int kTuneRounds = 2;
 
@@ -162,12 +168,12 @@ int log2_class(int64_t v) { return v <= 1 ? 0 : (int)std::log2((double)v); }
 
 template <typename Prepare, typename Launch>
 void run_chunk(pn_batch *b, std::tuple<int, int, int, int> cls, int n_shapes, int32_t chunk, bool may_plan,
-               ChunkSignature sig, Prepare &&prepare, Launch &&launch) {
+               ChunkSignature sig, int fallback, Prepare &&prepare, Launch &&launch) {
   int32_t k = 0;
   auto it = b->tuned.find(cls);
   int best = it == b->tuned.end() ? -1 : it->second;
   if (best < 0 && may_plan && n_shapes > 1 && chunk >= kTuneRounds * n_shapes * kTunePerShape + 1) {
-    constexpr int kMaxShapes = 4;
+    constexpr int kMaxShapes = 8;
     cudaEvent_t ev[kTuneRounds][2 * kMaxShapes];
     for (int r = 0; r < kTuneRounds; r++)
       for (int c = 0; c < 2 * n_shapes; c++) pn::ck(cudaEventCreate(&ev[r][c]), "tune event");
@@ -196,7 +202,7 @@ void run_chunk(pn_batch *b, std::tuple<int, int, int, int> cls, int n_shapes, in
       for (int c = 0; c < 2 * n_shapes; c++) cudaEventDestroy(ev[r][c]);
     b->tuned[cls] = best;
   }
-  if (best < 0) best = 0;
+  if (best < 0) best = fallback;
   const int units = prepare(best);  // work units of the shape (part of the launch sequence)
   if (k == 0 && may_plan && b->stream != nullptr) {
     sig.shape = best;
@@ -293,7 +299,9 @@ void solve_table(pn_batch *b, int32_t nsteps, int precision, const Stage &stage,
     L.vel_tiles = vs[n];
     L.str_tiles = ss[n];
     // blocks walk the tiles: resident blocks per SM by the tuned shape, never more than tiles
+    int staged = 0;
     auto shape = [&](int c) {
+      staged = c;
       L.blocks_vel = std::min(vs[n], sms * kTableShapes[c]);
       L.blocks_str = std::min(ss[n], sms * kTableShapes[c]);
       return 0;
@@ -309,11 +317,13 @@ void solve_table(pn_batch *b, int32_t nsteps, int precision, const Stage &stage,
     sig.p[2] = g.start[0];
     sig.p[3] = g.start[1];
     run_chunk(b, std::make_tuple((int)PN_FORM_TABLE, precision, log2_class(n), log2_class(vs[n] + ss[n])),
-              (int)(sizeof(kTableShapes) / sizeof(int)), chunk, may_alloc, sig, shape, [&](int c, int32_t k) {
+              (int)(sizeof(kTableShapes) / sizeof(int)), chunk, may_alloc, sig, 0, shape, [&](int c, int32_t k) {
                 shape(c);
                 pn::ck(pn::launch_table_batch(L, precision, k, b->stream), "batch step");
               });
     pn::ck(cudaStreamSynchronize(b->stream), "batch chunk");  // staging is reused next chunk
+    b->last_rows = 0;
+    b->last_shape = kTableShapes[staged];
     advance(b, chunk);
     done += chunk;
   }
@@ -325,19 +335,47 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision, const Stage &stage, 
   std::vector<pn::GridArgs<T>> ga[2] = {std::vector<pn::GridArgs<T>>(n), std::vector<pn::GridArgs<T>>(n)};
   std::vector<int> bs(n + 1, 0);
   std::vector<int> split(2 * (n + 1), 0);  // prefixes of the members' copies, then of their fix cells
-  const int tx = pn::grid_tile_x(), ty = pn::grid_tile_y();
+  const int tx = pn::kGridTileX;
   int sym = 2;
   bool tma = true;  // the tensor-copy kernel when every member has its maps
   for (pn_solver *s : b->members) tma = tma && s->d_tmaps != nullptr;
+  // launch shapes: (tile rows, z chunks per column) in a fixed order; the
+  // untuned and the allocation-free calls keep the members' current tile rows
+  bool same_rows = true;
+  for (pn_solver *s : b->members) same_rows = same_rows && s->tile_rows == b->members.front()->tile_rows;
+  if (!same_rows && !may_alloc)
+    throw pn::SetupError{PN_ERR_INVALID, "batch members are tiled differently; one pn_batch_solve call re-tiles "
+                                         "them"};
+  const int rows0 = same_rows ? b->members.front()->tile_rows : pn::kGridTileRows;
+  std::vector<std::pair<int, int>> shapes;
+  int keep = 0;  // (rows0, the launcher's chunks)
+  for (int rows : kGridRowShapes) {
+    if (rows != pn::kGridTileRows && (!tma || !pn::grid_tma_rows_supported(precision, rows))) continue;
+    for (int per : kGridChunkShapes) {
+      if (rows == rows0 && per == 0) keep = (int)shapes.size();
+      shapes.emplace_back(rows, per);
+    }
+  }
   int32_t done = 0;
   while (done < nsteps) {
     const int32_t chunk = common_chunk(b, nsteps - done, may_alloc);
-    // argument blocks of every member for z-chunk shape c (0: the launcher's
-    // choice, else c chunks per column), both step parities, staged
+    // argument blocks of every member for shape c (tile rows; z chunks: 0 the
+    // launcher's choice, else that many per column), both step parities,
+    // staged; members are re-tiled first when the shape's rows differ
     Staging g{};
     int staged_shape = -1;
     auto prepare = [&](int c) {
       if (c == staged_shape) return bs[n];
+      const int rows = shapes[c].first;
+      bool retile = false;
+      for (pn_solver *s : b->members) retile = retile || s->tile_rows != rows;
+      if (retile) {
+        if (!may_alloc) throw pn::SetupError{PN_ERR_INVALID, "re-tiling needs device allocation"};
+        pn::ck(cudaStreamSynchronize(b->stream), "retile sync");  // queued steps read the old tables
+        for (pn_solver *s : b->members)
+          if (!pn::grid_set_tile_rows(s, rows))
+            throw pn::SetupError{PN_ERR_INVALID, "member cannot take " + std::to_string(rows) + "-row tiles"};
+      }
       for (int m = 0; m < n; m++) {
         pn_solver *s = b->members[m];
         pn::GridArgs<T> a;
@@ -350,8 +388,8 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision, const Stage &stage, 
           a.sig_rows = (int32_t)(s->sig_rows - row0);
         }
         a.rec = s->rec_count;
-        const int per = kGridShapes[c];
-        a.kchunk = per == 0 ? pn::grid_chunk_layers(precision, a.nx, a.ny, a.nz, tma)
+        const int per = shapes[c].second;
+        a.kchunk = per == 0 ? pn::grid_chunk_layers(precision, a.nx, a.ny, a.nz, tma, rows)
                             : std::min(pn::kGridChunkMax, std::max(1, (a.nz + per - 1) / per));
         for (int p = 0; p < 2; p++) {  // step parity: buffers swap every step
           pn::GridArgs<T> q = a;
@@ -367,7 +405,7 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision, const Stage &stage, 
           }
           ga[p][m] = q;
         }
-        const int64_t blocks = (int64_t)(a.nx / (tx - 1) + 1) * (a.ny / (ty - 1) + 1) *
+        const int64_t blocks = (int64_t)(a.nx / (tx - 1) + 1) * (a.ny / (rows - 1) + 1) *
                                ((a.nz + a.kchunk - 1) / a.kchunk);
         bs[m + 1] = (int)(bs[m] + blocks);
         split[m + 1] = split[m] + a.n_copies;
@@ -391,9 +429,16 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision, const Stage &stage, 
       for (pn_solver *s : b->members) cubic = cubic && s->gfold != 1.0;
       if (cubic) sym |= 4;
     }
-    prepare(0);
     int64_t work = 0;
     for (pn_solver *s : b->members) work += (int64_t)s->grid.nx * s->grid.ny * s->grid.nz / 1024;
+    const auto key = std::make_tuple((int)PN_FORM_GRID, precision, log2_class(n), log2_class(work));
+    // the allocation-free call keeps the tiling: a tuned shape only when its rows match
+    int fallback = keep;
+    if (!may_alloc) {
+      auto it = b->tuned.find(key);
+      if (it != b->tuned.end() && shapes[it->second].first == rows0) fallback = it->second;
+    }
+    prepare(fallback);
     ChunkSignature sig{};
     sig.form = PN_FORM_GRID;
     sig.precision = precision;
@@ -404,8 +449,11 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision, const Stage &stage, 
     sig.p[1] = g.args[1];
     sig.p[2] = g.start[0];
     sig.p[3] = g.start[1];
-    run_chunk(b, std::make_tuple((int)PN_FORM_GRID, precision, log2_class(n), log2_class(work)),
-              (int)(sizeof(kGridShapes) / sizeof(int)), chunk, may_alloc, sig, prepare, [&](int c, int32_t k) {
+    sig.rows = shapes[fallback].first;
+    // (the allocation-free call looks up no tuned shape of its own: `fallback`)
+    run_chunk(b, may_alloc ? key : std::make_tuple(-1, 0, 0, 0), (int)shapes.size(), chunk, may_alloc, sig,
+              fallback, prepare,
+              [&](int c, int32_t k) {
                 prepare(c);
                 pn::GridBatchLaunch L;
                 L.n_members = n;
@@ -413,6 +461,7 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision, const Stage &stage, 
                 L.block_start = g.start[0];
                 L.total_blocks = bs[n];
                 L.sym = sym;
+                L.tile_rows = shapes[c].first;
                 pn::ck(tma ? pn::launch_grid_tma_batch(L, precision, k, b->stream)
                            : pn::launch_grid_batch(L, precision, k, b->stream),
                        "batch step");
@@ -428,6 +477,8 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision, const Stage &stage, 
                 }
               });
     pn::ck(cudaStreamSynchronize(b->stream), "batch chunk");
+    b->last_rows = shapes[staged_shape].first;
+    b->last_shape = shapes[staged_shape].second;
     advance(b, chunk);
     done += chunk;
   }
@@ -563,11 +614,14 @@ int pn_batch_solve_noalloc(pn_batch *b, int32_t nsteps) {
   });
 }
 
-int pn_batch_plan_stats(pn_batch *b, int64_t *graph_launches, int64_t *graph_captures, int32_t *tuned_classes) {
+int pn_batch_plan_stats(pn_batch *b, int64_t *graph_launches, int64_t *graph_captures, int32_t *tuned_classes,
+                        int32_t *tile_rows, int32_t *shape) {
   if (!b) return berr(PN_ERR_INVALID, "null batch");
   if (graph_launches) *graph_launches = b->graph_launches;
   if (graph_captures) *graph_captures = b->graph_captures;
   if (tuned_classes) *tuned_classes = (int32_t)b->tuned.size();
+  if (tile_rows) *tile_rows = b->last_rows;
+  if (shape) *shape = b->last_shape;
   return PN_OK;
 }
 

@@ -68,7 +68,7 @@ int64_t step_bytes(const pn_solver *s) {
   if (s->form == PN_FORM_GRID) {
     // S read + write, material byte per marched lattice cell; V read + write,
     // dt/rho per marched node (fixed at creation)
-    if (s->step_bytes_cached == 0) s->step_bytes_cached = grid_step_bytes(s->grid, s->mat.n_mat, e);
+    if (s->step_bytes_cached == 0) s->step_bytes_cached = grid_step_bytes(s->grid, s->mat.n_mat, e, s->tile_rows);
     return s->step_bytes_cached;
   }
   // per cell: S read in the velocity step, S read+write in the stress step,

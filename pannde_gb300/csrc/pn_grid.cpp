@@ -45,10 +45,10 @@ struct Tiles {
   }
 };
 
-Tiles tiles_of(const GridMap &g) {
+Tiles tiles_of(const GridMap &g, int tile_rows) {
   Tiles T;
-  T.tx = grid_tile_x();
-  T.ty = grid_tile_y();
+  T.tx = kGridTileX;
+  T.ty = tile_rows;
   T.nx = g.nx;
   T.ny = g.ny;
   T.nz = g.nz;
@@ -111,8 +111,8 @@ void ranges_of(std::vector<Keyed> &L, int64_t n_slots, std::vector<int32_t> &rng
 
 }  // namespace
 
-std::vector<int32_t> grid_tile_tops(const GridMap &g) {
-  const Tiles T = tiles_of(g);
+std::vector<int32_t> grid_tile_tops(const GridMap &g, int tile_rows) {
+  const Tiles T = tiles_of(g, tile_rows);
   std::vector<int32_t> top((size_t)T.blocks(), 0);
   for (int by = 0; by < T.by_count; by++)
     for (int bx = 0; bx < T.bx_count; bx++) {
@@ -151,8 +151,8 @@ bool grid_eligible(const MeshTables &m, const MaterialTables &mt, int precision,
   if (mt.n_mat >= 255) return no("more than 254 materials");
   int64_t marched = 0;
   if (want_tma(mt.n_mat)) {
-    const Tiles T = tiles_of(g);
-    const std::vector<int32_t> top = grid_tile_tops(g);
+    const Tiles T = tiles_of(g, kGridTileRows);
+    const std::vector<int32_t> top = grid_tile_tops(g, kGridTileRows);
     for (int by = 0; by < T.by_count; by++)
       for (int bx = 0; bx < T.bx_count; bx++) {
         const int64_t cols = std::min<int64_t>(T.tx - 1, g.nx - (int64_t)bx * (T.tx - 1)) *
@@ -171,10 +171,10 @@ bool grid_eligible(const MeshTables &m, const MaterialTables &mt, int precision,
 // per marched lattice node.  The tensor-copy kernel marches each tile's owned
 // columns up to its top solid layer (node layers 0..top; nothing when top is
 // 0), the classic kernel the whole box.
-int64_t grid_step_bytes(const GridMap &g, int32_t n_mat, int64_t e) {
+int64_t grid_step_bytes(const GridMap &g, int32_t n_mat, int64_t e, int tile_rows) {
   if (!want_tma(n_mat)) return g.grid_cells() * (12 * e + 1) + g.grid_nodes() * 7 * e;
-  const Tiles T = tiles_of(g);
-  const std::vector<int32_t> top = grid_tile_tops(g);
+  const Tiles T = tiles_of(g, tile_rows);
+  const std::vector<int32_t> top = grid_tile_tops(g, tile_rows);
   int64_t cells = 0, nodes = 0;
   for (int by = 0; by < T.by_count; by++)
     for (int bx = 0; bx < T.bx_count; bx++) {
@@ -193,7 +193,8 @@ int64_t grid_step_bytes(const GridMap &g, int32_t n_mat, int64_t e) {
 int64_t grid_footprint(const GridMap &g, const MaterialTables &mt, int precision) {
   const int64_t e = precision == PN_PREC_F32 ? 4 : 8;
   const int64_t gn = g.node_len(), gc = g.cell_sites();
-  const int64_t tiles = (int64_t)(g.nx / (grid_tile_x() - 1) + 1) * (g.ny / (grid_tile_y() - 1) + 1);
+  // (the default 32 x 8 tiles: more tiles than any other shape)
+  const int64_t tiles = (int64_t)(g.nx / (kGridTileX - 1) + 1) * (g.ny / (kGridTileRows - 1) + 1);
   // state (two halves), dt/rho, material bytes, stiffness rows, tensor maps,
   // per-tile top layers, error word and finiteness flags, split-site tables
   // (the copies' and fix cells' source and sensor entries come with those)
@@ -203,6 +204,64 @@ int64_t grid_footprint(const GridMap &g, const MaterialTables &mt, int precision
          (int64_t)g.fix_cell.size() * (int64_t)sizeof(FixCell) + 16;
 }
 
+
+namespace {
+
+// tensor maps of both input parities for tiles of `rows` rows (false: a
+// buffer or pitch the copies cannot take, or rows the storage has no kernel for)
+bool encode_maps(pn_solver *s, int rows, unsigned char *out) {
+  const GridMap &g = s->grid;
+  const size_t mb = grid_tma_maps_bytes();
+  bool ok = true;
+  for (int p = 0; p < 2 && ok; p++) {
+    const void *V[3] = {s->V[p][0], s->V[p][1], s->V[p][2]};
+    const void *S[6] = {s->S[p][0], s->S[p][1], s->S[p][2], s->S[p][3], s->S[p][4], s->S[p][5]};
+    ok = grid_tma_encode(s->precision, rows, g.nx, g.ny, g.nz, g.pnx, g.pcx, V, S, s->d_coef, s->d_gmat,
+                         out + p * mb);
+  }
+  return ok;
+}
+
+}  // namespace
+
+// Tile rows of a new solver's tensor-copy kernel (the batch tuner may change
+// them): 32 x 8 unless PN_GRID_TILE_ROWS names another shape the storage has.
+int grid_default_tile_rows(int precision, const GridMap &g) {
+  (void)g;
+  if (const char *v = std::getenv("PN_GRID_TILE_ROWS")) {
+    const int r = std::atoi(v);
+    if (grid_tma_rows_supported(precision, r)) return r;
+  }
+  return kGridTileRows;
+}
+
+// Re-tile a grid-form solver with the tensor-copy kernel: tensor maps, tile
+// tops, and the per-(tile, layer) source and sensor lists for `rows` rows.
+// Results do not depend on the tiling.  False (nothing changed) when the
+// solver has no tensor-copy kernel or its storage no such tiles.
+bool grid_set_tile_rows(pn_solver *s, int rows) {
+  if (s->form != PN_FORM_GRID || !s->d_tmaps) return rows == s->tile_rows;
+  if (rows == s->tile_rows) return true;
+  if (!grid_tma_rows_supported(s->precision, rows)) return false;
+  const size_t mb = grid_tma_maps_bytes();
+  std::vector<unsigned char> maps(2 * mb);
+  if (!encode_maps(s, rows, maps.data())) return false;
+  ck(cudaStreamSynchronize(s->stream), "retile sync");  // work in flight reads the old tables
+  s->tile_rows = rows;
+  s->upload_raw(s->d_tmaps, maps.data(), 2 * mb);
+  const std::vector<int32_t> top = grid_tile_tops(s->grid, rows);
+  s->release(s->d_ktop);
+  s->d_ktop = s->alloc<int32_t>(top.size() * sizeof(int32_t));
+  s->upload_raw(s->d_ktop, top.data(), top.size() * sizeof(int32_t));
+  s->step_bytes_cached = 0;
+  if (!s->src.empty() && !s->src_dirty) grid_sources(s);
+  if (s->n_sens > 0) {
+    s->release(s->d_srng); s->release(s->d_skey); s->release(s->d_sidx);
+    grid_sensors(s, s->sensor_pairs);
+  }
+  ck(cudaStreamSynchronize(s->stream), "retile upload");
+  return true;
+}
 
 void grid_create(pn_solver *s) {
   const GridMap &g = s->grid;
@@ -242,20 +301,17 @@ void grid_create(pn_solver *s) {
   s->cur = 0;
   s->d_err = s->alloc<int32_t>(16);
   ck(cudaMemsetAsync(s->d_err, 0, 16, s->stream), "memset");
+  s->tile_rows = kGridTileRows;
   if (want_tma(s->mat.n_mat)) {
+    const int rows = grid_default_tile_rows(s->precision, g);
     const size_t mb = grid_tma_maps_bytes();
     std::vector<unsigned char> maps(2 * mb);
-    bool ok = true;
-    for (int p = 0; p < 2 && ok; p++) {
-      const void *V[3] = {s->V[p][0], s->V[p][1], s->V[p][2]};
-      const void *S[6] = {s->S[p][0], s->S[p][1], s->S[p][2], s->S[p][3], s->S[p][4], s->S[p][5]};
-      ok = grid_tma_encode(s->precision, g.nx, g.ny, g.nz, g.pnx, g.pcx, V, S, s->d_coef, s->d_gmat,
-                           maps.data() + p * mb);
-    }
+    const bool ok = encode_maps(s, rows, maps.data());
     if (ok) {
+      s->tile_rows = rows;
       s->d_tmaps = s->alloc<void>(2 * mb);
       s->upload_raw(s->d_tmaps, maps.data(), 2 * mb);
-      const std::vector<int32_t> top = grid_tile_tops(g);
+      const std::vector<int32_t> top = grid_tile_tops(g, rows);
       s->d_ktop = s->alloc<int32_t>(top.size() * sizeof(int32_t));
       s->upload_raw(s->d_ktop, top.data(), top.size() * sizeof(int32_t));
       // a cubic lattice: every difference is scaled by the same 0.25/h, which
@@ -407,7 +463,7 @@ void grid_sources(pn_solver *s) {
   s->release(s->d_frng); s->release(s->d_fkey); s->release(s->d_fsig); s->release(s->d_fw);
   s->release(s->d_mrng); s->release(s->d_mkey); s->release(s->d_msig); s->release(s->d_mw);
   const GridMap &g = s->grid;
-  const Tiles T = tiles_of(g);
+  const Tiles T = tiles_of(g, s->tile_rows);
   s->n_force = (int32_t)fe.size();
   s->n_moment = (int32_t)me.size();
   s->n_src_nodes = s->n_src_cells = 0;
@@ -469,7 +525,8 @@ void grid_sources(pn_solver *s) {
 
 void grid_sensors(pn_solver *s, const std::vector<std::pair<int32_t, int32_t>> &pr) {
   const GridMap &g = s->grid;
-  const Tiles T = tiles_of(g);
+  const Tiles T = tiles_of(g, s->tile_rows);
+  if (&pr != &s->sensor_pairs) s->sensor_pairs = pr;  // kept for re-tiling
   std::vector<Keyed> L;
   s->split_sensors.clear();
   for (auto &p : pr) {
@@ -556,6 +613,7 @@ void grid_args(pn_solver *s, GridArgs<T> &a) {
   // tile copies unissued, so the tensor-copy kernel's bounded wait runs out
   const char *skip = std::getenv("PN_TEST_GRID_SKIP_COPY");
   a.test_skip_layer = skip && *skip ? std::atoi(skip) : kNoLayer;
+  a.tile_rows = s->tile_rows;
 }
 
 const void *grid_maps_for(const pn_solver *s, int in) {

@@ -87,6 +87,8 @@ struct pn_solver {
   void *d_tmaps = nullptr;   // tensor maps [2 input parities] (null: classic kernel)
   int32_t *d_ktop = nullptr; // [tiles] cell layers the tensor-copy kernel marches per tile
   mutable int64_t step_bytes_cached = 0;  // grid form: algorithmic bytes of one step (0: not yet)
+  int tile_rows = pn::kGridTileRows;      // grid form: rows TY of the 32 x TY block tiles
+  std::vector<std::pair<int32_t, int32_t>> sensor_pairs;  // grid form: (node, sensor) sorted, for re-tiling
   // cubic lattice with the tensor-copy kernel: 0.25/h folded into dt/rho, dt*C
   // and the force weights (the kernel's g is then 1); 1.0 when not folded
   double gfold = 1.0;
@@ -298,10 +300,15 @@ bool grid_eligible(const MeshTables &m, const MaterialTables &mt, int precision,
                    std::string *why = nullptr);
 // per tile: 1 + the highest solid cell layer in the columns of its cell box
 // with the apron, i.e. the cell layers the tensor-copy kernel marches
-std::vector<int32_t> grid_tile_tops(const GridMap &g);
+std::vector<int32_t> grid_tile_tops(const GridMap &g, int tile_rows = kGridTileRows);
+// tile rows a new solver's tensor-copy kernel starts with
+int grid_default_tile_rows(int precision, const GridMap &g);
+// re-tile a solver's tensor-copy kernel (maps, tile tops, source and sensor
+// lists); false when it has no such kernel or tiles of that many rows
+bool grid_set_tile_rows(pn_solver *s, int rows);
 int64_t grid_footprint(const GridMap &g, const MaterialTables &mt, int precision);
 // algorithmic HBM bytes of one grid step over the lattice the kernel marches
-int64_t grid_step_bytes(const GridMap &g, int32_t n_mat, int64_t e);
+int64_t grid_step_bytes(const GridMap &g, int32_t n_mat, int64_t e, int tile_rows = kGridTileRows);
 void grid_create(pn_solver *s);
 void grid_sources(pn_solver *s);
 void grid_sensors(pn_solver *s, const std::vector<std::pair<int32_t, int32_t>> &sorted);

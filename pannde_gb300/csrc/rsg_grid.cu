@@ -395,8 +395,6 @@ cudaError_t launch_batch_sym(const GridBatchLaunch &b, int step, cudaStream_t st
 
 }  // namespace
 
-int grid_tile_x() { return 32; }
-int grid_tile_y() { return 8; }
 
 int grid_chunk_for(int nz, long long xy_blocks, int sms, int per_sm) {
   if (nz <= 0) return 1;
@@ -415,17 +413,18 @@ int grid_chunk_for(int nz, long long xy_blocks, int sms, int per_sm) {
   return (int)((nz + chunks - 1) / chunks);
 }
 
-int grid_chunk_layers(int precision, int nx, int ny, int nz, bool tma) {
+int grid_chunk_layers(int precision, int nx, int ny, int nz, bool tma, int tile_rows) {
   int sms = 0, per_sm = 0;
   cudaError_t e = precision == 2 ? Setup<float, 32, 8, 0>::ensure(sms, per_sm)
                 : precision == 3 ? Setup<df64, 32, 8, 0>::ensure(sms, per_sm)
                                  : Setup<double, 32, 8, 0>::ensure(sms, per_sm);
   if (e != cudaSuccess || nz <= 0) return std::min(std::max(nz, 1), kGridChunkMax);
+  if (!tma) tile_rows = kGridTileRows;
   if (tma) {
-    const int p = grid_tma_blocks_per_sm(precision);
+    const int p = grid_tma_blocks_per_sm(precision, tile_rows);
     if (p > 0) per_sm = p;
   }
-  const long long xy = (long long)(nx / 31 + 1) * (ny / 7 + 1);
+  const long long xy = (long long)(nx / (kGridTileX - 1) + 1) * (ny / (tile_rows - 1) + 1);
   return grid_chunk_for(nz, xy, sms, per_sm);
 }
 

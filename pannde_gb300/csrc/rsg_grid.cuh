@@ -82,6 +82,7 @@ struct GridArgs {
   const int32_t *cm_sig;
   const T *cm_w;
   int32_t test_skip_layer;  // failure-path test: the layer whose copies are never issued (kNoLayer: none)
+  int32_t tile_rows;        // rows TY of the 32 x TY block tile (8, or 16 with the tensor-copy kernel)
 };
 
 constexpr int32_t kNoLayer = INT32_MIN;  // no layer index (layers run from -1 to nz)
@@ -89,14 +90,16 @@ constexpr int32_t kNoLayer = INT32_MIN;  // no layer index (layers run from -1 t
 constexpr int kGridChunkMax = 64;     // cell layers per z chunk, at most
 constexpr int kGridTmaRowsMax = 32;   // stiffness rows the tensor-copy kernel stages
 
-int grid_tile_x();
-int grid_tile_y();
+// block tiles: 32 x TY threads, one warp per row; TY = 8 everywhere, 16 as
+// well for the tensor-copy kernel with FP32 storage
+constexpr int kGridTileX = 32;
+constexpr int kGridTileRows = 8;  // the classic kernel's, and the default
 // cell layers per z chunk: about one wave of blocks, at least four layers,
 // at most kGridChunkMax
 int grid_chunk_for(int nz, long long xy_blocks, int sms, int per_sm);
 // cell layers per z chunk the launcher picks for this lattice, precision and
 // kernel (tma: the tensor-copy kernel of rsg_grid_tma.cu)
-int grid_chunk_layers(int precision, int nx, int ny, int nz, bool tma);
+int grid_chunk_layers(int precision, int nx, int ny, int nz, bool tma, int tile_rows = kGridTileRows);
 
 // a batch of grid-form members: argument blocks (kchunk set) and the prefix
 // of their block counts ((nx/(TX-1)+1) * (ny/(TY-1)+1) * chunks each)
@@ -106,6 +109,7 @@ struct GridBatchLaunch {
   const int *block_start;  // [n_members + 1]
   int total_blocks;
   int sym;                 // most general symmetry class among the members
+  int tile_rows;           // TY of every member's tiles
 };
 cudaError_t launch_grid_batch(const GridBatchLaunch &b, int precision, int step, cudaStream_t st);
 cudaError_t launch_grid_f32(const GridArgs<float> &a, int sym, cudaStream_t st);
@@ -116,9 +120,12 @@ cudaError_t launch_grid_df64(const GridArgs<float2> &a, int sym, cudaStream_t st
 // grid_tma_maps_bytes(); encoding fails (false) when a buffer or pitch does not
 // meet the copy's alignment rules
 size_t grid_tma_maps_bytes();
-bool grid_tma_encode(int precision, int nx, int ny, int nz, int pnx, int pcx, const void *const V[3],
-                     const void *const S[6], const void *coef, const uint8_t *mat, void *out);
-int grid_tma_blocks_per_sm(int precision);
+// tile rows the tensor-copy kernel has for this storage (8; 16 for FP32)
+bool grid_tma_rows_supported(int precision, int tile_rows);
+bool grid_tma_encode(int precision, int tile_rows, int nx, int ny, int nz, int pnx, int pcx,
+                     const void *const V[3], const void *const S[6], const void *coef, const uint8_t *mat,
+                     void *out);
+int grid_tma_blocks_per_sm(int precision, int tile_rows = kGridTileRows);
 cudaError_t launch_grid_tma(const void *args /* GridArgs<storage type> */, int precision, int sym,
                             cudaStream_t st);
 cudaError_t launch_grid_tma_batch(const GridBatchLaunch &b, int precision, int step, cudaStream_t st);

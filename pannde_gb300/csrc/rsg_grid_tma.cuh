@@ -1,0 +1,642 @@
+// rsg_grid_tma.cuh -- the fused voxel-grid step with tensor-copy (TMA) staging
+// (templates; rsg_grid_tma.cu instantiates 32 x 8 tiles for every storage
+// type plus the dispatch and the tensor-map encoding, rsg_grid_tma16.cu 32 x 16
+// tiles for FP32 storage).
+//
+// Same arithmetic as rsg_grid.cu (a block owns a 31 x (TY-1) column of nodes
+// and cells over a chunk of layers; its 32 x TY threads are the nodes plus a
+// one-node apron on +x / +y; TY = 8 or 16 rows), but every per-layer input
+// tile arrives in shared memory by cp.async.bulk.tensor, issued by one thread
+// one layer ahead and completed on an mbarrier:
+//   slot ring (4 layers)    S_in[6] cell tile (33 x (TY+1) used, x rounded down
+//                           to the 16-byte boundary), material tile (31 x (TY-1))
+//   node ring (2 layers)    V_in[3] and coef node tiles (32 x TY used)
+// No thread holds prefetched values in registers and the loads never stall an
+// instruction stream; out-of-lattice elements arrive as zeros (the tensor
+// copy's fill), which is the void-site value.
+//
+// One __syncthreads per layer: iteration k runs
+//   B(k)    velocity of node layer k from cell layers k-1 (partial sums in
+//           registers) and k (slot k), written to the computed-velocity tile
+//           k&1 and, for owned nodes, to V_out (HostRSGTDUT.hpp:338-362)
+//   C(k-2)  stress of cell layer k-2 from node layers k-2 (partial sums in
+//           registers) and k-1 (computed tile (k-1)&1, complete since the
+//           previous barrier) (HostRSGTDUT.hpp:278-293)
+// and thread 0 first issues the copies of layer k+1 into slot (k+1)&3, whose
+// previous layer k-3 was last read before the previous barrier.
+//
+// Every wait is bounded (about one second of %globaltimer); a wait that gives
+// up records an error word for the host, the block drains its own copies in
+// flight (again bounded) and returns.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <type_traits>
+
+#include "df64.cuh"
+#include "rsg_common.cuh"
+#include "rsg_grid.cuh"
+
+namespace pn {
+namespace {
+
+constexpr int TX = 32;  // a tile row is one warp
+constexpr int KC_MAX = kGridChunkMax;  // cell layers per chunk (source-range staging)
+constexpr int ROWS_MAX = kGridTmaRowsMax;
+
+struct GridMaps {
+  CUtensorMap S[6];
+  CUtensorMap V[3];
+  CUtensorMap coef;
+  CUtensorMap mat;
+};
+
+// shared-memory geometry for a storage element of ESZ bytes.  Copies run PD
+// layers ahead of the layer being computed.  A layer's stress tile is read in
+// its own iteration (velocity half) and, with OWN_SMEM, two iterations later
+// (a cell's old stress in the stress half; without it that value comes from
+// global memory, mostly L2, which needs fewer slots: the room for a third
+// block per SM with 8-byte storage).  Slots per ring: stress PD + 1 (+ 2 with
+// OWN_SMEM), velocity + dt/rho PD + 1, material PD + 3 (read in the stress
+// half, two iterations after its layer's).
+template <int ESZ, int TY>
+struct Geo {
+  static constexpr int NT = TX * TY;
+  static constexpr int PD = 1;
+  static constexpr bool OWN_SMEM = ESZ == 4;
+  static constexpr int NS = PD + 1 + (OWN_SMEM ? 2 : 0);
+  static constexpr int NV = PD + 1;
+  static constexpr int NM = PD + 3;
+  static constexpr int A = 16 / ESZ;              // x alignment of a copy (elements)
+  static constexpr int BWC = ESZ == 4 ? 36 : 34;  // cell tile width: offset (< A) + 33
+  static constexpr int BWN = ESZ == 4 ? 36 : 34;  // node tile width: offset (< A) + 32
+  static constexpr int BWM = 48;                  // material tile width: offset (< 16) + 31
+  static constexpr int SBOX_BYTES = BWC * (TY + 1) * ESZ;
+  static constexpr int SBOX = (SBOX_BYTES + 127) / 128 * 128;
+  static constexpr int VBOX = BWN * TY * ESZ;
+  static constexpr int MBOX_BYTES = BWM * (TY - 1);
+  static constexpr int MBOX = (MBOX_BYTES + 127) / 128 * 128;
+  static constexpr int SLOT = 6 * SBOX;                        // S[6] of one layer
+  static constexpr int VSLOT = 4 * VBOX;                       // V[3], dt/rho of one layer
+  static constexpr uint32_t TX_BYTES = 6 * SBOX_BYTES + 4 * VBOX + MBOX_BYTES;
+  static constexpr int OFF_V = NS * SLOT;                      // velocity ring [NV]
+  static constexpr int OFF_M = OFF_V + NV * VSLOT;             // material ring [NM]
+  static constexpr int OFF_VT = OFF_M + NM * MBOX;             // computed velocity [2][3][NT]
+  static constexpr int OFF_C = OFF_VT + 2 * 3 * NT * ESZ;      // dt*C rows [ROWS_MAX][36]
+  static constexpr int OFF_R = OFF_C + ROWS_MAX * 36 * ESZ;    // ranges f, s [KC_MAX+2], m [KC_MAX]
+  static constexpr int OFF_B = OFF_R + (3 * KC_MAX + 4) * 8;   // mbarriers [NS]
+  static constexpr int BYTES = OFF_B + NS * 8;
+  static constexpr size_t SMEM = BYTES + 128;                  // + base alignment
+  static_assert(SLOT % 128 == 0 && VBOX % 128 == 0 && OFF_V % 128 == 0 && OFF_M % 128 == 0 && OFF_B % 8 == 0,
+                "alignment");
+  static_assert(SBOX % ESZ == 0 && VBOX % ESZ == 0, "element size");
+};
+
+template <typename R> struct GNum;
+template <> struct GNum<float> {
+  using S = float;
+  static __device__ __forceinline__ float ld(const float *p, int64_t i) { return __ldg(p + i); }
+  static __device__ __forceinline__ float val(float v) { return v; }
+  static __device__ __forceinline__ float sto(float v) { return v; }
+  static __device__ __forceinline__ void st(float *p, int64_t i, float v) { p[i] = v; }
+  static __device__ __forceinline__ double dbl(float v) { return (double)v; }
+};
+template <> struct GNum<double> {
+  using S = double;
+  static __device__ __forceinline__ double ld(const double *p, int64_t i) { return __ldg(p + i); }
+  static __device__ __forceinline__ double val(double v) { return v; }
+  static __device__ __forceinline__ double sto(double v) { return v; }
+  static __device__ __forceinline__ void st(double *p, int64_t i, double v) { p[i] = v; }
+  static __device__ __forceinline__ double dbl(double v) { return v; }
+};
+template <> struct GNum<df64> {
+  using S = float2;
+  static __device__ __forceinline__ df64 ld(const float2 *p, int64_t i) {
+    const float2 v = __ldg(p + i);
+    return df64(v.x, v.y);
+  }
+  static __device__ __forceinline__ df64 val(float2 v) { return df64(v.x, v.y); }
+  static __device__ __forceinline__ float2 sto(df64 v) { return make_float2(v.hi, v.lo); }
+  static __device__ __forceinline__ void st(float2 *p, int64_t i, df64 v) { p[i] = make_float2(v.hi, v.lo); }
+  static __device__ __forceinline__ double dbl(df64 v) { return (double)v.hi + (double)v.lo; }
+};
+
+__host__ __device__ constexpr bool c_used(int sym, int k, int j) {
+  return sym == 0 ? true
+       : sym == 2 ? ((k < 3 && j < 3) || k == j)
+                  : ((k < 3 && j < 3) || k == j || (k == 5 && j < 3) || (j == 5 && k < 3) ||
+                     (k == 3 && j == 4) || (k == 4 && j == 3));
+}
+
+// ---- PTX wrappers: mbarrier, tensor copy, timer -------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// wait for phase `parity` of the barrier; false after about one second (the
+// loop out of line: the first try usually succeeds)
+__device__ __noinline__ bool mbar_wait_slow(uint32_t bar, uint32_t parity) {
+  const uint64_t t0 = global_ns();
+  for (uint32_t n = 1;; n++) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((n & 63) == 0 && global_ns() - t0 > 1000000000ull) return false;
+  }
+}
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  return mbar_try_wait(bar, parity) || mbar_wait_slow(bar, parity);
+}
+// the whole wait out of line (fewer registers live across it: the batch
+// kernel, which reads its arguments through global memory)
+__device__ __noinline__ bool mbar_wait_call(uint32_t bar, uint32_t parity) {
+  return mbar_try_wait(bar, parity) || mbar_wait_slow(bar, parity);
+}
+__device__ __forceinline__ void proxy_fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void tma_prefetch_map(const void *map) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(map) : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const void *map, int x, int y, int z, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ int floor_to(int v, int m) {  // largest multiple of m <= v (m > 0)
+  return v >= 0 ? v / m * m : -((-v + m - 1) / m) * m;
+}
+
+// error word codes
+constexpr int32_t kErrWait = 1;
+
+template <typename R, int SYM, int TY, bool BATCH = false>
+__device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::S> &a, const GridMaps *M,
+                                               int bx, int by, int bz, int gxc, int step) {
+  using N = GNum<R>;
+  using St = typename N::S;
+  using G = Geo<(int)sizeof(St), TY>;
+  constexpr int NT = G::NT;
+  // SYM: material symmetry class (bits 0-1, see c_used) | 4 when the lattice is
+  // cubic and 0.25/h has been folded into the coefficients (g = 1)
+  constexpr bool CUBIC = (SYM & 4) != 0;
+  constexpr int SB = G::SBOX / (int)sizeof(St);  // field stride in a slot (elements)
+  constexpr int VB = G::VBOX / (int)sizeof(St);
+  extern __shared__ unsigned char smem_raw[];
+  // 128-byte aligned base.  A single launch derives it from smem_raw by an
+  // offset, so that every tile pointer stays in the shared state space (shared
+  // loads and stores, 32-bit addressing: FP32 45.4 -> 47.8, double-float 18.0
+  // -> 19.3 Gcell-steps/s on the laminate).  The batch kernel, which reads its
+  // arguments through global memory, spilled with that and ran slower; it keeps
+  // the generic pointer.
+  unsigned char *base = BATCH ? (unsigned char *)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127)
+                              : smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+  St *sVt = reinterpret_cast<St *>(base + G::OFF_VT);
+  St *sC = reinterpret_cast<St *>(base + G::OFF_C);
+  int2 *sRf = reinterpret_cast<int2 *>(base + G::OFF_R);
+  int2 *sRs = sRf + (KC_MAX + 2);
+  int2 *sRm = sRs + (KC_MAX + 2);
+  const uint32_t bars = smem_u32(base + G::OFF_B);
+
+  const int t = threadIdx.x;
+  const int tx = t % TX, ty = t / TX;
+  const int i0 = bx * (TX - 1), j0 = by * (TY - 1);
+  const int blk = by * gxc + bx;
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+  const int i = i0 + tx, j = j0 + ty;
+  const bool node_own = (i <= nx) && (j <= ny) && tx < TX - 1 && ty < TY - 1;
+  const bool cell_own = tx < TX - 1 && ty < TY - 1 && i < nx && j < ny;
+  const int64_t nplane = (int64_t)a.pnx * (ny + 1), cplane = (int64_t)a.pcx * ny;
+  const int64_t nidx0 = (int64_t)j * a.pnx + i;
+  const int64_t cidx0 = (int64_t)j * a.pcx + i;
+  const R gx = N::val(a.g[0]), gy = N::val(a.g[1]), gz = N::val(a.g[2]);
+  const St *sigrow = a.sigval ? a.sigval + (int64_t)min(step, a.sig_rows - 1) * a.sig_stride : nullptr;
+  const int64_t rec = a.rec + step;
+  // columns of the tile (and its apron) hold no solid cell at or above ktop:
+  // the march ends there, and a chunk above it has nothing to do
+  const int ktop = a.ktop ? min(nz, __ldg(a.ktop + blk)) : nz;
+  const int k0 = bz * a.kchunk, k1 = min(ktop, k0 + a.kchunk);
+  if (k0 >= ktop) return;
+  const bool last_chunk = k1 == ktop;
+
+  // tile origins of the copies (x on the 16-byte boundary) and offsets in them
+  const int xs_c = floor_to(i0 - 1, G::A), oc = i0 - 1 - xs_c;
+  const int xs_n = floor_to(i0, G::A), on = i0 - xs_n;
+  const int xs_m = floor_to(i0, 16), om = i0 - xs_m;
+
+  // layer L is copy number u = L - k0 + 1 of the block: stress slot and
+  // mbarrier u % NS (phase (u / NS) & 1), velocity slot u % NV, material slot u % NM
+  auto ucount = [&](int L) { return (uint32_t)(L - k0 + 1); };
+  auto sslot = [&](int L) { return base + (ucount(L) % G::NS) * G::SLOT; };
+  auto vslot = [&](int L) { return base + G::OFF_V + (ucount(L) % G::NV) * G::VSLOT; };
+  auto mslot = [&](int L) { return base + G::OFF_M + (ucount(L) % G::NM) * G::MBOX; };
+  auto bar_of = [&](int L) { return bars + 8u * (ucount(L) % G::NS); };
+  auto parity = [&](int L) { return (ucount(L) / G::NS) & 1u; };
+  auto issue = [&](int L) {  // thread 0: copies of layer L
+    if (L == a.test_skip_layer) return;  // failure-path test: this layer's wait runs out
+    const uint32_t bar = bar_of(L);
+    unsigned char *sl = sslot(L), *vl = vslot(L);
+    mbar_expect_tx(bar, G::TX_BYTES);
+#pragma unroll
+    for (int f = 0; f < 6; f++) tma_load_3d(smem_u32(sl + f * G::SBOX), &M->S[f], xs_c, j0 - 1, L, bar);
+#pragma unroll
+    for (int c = 0; c < 3; c++) tma_load_3d(smem_u32(vl + c * G::VBOX), &M->V[c], xs_n, j0, L, bar);
+    tma_load_3d(smem_u32(vl + 3 * G::VBOX), &M->coef, xs_n, j0, L, bar);
+    tma_load_3d(smem_u32(mslot(L)), &M->mat, xs_m, j0, L, bar);
+  };
+
+  if (t == 0) {
+#pragma unroll
+    for (int f = 0; f < 6; f++) tma_prefetch_map(&M->S[f]);
+#pragma unroll
+    for (int c = 0; c < 3; c++) tma_prefetch_map(&M->V[c]);
+    tma_prefetch_map(&M->coef);
+    tma_prefetch_map(&M->mat);
+#pragma unroll
+    for (int s = 0; s < G::NS; s++) mbar_init(bars + 8u * s, 1);
+    mbar_init_fence();
+  }
+  // per-chunk tables: stiffness rows, source and sensor ranges
+  for (int q = t; q < a.n_rows * 36; q += NT) sC[q] = a.ctab[q];
+  const int nL = k1 - k0 + 2;  // node layers k0-1 .. k1
+  for (int q = t; q < nL; q += NT) {
+    const int k = k0 - 1 + q;
+    const bool ok = k >= 0 && k <= nz;
+    sRf[q] = (a.f_rng && ok) ? a.f_rng[(int64_t)blk * (nz + 1) + k] : make_int2(0, 0);
+    sRs[q] = (a.s_rng && ok) ? a.s_rng[(int64_t)blk * (nz + 1) + k] : make_int2(0, 0);
+  }
+  for (int q = t; q < k1 - k0; q += NT) sRm[q] = a.m_rng ? a.m_rng[(int64_t)blk * nz + k0 + q] : make_int2(0, 0);
+  __syncthreads();
+  // the copies are issued (and, on failure, drained) by the first thread of
+  // the last warp: its row is the tile's apron, which has no stress half
+  constexpr int ISSUER = (TY - 1) * TX;
+  if (t == ISSUER) {
+#pragma unroll
+    for (int d = 0; d <= G::PD; d++)
+      if (k0 - 1 + d <= k1) issue(k0 - 1 + d);
+  }
+
+  // per cell layer: A = (x, y differences) + z sum, B = the same - z sum; a
+  // node's acceleration is A of the layer above + B of the layer below
+  R blx = R(), bly = R(), blz = R();  // B of the layer below
+  R spx[3], spy[3], ss[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) spx[c] = spy[c] = ss[c] = R();
+  const int ra = ty * G::BWC + oc + tx;  // cell (i-1, j-1) in the cell tile
+  const int rv = ty * G::BWN + on + tx;  // node (i, j) in the node tile
+  int waited = k0 - 2;                   // last layer this thread has waited for
+  bool fail = false;
+
+  // FP32 storage: two layers per unrolled body, so the values carried from
+  // one layer to the next alternate registers instead of moving
+#pragma unroll(sizeof(St) == 4 ? 2 : 1)
+  for (int k = k0 - 1; k <= k1 + 1; k++) {
+    if (t == ISSUER && k >= k0 && k + G::PD <= k1) {
+      proxy_fence_async_smem();
+      issue(k + G::PD);
+    }
+    // ---- B: velocity of node layer k
+    if (k <= k1) {
+      if (BATCH ? mbar_wait_call(bar_of(k), parity(k)) : mbar_wait(bar_of(k), parity(k))) waited = k;
+      else fail = true;
+      const St *Sk = reinterpret_cast<const St *>(sslot(k));
+      auto cellv = [&](int f, int q) { return N::val(Sk[f * SB + q]); };
+      const int ib = ra + 1, id = ra + G::BWC, ic = id + 1;
+      R A, B, C, D;
+      A = cellv(0, ra); B = cellv(0, ib); C = cellv(0, ic); D = cellv(0, id);
+      const R px0 = diff22(B, C, A, D);
+      A = cellv(1, ra); B = cellv(1, ib); C = cellv(1, ic); D = cellv(1, id);
+      const R py1 = diff22(C, D, A, B);
+      A = cellv(2, ra); B = cellv(2, ib); C = cellv(2, ic); D = cellv(2, id);
+      const R s2 = sum22(A, B, C, D);
+      A = cellv(3, ra); B = cellv(3, ib); C = cellv(3, ic); D = cellv(3, id);
+      R py3, s3;
+      diffsum22(A, B, C, D, py3, s3);
+      A = cellv(4, ra); B = cellv(4, ib); C = cellv(4, ic); D = cellv(4, id);
+      R px4, s4;
+      diffsum22(A, D, B, C, px4, s4);
+      A = cellv(5, ra); B = cellv(5, ib); C = cellv(5, ic); D = cellv(5, id);
+      R px5, py5;
+      diffdiff22(A, B, C, D, px5, py5);
+      // x: Sxx along x, Sxy along y, Sxz along z; y: Sxy, Syy, Syz; z: Sxz, Syz, Szz
+      R tx, ty, tz, ax, ay, az, nbx, nby, nbz;
+      if constexpr (CUBIC) {  // 0.25/h folded into dt/rho and the force weights
+        tx = px0 + py5;
+        ty = px5 + py1;
+        tz = px4 + py3;
+        ax = tx + s4;
+        ay = ty + s3;
+        az = tz + s2;
+        nbx = tx - s4;
+        nby = ty - s3;
+        nbz = tz - s2;
+      } else {
+        tx = madd(gy, py5, gx * px0);
+        ty = madd(gy, py1, gx * px5);
+        tz = madd(gy, py3, gx * px4);
+        ax = madd(gz, s4, tx);
+        ay = madd(gz, s3, ty);
+        az = madd(gz, s2, tz);
+        nbx = madd(-gz, s4, tx);
+        nby = madd(-gz, s3, ty);
+        nbz = madd(-gz, s2, tz);
+      }
+      if (k >= k0) {
+        ax = ax + blx;
+        ay = ay + bly;
+        az = az + blz;
+        const int2 fr = sRf[k - k0 + 1];
+        for (int e = fr.x; e < fr.y; e++) {  // force sources of this block and layer
+          const int key = __ldg(a.f_key + e);
+          if ((key & 0xffff) != t) continue;
+          const R w = N::val(a.f_w[e]), sg = N::val(sigrow[__ldg(a.f_sig + e)]);
+          const int d = key >> 16;
+          if (d == 0) ax = madd(w, sg, ax);
+          else if (d == 1) ay = madd(w, sg, ay);
+          else az = madd(w, sg, az);
+        }
+        const St *Vk = reinterpret_cast<const St *>(vslot(k));
+        R vn[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) vn[c] = N::val(Vk[c * VB + rv]);
+        // dt/rho is 0 at void and padding sites, whose differences are 0 too:
+        // the update leaves them unchanged without a branch
+        const R cf = N::val(Vk[3 * VB + rv]);
+        vn[0] = madd(cf, ax, vn[0]);
+        vn[1] = madd(cf, ay, vn[1]);
+        vn[2] = madd(cf, az, vn[2]);
+        St *Vt = sVt + (k & 1) * 3 * NT;
+#pragma unroll
+        for (int c = 0; c < 3; c++) Vt[c * NT + t] = N::sto(vn[c]);
+        if (node_own && (k < k1 || last_chunk)) {
+          const int64_t n = (int64_t)k * nplane + nidx0;
+#pragma unroll
+          for (int c = 0; c < 3; c++) N::st(a.V_out[c], n, vn[c]);
+          const int2 sr = sRs[k - k0 + 1];
+          if (rec < a.rec_cap) {
+            for (int e = sr.x; e < sr.y; e++) {  // sensor traces
+              if (__ldg(a.s_key + e) != t) continue;
+              double *tr = a.traces + (rec * a.n_sens + __ldg(a.s_idx + e)) * 3;
+              tr[0] = N::dbl(vn[0]);
+              tr[1] = N::dbl(vn[1]);
+              tr[2] = N::dbl(vn[2]);
+            }
+          }
+        }
+      }
+      blx = nbx;
+      bly = nby;
+      blz = nbz;
+    }
+
+    // ---- C: partial sums of node layer k-1, stress of cell layer k-2
+    if (k - 1 >= k0 && k - 1 <= k1 && tx < TX - 1 && ty < TY - 1) {
+      const St *Vt = sVt + ((k - 1) & 1) * 3 * NT;
+      const int ia = t, ib = t + 1, ic = t + TX + 1, id = t + TX;
+      R px[3], py[3], s[3];
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const R A = N::val(Vt[c * NT + ia]), B = N::val(Vt[c * NT + ib]);
+        const R C = N::val(Vt[c * NT + ic]), D = N::val(Vt[c * NT + id]);
+        px[c] = diff22(B, C, A, D);
+        diffsum22(A, B, C, D, py[c], s[c]);
+      }
+      const int kc = k - 2;
+      if (kc >= k0 && cell_own) {
+        const R d00 = spx[0] + px[0], d10 = spy[0] + py[0], d20 = s[0] - ss[0];
+        const R d01 = spx[1] + px[1], d11 = spy[1] + py[1], d21 = s[1] - ss[1];
+        const R d02 = spx[2] + px[2], d12 = spy[2] + py[2], d22 = s[2] - ss[2];
+        R e[6];
+        if constexpr (CUBIC) {  // 0.25/h folded into dt*C
+          e[0] = d00;
+          e[1] = d11;
+          e[2] = d22;
+          e[3] = d12 + d21;
+          e[4] = d02 + d20;
+          e[5] = d01 + d10;
+        } else {
+          e[0] = gx * d00;
+          e[1] = gy * d11;
+          e[2] = gz * d22;
+          e[3] = madd(gz, d21, gy * d12);
+          e[4] = madd(gz, d20, gx * d02);
+          e[5] = madd(gy, d10, gx * d01);
+        }
+        const int64_t cg = (int64_t)kc * cplane + cidx0;
+        const int row = mslot(kc)[ty * G::BWM + om + tx];
+        const St *Cm = sC + 36 * row;
+        R acc[6];  // the cell's stress before the update
+        if constexpr (G::OWN_SMEM) {
+          const St *Sc = reinterpret_cast<const St *>(sslot(kc));
+          const int own = ra + G::BWC + 1;  // cell (i, j)
+#pragma unroll
+          for (int f = 0; f < 6; f++) acc[f] = N::val(Sc[f * SB + own]);
+        } else {  // in L2: its tile was copied two layers ago
+#pragma unroll
+          for (int f = 0; f < 6; f++) acc[f] = N::ld(a.S_in[f], cg);
+        }
+        const int2 mr = sRm[kc - k0];
+        for (int ee = mr.x; ee < mr.y; ee++) {  // moment sources of this block and cell layer
+          const int key = __ldg(a.m_key + ee);
+          if ((key & 0xffff) != t) continue;
+          const R w = N::val(a.m_w[ee]), sg = N::val(sigrow[__ldg(a.m_sig + ee)]);
+          const int kk = key >> 16;
+#pragma unroll
+          for (int f = 0; f < 6; f++)
+            if (f == kk) acc[f] = madd(w, sg, acc[f]);
+        }
+        // FP64 (bound by the FP64 pipe): when every active lane's row is
+        // orthotropic (C11..C33 block and the shear diagonal only: a laminate's
+        // 0/90 plies beside its +-45 ones), the 12-term product; the others are
+        // zero.  (The FP32-pipe forms measured no gain or a loss from the vote.)
+        bool ortho = (SYM & 3) == 2;
+        if constexpr ((SYM & 3) != 2 && std::is_same<R, double>::value)
+          ortho = __all_sync(__activemask(), (a.ortho_rows >> row) & 1u);
+        if (ortho) {
+#pragma unroll
+          for (int kk = 0; kk < 6; kk++) {
+#pragma unroll
+            for (int jj = 0; jj < 6; jj++)
+              if (c_used(2, kk, jj)) acc[kk] = madd(N::val(Cm[6 * kk + jj]), e[jj], acc[kk]);
+            N::st(a.S_out[kk], cg, acc[kk]);
+          }
+        } else {
+#pragma unroll
+          for (int kk = 0; kk < 6; kk++) {
+#pragma unroll
+            for (int jj = 0; jj < 6; jj++)
+              if (c_used(SYM & 3, kk, jj)) acc[kk] = madd(N::val(Cm[6 * kk + jj]), e[jj], acc[kk]);
+            N::st(a.S_out[kk], cg, acc[kk]);
+          }
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        spx[c] = px[c];
+        spy[c] = py[c];
+        ss[c] = s[c];
+      }
+    }
+    if (__syncthreads_or(fail)) {
+      // give up: record, drain this block's copies in flight, return
+      if (t == ISSUER) {
+        if (a.err) atomicExch(a.err, kErrWait);
+        const int issued = min(k1, max(k + G::PD, k0 - 1 + G::PD));
+        for (int L = waited + 1; L <= issued; L++) (void)mbar_wait(bar_of(L), parity(L));
+      }
+      return;
+    }
+  }
+}
+
+// minimum blocks per SM each storage type is compiled for (the register cap
+// follows): 3 for 8-byte storage (80 registers; shared memory holds 3 blocks);
+// none for 4-byte storage (the compiler's 62-64 registers give 4 blocks, and a
+// cap of 4 blocks measured 6% slower)
+// (32 x 16 tiles with 8-byte storage: shared memory holds one block per SM)
+template <typename R, int TY> struct GMinBlocks { static constexpr int v = TY == 8 ? 3 : 1; };
+template <int TY> struct GMinBlocks<float, TY> { static constexpr int v = 0; };
+
+template <typename R, int SYM, int TY>
+__global__ void __launch_bounds__(TX *TY, GMinBlocks<R, TY>::v)
+    k_grid_tma(const GridArgs<typename GNum<R>::S> a, int step) {
+  const GridMaps *M = reinterpret_cast<const GridMaps *>(a.tmaps);
+  grid_block_tma<R, SYM, TY>(a, M, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x, step);
+}
+
+template <typename R, int SYM, int TY>
+__global__ void __launch_bounds__(TX *TY, GMinBlocks<R, TY>::v)
+    k_grid_tma_batch(const GridArgs<typename GNum<R>::S> *__restrict__ args, const int *__restrict__ block_start,
+                     int n_members, int step) {
+  const int id = blockIdx.x;
+  int lo = 0, hi = n_members;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(block_start + mid) <= id) lo = mid;
+    else hi = mid;
+  }
+  const GridArgs<typename GNum<R>::S> &a = args[lo];
+  const GridMaps *M = reinterpret_cast<const GridMaps *>(a.tmaps);
+  const int local = id - __ldg(block_start + lo);
+  const int gxc = a.nx / (TX - 1) + 1, gyc = a.ny / (TY - 1) + 1;
+  grid_block_tma<R, SYM, TY, true>(a, M, local % gxc, (local / gxc) % gyc, local / (gxc * gyc), gxc, step);
+}
+
+template <typename R, int SYM, int TY>
+struct SetupT {
+  using St = typename GNum<R>::S;
+  static constexpr size_t smem = Geo<(int)sizeof(St), TY>::SMEM;
+  static cudaError_t ensure(int &sms, int &per_sm) {
+    static unsigned long long done = 0;
+    static int s_sms[64] = {0}, s_per[64] = {0};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const int d = dev & 63;
+    if (!(done & (1ull << d))) {
+      e = cudaFuncSetAttribute(k_grid_tma<R, SYM, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_grid_tma_batch<R, SYM, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+      if (e == cudaSuccess) e = cudaDeviceGetAttribute(&s_sms[d], cudaDevAttrMultiProcessorCount, dev);
+      if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s_per[d], k_grid_tma<R, SYM, TY>, TX * TY, smem);
+      if (e != cudaSuccess) return e;
+      s_per[d] = s_per[d] > 0 ? s_per[d] : 1;
+      done |= 1ull << d;
+    }
+    sms = s_sms[d];
+    per_sm = s_per[d];
+    return cudaSuccess;
+  }
+};
+
+template <typename R, int SYM, int TY>
+cudaError_t launch_t(const GridArgs<typename GNum<R>::S> &a, cudaStream_t st) {
+  using S = SetupT<R, SYM, TY>;
+  int sms = 0, per_sm = 0;
+  cudaError_t e = S::ensure(sms, per_sm);
+  if (e != cudaSuccess) return e;
+  GridArgs<typename GNum<R>::S> b = a;
+  const unsigned gx = (unsigned)(a.nx / (TX - 1) + 1), gy = (unsigned)(a.ny / (TY - 1) + 1);
+  if (b.kchunk <= 0) b.kchunk = grid_chunk_for(a.nz, (long long)gx * gy, sms, per_sm);
+  if (b.kchunk > KC_MAX) return cudaErrorInvalidValue;
+  const dim3 grid(gx, gy, (unsigned)((a.nz + b.kchunk - 1) / b.kchunk));
+  k_grid_tma<R, SYM, TY><<<grid, TX * TY, S::smem, st>>>(b, 0);
+  return cudaGetLastError();
+}
+
+template <typename R, int SYM, int TY>
+cudaError_t launch_batch_t(const GridBatchLaunch &b, int step, cudaStream_t st) {
+  using S = SetupT<R, SYM, TY>;
+  int sms = 0, per_sm = 0;
+  cudaError_t e = S::ensure(sms, per_sm);
+  if (e != cudaSuccess) return e;
+  if (b.total_blocks <= 0) return cudaSuccess;
+  k_grid_tma_batch<R, SYM, TY><<<b.total_blocks, TX * TY, S::smem, st>>>(
+      (const GridArgs<typename GNum<R>::S> *)b.args, b.block_start, b.n_members, step);
+  return cudaGetLastError();
+}
+
+template <typename T> inline bool is_one(T v) { return v == T(1); }
+template <> inline bool is_one<float2>(float2 v) { return v.x == 1.0f && v.y == 0.0f; }
+
+template <typename R, int TY>
+cudaError_t launch_sym(const GridArgs<typename GNum<R>::S> &a, int sym, cudaStream_t st) {
+  if (a.nx <= 0 || a.ny <= 0 || a.nz <= 0) return cudaSuccess;
+  if (!a.tmaps || a.n_rows > ROWS_MAX) return cudaErrorInvalidValue;
+  const bool cubic = is_one(a.g[0]) && is_one(a.g[1]) && is_one(a.g[2]);
+  switch ((sym & 3) | (cubic ? 4 : 0)) {
+    case 2: return launch_t<R, 2, TY>(a, st);
+    case 1: return launch_t<R, 1, TY>(a, st);
+    case 0: return launch_t<R, 0, TY>(a, st);
+    case 6: return launch_t<R, 6, TY>(a, st);
+    case 5: return launch_t<R, 5, TY>(a, st);
+    default: return launch_t<R, 4, TY>(a, st);
+  }
+}
+
+// b.sym: the members' most general symmetry class | 4 when every member is cubic
+template <typename R, int TY>
+cudaError_t launch_batch_sym(const GridBatchLaunch &b, int step, cudaStream_t st) {
+  switch (b.sym) {
+    case 2: return launch_batch_t<R, 2, TY>(b, step, st);
+    case 1: return launch_batch_t<R, 1, TY>(b, step, st);
+    case 0: return launch_batch_t<R, 0, TY>(b, step, st);
+    case 6: return launch_batch_t<R, 6, TY>(b, step, st);
+    case 5: return launch_batch_t<R, 5, TY>(b, step, st);
+    default: return launch_batch_t<R, 4, TY>(b, step, st);
+  }
+}
+
+}  // namespace
+}  // namespace pn

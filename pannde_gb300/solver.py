@@ -223,10 +223,14 @@ class Batch:
         N.check(self._lib.pn_batch_solve_noalloc(self._h, int(nsteps)))
 
     def plan_stats(self) -> dict:
-        """{"graph_launches", "graph_captures", "tuned_classes"} (pn_batch_plan_stats)"""
+        """{"graph_launches", "graph_captures", "tuned_classes", "tile_rows", "shape"}
+        (pn_batch_plan_stats; tile_rows and shape of the last chunk run)"""
         gl, gc, tc = c_int64(0), c_int64(0), ctypes.c_int32(0)
-        N.check(self._lib.pn_batch_plan_stats(self._h, ctypes.byref(gl), ctypes.byref(gc), ctypes.byref(tc)))
-        return {"graph_launches": gl.value, "graph_captures": gc.value, "tuned_classes": tc.value}
+        tr, sh = ctypes.c_int32(0), ctypes.c_int32(0)
+        N.check(self._lib.pn_batch_plan_stats(self._h, ctypes.byref(gl), ctypes.byref(gc), ctypes.byref(tc),
+                                              ctypes.byref(tr), ctypes.byref(sh)))
+        return {"graph_launches": gl.value, "graph_captures": gc.value, "tuned_classes": tc.value,
+                "tile_rows": tr.value, "shape": sh.value}
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

@@ -33,7 +33,7 @@ def test_library_exports_every_declared_symbol():
         assert hasattr(lib, n), f"{n} declared but not exported"
         assert n in N.SIGNATURES, f"{n} has no ctypes prototype"
     assert set(N.SIGNATURES) <= names
-    assert lib.pn_abi_version() == N.ABI_VERSION == 2
+    assert lib.pn_abi_version() == N.ABI_VERSION == 3
 
 
 def plan(mesh, material=None, table=None, dt=1e-9, precision=N.PN_PREC_F64):
