@@ -333,7 +333,11 @@ int pn_solver_get_info(pn_solver *s, pn_solver_info *info);
    S[6] receive the pointers.  Element type by precision (double, float, or
    float2 (hi, lo) for PN_PREC_DF64); order by form: the caller's node / cell
    numbering in the table form, the lattice numbering (x fastest) in the grid
-   form. */
+   form.  The FP64 grid form chooses per tile between FP64 and double-float
+   arithmetic from the values its last step stored; this call puts every tile
+   on the FP64 path for the next step, so values written through the pointers
+   after this call and before the next solve are taken exactly -- call it
+   again after writing between later steps. */
 int pn_solver_device_state(pn_solver *s, void **V, void **S);
 
 /* Energy audit of the current state, formed and summed in FP64 whatever the
@@ -453,6 +457,15 @@ int pn_partitioned_get_traces(pn_partitioned *p, double *out, int64_t max_record
 /* partitions, halo node copies, local cells summed over partitions */
 int pn_partitioned_info(pn_partitioned *p, int32_t *n_parts, int64_t *halo_nodes, int64_t *local_cells);
 int pn_partitioned_destroy(pn_partitioned *p);
+
+/* Blocks of the FP64 grid form's step kernel that took the FP64 path and the
+   double-float path since the solver was created (both 0 in other forms).
+   No counterpart in the reference: the FP64 form computes each tile in
+   double-float arithmetic (48-bit significand, |error| well inside the
+   1e-10 contract) unless the tile or a neighbour holds values outside
+   double-float's range or a source term this step does, and then in IEEE
+   double. */
+int pn_solver_path_counts(pn_solver *s, int64_t *fp64_blocks, int64_t *df64_blocks);
 
 /* ---- diagnostics -------------------------------------------------------------
    Issue rates of the arithmetic pipes the step kernels lean on, measured on

@@ -151,6 +151,7 @@ SIGNATURES = {
     "pn_partitioned_info": (c_int, [c_void_p, P_int32, POINTER(c_int64), POINTER(c_int64)]),
     "pn_partitioned_destroy": (c_int, [c_void_p]),
     "pn_measure_pipe_rates": (c_int, [P_double, c_int32]),
+    "pn_solver_path_counts": (c_int, [c_void_p, POINTER(c_int64), POINTER(c_int64)]),
 }
 
 

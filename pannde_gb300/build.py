@@ -6,6 +6,7 @@ Sources (``pannde_gb300/csrc``):
   rsg_grid.cu   fused voxel-grid step kernel  nvcc, sm_103a
   rsg_grid_tma.cu  grid step, tensor-copy staging (32 x 8 tiles)  nvcc, sm_103a
   rsg_grid_tma16.cu  the same with 32 x 16 tiles (FP32 storage)  nvcc, sm_103a
+  rsg_grid_tma_f64.cu  the FP64 form's step (double-float / FP64 path per block)  nvcc, sm_103a
   rsg_state.cu  state convert / permute       nvcc, sm_103a
   rsg_split.cu  grid form: fix-up of split lattice sites (cracks)  nvcc, sm_103a
   pn_noalloc.cu fixed scratch of the allocation-free batch solve   nvcc
@@ -62,6 +63,7 @@ def _jobs() -> list[tuple[list[str], Path]]:
         (common_cu + ["-c", str(CSRC / "rsg_grid.cu")], OUT / "rsg_grid.o"),
         (common_cu + ["-c", str(CSRC / "rsg_grid_tma.cu")], OUT / "rsg_grid_tma.o"),
         (common_cu + ["-c", str(CSRC / "rsg_grid_tma16.cu")], OUT / "rsg_grid_tma16.o"),
+        (common_cu + ["-c", str(CSRC / "rsg_grid_tma_f64.cu")], OUT / "rsg_grid_tma_f64.o"),
         (common_cu + ["-c", str(CSRC / "rsg_state.cu")], OUT / "rsg_state.o"),
         (common_cu + ["-c", str(CSRC / "rsg_split.cu")], OUT / "rsg_split.o"),
         (common_cu + ["-c", str(CSRC / "pn_noalloc.cu")], OUT / "pn_noalloc.o"),

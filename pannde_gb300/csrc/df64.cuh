@@ -18,6 +18,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cstdint>
+
 namespace pn {
 
 struct df64 {
@@ -133,5 +135,45 @@ __device__ __forceinline__ float madd(float a, float b, float c) { return a * b 
 __device__ __forceinline__ double madd(double a, double b, double c) { return a * b + c; }
 
 __device__ __forceinline__ bool operator==(df64 a, df64 b) { return a.hi == b.hi && a.lo == b.lo; }
+
+// ---- between IEEE double and double-float ---------------------------------
+// GB300 converts double <-> float on its FP64 unit, at the FP64 FMA rate; these
+// conversions run on the integer and FP32 pipes instead (loads) or keep to
+// two conversions and one FP64 add (stores).
+//
+// split_double: d = hi + lo exactly up to the first 47 significant bits (the
+// rest truncated: |d - (hi + lo)| < 2^-46 |d|).  hi keeps d's sign, exponent
+// and top 23 fraction bits: the double's exponent field, rebiased from 1023
+// to 127, is (e11 - 896) mod 256 = (e11 mod 256) ^ 0x80 whenever the result
+// is a normal float, so a funnel shift of the high and low words by 3 and a
+// flip of bit 30 give hi's bits.  lo holds the next 23 fraction bits m as
+// (P | m) - P with P = sign | hi's exponent - 23, exact by Sterbenz.
+// Exact (to those 47 bits) for 2^-102 <= |d| < 2^128 (biased exponents
+// 921..1150); d == +-0 and every value outside that range give 0 -- the
+// double-float path takes only values its range check admitted (see
+// in_df64_range), so this only keeps a stray value from becoming garbage.
+__device__ __forceinline__ df64 split_double(double d) {
+  const uint32_t hw = (uint32_t)__double2hiint(d), lw = (uint32_t)__double2loint(d);
+  const uint32_t f = __funnelshift_l(lw, hw, 3) ^ 0x40000000u;
+  const uint32_t hib = (f & 0x7fffffffu) | (hw & 0x80000000u);
+  const uint32_t pb = (hib & 0xff800000u) - (23u << 23);
+  const float lo = __fsub_rn(__uint_as_float(pb | ((lw >> 6) & 0x7fffffu)), __uint_as_float(pb));
+  const bool zero = (((hw >> 20) & 0x7ffu) - 921u) > (1150u - 921u);
+  return df64(zero ? 0.f : __uint_as_float(hib), zero ? 0.f : lo);
+}
+
+// join_double: hi + lo rounded once to the nearest double (both convert
+// exactly; the FP64 add rounds the exact sum)
+__device__ __forceinline__ double join_double(df64 v) { return __dadd_rn((double)v.hi, (double)v.lo); }
+
+// whether d is 0 or its biased exponent lies in [e_lo, e_hi]: the values the
+// double-float path of the FP64 form takes (bounds chosen by the host so that
+// every product with the step's coefficients stays within 2^+-100)
+__device__ __forceinline__ bool in_df64_range(double d, uint32_t e_lo, uint32_t e_hi) {
+  const uint32_t hw = (uint32_t)__double2hiint(d);
+  const uint32_t e = (hw >> 20) & 0x7ffu;
+  const bool zero = (hw & 0x7fffffffu) == 0u && __double2loint(d) == 0;
+  return zero || (e - e_lo) <= (e_hi - e_lo);
+}
 
 }  // namespace pn

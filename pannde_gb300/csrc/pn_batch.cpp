@@ -356,6 +356,9 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision, const Stage &stage, 
       shapes.emplace_back(rows, per);
     }
   }
+  // FP64 form: the per-block path choice when every member keeps its flags
+  bool range_flags = tma && precision == PN_PREC_F64;
+  for (pn_solver *s : b->members) range_flags = range_flags && s->d_rflags != nullptr;
   int32_t done = 0;
   while (done < nsteps) {
     const int32_t chunk = common_chunk(b, nsteps - done, may_alloc);
@@ -462,6 +465,7 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision, const Stage &stage, 
                 L.total_blocks = bs[n];
                 L.sym = sym;
                 L.tile_rows = shapes[c].first;
+                L.range_flags = range_flags ? 1 : 0;
                 pn::ck(tma ? pn::launch_grid_tma_batch(L, precision, k, b->stream)
                            : pn::launch_grid_batch(L, precision, k, b->stream),
                        "batch step");
@@ -477,6 +481,8 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision, const Stage &stage, 
                 }
               });
     pn::ck(cudaStreamSynchronize(b->stream), "batch chunk");
+    if (!range_flags)  // members stepped without their flags: FP64 path first when next alone
+      for (pn_solver *s : b->members) pn::grid_reset_range_flags(s);
     b->last_rows = shapes[staged_shape].first;
     b->last_shape = shapes[staged_shape].second;
     advance(b, chunk);

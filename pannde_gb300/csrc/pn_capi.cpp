@@ -539,10 +539,13 @@ int pn_solver_get_info(pn_solver *s, pn_solver_info *info) {
 }
 
 int pn_solver_device_state(pn_solver *s, void **V, void **S) {
-  if (!s || !V || !S) return set_err(PN_ERR_INVALID, "null argument");
-  for (int k = 0; k < 3; k++) V[k] = s->V[s->cur][k];
-  for (int k = 0; k < 6; k++) S[k] = s->S[s->cur][k];
-  return PN_OK;
+  return guarded([&]() -> int {
+    if (!s || !V || !S) return set_err(PN_ERR_INVALID, "null argument");
+    for (int k = 0; k < 3; k++) V[k] = s->V[s->cur][k];
+    for (int k = 0; k < 6; k++) S[k] = s->S[s->cur][k];
+    if (s->form == PN_FORM_GRID) pn::grid_reset_range_flags(s);  // the caller may write through them
+    return PN_OK;
+  });
 }
 
 int pn_solver_energy(pn_solver *s, double *kinetic, double *strain) {
@@ -551,6 +554,20 @@ int pn_solver_energy(pn_solver *s, double *kinetic, double *strain) {
     pn::ck(cudaStreamSynchronize(s->stream), "energy sync");
     if (const int rc = pn::device_check(s)) return rc;
     pn::energy(s, *kinetic, *strain);
+    return PN_OK;
+  });
+}
+
+int pn_solver_path_counts(pn_solver *s, int64_t *fp64_blocks, int64_t *df64_blocks) {
+  return guarded([&]() -> int {
+    if (!s || !fp64_blocks || !df64_blocks) return set_err(PN_ERR_INVALID, "null argument");
+    unsigned long long c[2] = {0ull, 0ull};
+    if (s->d_pathcnt) {
+      pn::ck(cudaMemcpyAsync(c, s->d_pathcnt, sizeof(c), cudaMemcpyDeviceToHost, s->stream), "path counts");
+      pn::ck(cudaStreamSynchronize(s->stream), "path counts");
+    }
+    *fp64_blocks = (int64_t)c[0];
+    *df64_blocks = (int64_t)c[1];
     return PN_OK;
   });
 }

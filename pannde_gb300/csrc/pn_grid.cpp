@@ -207,6 +207,21 @@ int64_t grid_footprint(const GridMap &g, const MaterialTables &mt, int precision
 
 namespace {
 
+// The FP64 form's double-float range as biased double exponents [e_lo, e_hi]:
+// every value the double-float path takes is 0 or lies in
+// [2^-100 / min(1, cmin), 2^100 / max(1, cmax)], so that its products with
+// the step's coefficients (nonzero magnitudes cmin..cmax) stay within
+// 2^-100..2^100, where a double-float keeps its 48-bit significand (the low
+// word stays a normal float) and nothing overflows.
+void range_bounds(double cmin, double cmax, int32_t &e_lo, int32_t &e_hi) {
+  const double lo = std::ldexp(1.0, -100) / std::min(1.0, cmin);
+  const double hi = std::ldexp(1.0, 100) / std::max(1.0, cmax);
+  const int elo = (int)std::ceil(std::log2(lo)) + 1023;       // 2^(e-1023) >= lo
+  const int ehi = (int)std::floor(std::log2(hi)) - 1 + 1023;  // 2^(e-1023+1) <= hi
+  e_lo = std::min(2046, std::max(1, elo));
+  e_hi = std::min(2046, std::max(0, ehi));
+}
+
 // tensor maps of both input parities for tiles of `rows` rows (false: a
 // buffer or pitch the copies cannot take, or rows the storage has no kernel for)
 bool encode_maps(pn_solver *s, int rows, unsigned char *out) {
@@ -329,8 +344,44 @@ void grid_create(pn_solver *s) {
       }
     }
   }
+  // the FP64 form: each block of a step takes the double-float path unless
+  // its tile's neighbourhood holds values outside that path's range
+  // (PN_F64_PATH=fp64 keeps every block on the FP64 path, for comparisons)
+  const char *path = std::getenv("PN_F64_PATH");
+  if (s->precision == PN_PREC_F64 && s->d_tmaps && !(path && std::strcmp(path, "fp64") == 0)) {
+    double cmin = 1.0, cmax = 1.0;
+    auto see = [&](double v) {
+      v = std::fabs(v);
+      if (v == 0.0) return;
+      cmin = std::min(cmin, v);
+      cmax = std::max(cmax, v);
+    };
+    for (int64_t q = 0; q < gn; q++) see(coef[q]);
+    for (double v : ct) see(v);
+    if (s->gfold == 1.0) {
+      see(0.25 / s->mesh.hx);
+      see(0.25 / s->mesh.hy);
+      see(0.25 / s->mesh.hz);
+    }
+    s->r_cmin = cmin;
+    s->r_cmax = cmax;
+    range_bounds(cmin, cmax, s->r_elo, s->r_ehi);
+    const int64_t tiles = (int64_t)(g.nx / (kGridTileX - 1) + 1) * (g.ny / (kGridTileRows - 1) + 1);
+    s->d_rflags = s->alloc<uint8_t>((size_t)(3 * tiles));
+    s->d_pathcnt = s->alloc<unsigned long long>(2 * sizeof(unsigned long long));
+    ck(cudaMemsetAsync(s->d_pathcnt, 0, 2 * sizeof(unsigned long long), s->stream), "memset");
+    grid_reset_range_flags(s);
+  }
   grid_split_upload(s);
   ck(cudaStreamSynchronize(s->stream), "create sync");
+}
+
+void grid_reset_range_flags(pn_solver *s) {
+  if (!s->d_rflags) return;
+  const GridMap &g = s->grid;
+  const int64_t tiles = (int64_t)(g.nx / (kGridTileX - 1) + 1) * (g.ny / (kGridTileRows - 1) + 1);
+  ck(cudaMemsetAsync(s->d_rflags, 0, (size_t)(3 * tiles), s->stream), "memset");
+  ck(cudaMemsetAsync(s->d_rflags + (s->step % 3) * tiles, 1, (size_t)tiles, s->stream), "memset");
 }
 
 void grid_split_upload(pn_solver *s) {
@@ -443,6 +494,7 @@ int grid_put_state(pn_solver *s, const double *const *V, const double *const *S)
   ck(cudaStreamSynchronize(s->stream), "set_state");
   if (bad[0] || bad[1]) return (bad[0] ? 1 : 0) | (bad[1] ? 2 : 0);
   s->cur = b;
+  grid_reset_range_flags(s);  // the new state's ranges are not known: FP64 for one step
   return 0;
 }
 
@@ -519,6 +571,20 @@ void grid_sources(pn_solver *s) {
   }
   upload(F, g.nz + 1, s->d_frng, s->d_fkey, s->d_fsig, s->d_fw);
   upload(M, g.nz, s->d_mrng, s->d_mkey, s->d_msig, s->d_mw);
+  if (s->d_rflags) {  // the double-float range also covers the source weights
+    double cmin = s->r_cmin, cmax = s->r_cmax;
+    for (const std::vector<Keyed> *L : {&F, &M})
+      for (const Keyed &k : *L) {
+        const double v = std::fabs(k.w);
+        if (v == 0.0) continue;
+        cmin = std::min(cmin, v);
+        cmax = std::max(cmax, v);
+      }
+    for (auto &f : s->split_forces) if (f.w != 0.0) { cmin = std::min(cmin, std::fabs(f.w)); cmax = std::max(cmax, std::fabs(f.w)); }
+    for (auto &m : s->fix_moments) if (m.w != 0.0) { cmin = std::min(cmin, std::fabs(m.w)); cmax = std::max(cmax, std::fabs(m.w)); }
+    range_bounds(cmin, cmax, s->r_elo, s->r_ehi);
+    grid_reset_range_flags(s);  // tiles judged under the old bounds: FP64 for one step
+  }
   grid_split_upload(s);
   ck(cudaStreamSynchronize(s->stream), "sources upload");
 }
@@ -614,6 +680,11 @@ void grid_args(pn_solver *s, GridArgs<T> &a) {
   const char *skip = std::getenv("PN_TEST_GRID_SKIP_COPY");
   a.test_skip_layer = skip && *skip ? std::atoi(skip) : kNoLayer;
   a.tile_rows = s->tile_rows;
+  a.rflags = s->d_rflags;
+  a.flag_phase = (int32_t)(s->step % 3);
+  a.r_elo = s->r_elo;
+  a.r_ehi = s->r_ehi;
+  a.path_count = s->d_pathcnt;
 }
 
 const void *grid_maps_for(const pn_solver *s, int in) {
@@ -648,6 +719,7 @@ void run(pn_solver *s, int32_t nsteps) {
         a.S_out[c] = (T *)s->S[out][c];
       }
       a.tmaps = grid_maps_for(s, in);
+      a.flag_phase = (int32_t)((s->step + k) % 3);
       a.sigval = nsig > 0 ? (const T *)s->d_sig + sig_row(s, k) * nsig : nullptr;
       a.rec = s->rec_count + k;  // sigval points at this step's row (stride 0)
       pn_solver::Mark m{};

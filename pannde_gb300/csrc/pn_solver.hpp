@@ -88,6 +88,13 @@ struct pn_solver {
   int32_t *d_ktop = nullptr; // [tiles] cell layers the tensor-copy kernel marches per tile
   mutable int64_t step_bytes_cached = 0;  // grid form: algorithmic bytes of one step (0: not yet)
   int tile_rows = pn::kGridTileRows;      // grid form: rows TY of the 32 x TY block tiles
+  // FP64 form with the tensor-copy kernel: per-tile path flags [3][tiles] and
+  // the double-float range (biased double exponents), from the coefficient
+  // magnitudes r_cmin..r_cmax; block counts of the two paths [fp64, df64]
+  uint8_t *d_rflags = nullptr;
+  int32_t r_elo = 1, r_ehi = 0;
+  double r_cmin = 1.0, r_cmax = 1.0;
+  unsigned long long *d_pathcnt = nullptr;
   std::vector<std::pair<int32_t, int32_t>> sensor_pairs;  // grid form: (node, sensor) sorted, for re-tiling
   // cubic lattice with the tensor-copy kernel: 0.25/h folded into dt/rho, dt*C
   // and the force weights (the kernel's g is then 1); 1.0 when not folded
@@ -319,6 +326,10 @@ void grid_run(pn_solver *s, int32_t nsteps);
 int grid_put_state(pn_solver *s, const double *const *V, const double *const *S);
 void grid_split_upload(pn_solver *s);  // the fix-up tables of split sites
 void grid_get_state(pn_solver *s, double *const *V, double *const *S);
+
+// FP64 form: every tile back on the FP64 path for the next step (state or
+// tiling changed; pn_grid.cpp)
+void grid_reset_range_flags(pn_solver *s);
 
 // algorithmic HBM bytes of one step in the solver's form
 int64_t step_bytes(const pn_solver *s);

@@ -83,6 +83,13 @@ struct GridArgs {
   const T *cm_w;
   int32_t test_skip_layer;  // failure-path test: the layer whose copies are never issued (kNoLayer: none)
   int32_t tile_rows;        // rows TY of the 32 x TY block tile (8, or 16 with the tensor-copy kernel)
+  // FP64 form with the tensor-copy kernel: per-tile path flags [3][tiles]
+  // (rsg_grid_tma.cuh fp64_path) and the double-float range as biased double
+  // exponents [r_elo, r_ehi]; rflags null: no path choice (the other forms)
+  uint8_t *rflags;
+  int32_t flag_phase;       // (step of this launch's step 0) % 3
+  int32_t r_elo, r_ehi;
+  unsigned long long *path_count;  // [2] blocks that took the FP64 / double-float path, or null
 };
 
 constexpr int32_t kNoLayer = INT32_MIN;  // no layer index (layers run from -1 to nz)
@@ -110,6 +117,7 @@ struct GridBatchLaunch {
   int total_blocks;
   int sym;                 // most general symmetry class among the members
   int tile_rows;           // TY of every member's tiles
+  int range_flags;         // FP64 form: every member has path flags (rflags)
 };
 cudaError_t launch_grid_batch(const GridBatchLaunch &b, int precision, int step, cudaStream_t st);
 cudaError_t launch_grid_f32(const GridArgs<float> &a, int sym, cudaStream_t st);

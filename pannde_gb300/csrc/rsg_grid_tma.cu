@@ -1,6 +1,7 @@
 // rsg_grid_tma.cu -- the tensor-copy grid step (rsg_grid_tma.cuh) with 32 x 8
 // tiles for every storage type, the tensor-map encoding, and the launch
-// dispatch by tile rows (32 x 16 FP32 tiles come from rsg_grid_tma16.cu).
+// dispatch (32 x 16 FP32 tiles come from rsg_grid_tma16.cu, the FP64 form's
+// per-block path kernels from rsg_grid_tma_f64.cu).
 #include "rsg_grid_tma.cuh"
 
 namespace pn {
@@ -9,6 +10,9 @@ namespace pn {
 cudaError_t launch_grid_tma_f32_rows16(const GridArgs<float> &a, int sym, cudaStream_t st);
 cudaError_t launch_grid_tma_batch_f32_rows16(const GridBatchLaunch &b, int step, cudaStream_t st);
 int grid_tma_blocks_per_sm_f32_rows16();
+// rsg_grid_tma_f64.cu
+cudaError_t launch_grid_tma_f64h(const GridArgs<double> &a, int sym, cudaStream_t st);
+cudaError_t launch_grid_tma_batch_f64h(const GridBatchLaunch &b, int step, cudaStream_t st);
 
 namespace {
 
@@ -116,6 +120,7 @@ cudaError_t launch_grid_tma(const void *args, int precision, int sym, cudaStream
   }
   const GridArgs<double> &a = *(const GridArgs<double> *)args;
   if (a.tile_rows != 8) return cudaErrorInvalidValue;
+  if (a.rflags) return launch_grid_tma_f64h(a, sym, st);  // the FP64 form: per-block double-float / FP64 path
   return launch_sym<double, 8>(a, sym, st);
 }
 
@@ -124,6 +129,7 @@ cudaError_t launch_grid_tma_batch(const GridBatchLaunch &b, int precision, int s
   if (precision == 2)
     return b.tile_rows == 16 ? launch_grid_tma_batch_f32_rows16(b, step, st) : launch_batch_sym<float, 8>(b, step, st);
   if (precision == 3) return launch_batch_sym<df64, 8>(b, step, st);
+  if (b.range_flags) return launch_grid_tma_batch_f64h(b, step, st);
   return launch_batch_sym<double, 8>(b, step, st);
 }
 

@@ -97,33 +97,67 @@ struct Geo {
   static_assert(SBOX % ESZ == 0 && VBOX % ESZ == 0, "element size");
 };
 
-template <typename R> struct GNum;
+// Kinds of step: K picks the arithmetic type R, the storage type S of global
+// memory and of the tensor copies, and the type T of the shared tiles the
+// block itself writes or converts (computed velocities, stiffness rows, and
+// for df64d the stress slots):
+//   float / double / df64   R, S and T alike (df64 stored as float2)
+//   df64d                   the FP64 form's double-float path: S double, R
+//                           df64, T float2 -- loads split doubles exactly
+//                           (split_double), stores join them (join_double),
+//                           stress tiles are split in place once per layer
+struct df64d {};
+template <typename K> struct GNum;
 template <> struct GNum<float> {
   using S = float;
+  using T = float;
+  using R = float;
+  static constexpr bool SPLIT = false;
   static __device__ __forceinline__ float ld(const float *p, int64_t i) { return __ldg(p + i); }
   static __device__ __forceinline__ float val(float v) { return v; }
-  static __device__ __forceinline__ float sto(float v) { return v; }
+  static __device__ __forceinline__ float tval(float v) { return v; }
+  static __device__ __forceinline__ float tsto(float v) { return v; }
   static __device__ __forceinline__ void st(float *p, int64_t i, float v) { p[i] = v; }
   static __device__ __forceinline__ double dbl(float v) { return (double)v; }
 };
 template <> struct GNum<double> {
   using S = double;
+  using T = double;
+  using R = double;
+  static constexpr bool SPLIT = false;
   static __device__ __forceinline__ double ld(const double *p, int64_t i) { return __ldg(p + i); }
   static __device__ __forceinline__ double val(double v) { return v; }
-  static __device__ __forceinline__ double sto(double v) { return v; }
+  static __device__ __forceinline__ double tval(double v) { return v; }
+  static __device__ __forceinline__ double tsto(double v) { return v; }
   static __device__ __forceinline__ void st(double *p, int64_t i, double v) { p[i] = v; }
   static __device__ __forceinline__ double dbl(double v) { return v; }
 };
 template <> struct GNum<df64> {
   using S = float2;
+  using T = float2;
+  using R = df64;
+  static constexpr bool SPLIT = false;
   static __device__ __forceinline__ df64 ld(const float2 *p, int64_t i) {
     const float2 v = __ldg(p + i);
     return df64(v.x, v.y);
   }
   static __device__ __forceinline__ df64 val(float2 v) { return df64(v.x, v.y); }
-  static __device__ __forceinline__ float2 sto(df64 v) { return make_float2(v.hi, v.lo); }
+  static __device__ __forceinline__ df64 tval(float2 v) { return df64(v.x, v.y); }
+  static __device__ __forceinline__ float2 tsto(df64 v) { return make_float2(v.hi, v.lo); }
   static __device__ __forceinline__ void st(float2 *p, int64_t i, df64 v) { p[i] = make_float2(v.hi, v.lo); }
   static __device__ __forceinline__ double dbl(df64 v) { return (double)v.hi + (double)v.lo; }
+};
+template <> struct GNum<df64d> {
+  using S = double;
+  using T = float2;
+  using R = df64;
+  static constexpr bool SPLIT = true;
+  static __device__ __forceinline__ df64 ld(const double *p, int64_t i) { return split_double(__ldg(p + i)); }
+  static __device__ __forceinline__ df64 val(double v) { return split_double(v); }
+  static __device__ __forceinline__ df64 tval(float2 v) { return df64(v.x, v.y); }
+  static __device__ __forceinline__ float2 tsto(df64 v) { return make_float2(v.hi, v.lo); }
+  static __device__ __forceinline__ void st(double *p, int64_t i, df64 v) { p[i] = join_double(v); }
+  static __device__ __forceinline__ double dbl(df64 v) { return join_double(v); }
 };
 
 __host__ __device__ constexpr bool c_used(int sym, int k, int j) {
@@ -199,11 +233,17 @@ __device__ __forceinline__ int floor_to(int v, int m) {  // largest multiple of 
 // error word codes
 constexpr int32_t kErrWait = 1;
 
-template <typename R, int SYM, int TY, bool BATCH = false>
-__device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::S> &a, const GridMaps *M,
+// RANGE (the FP64 form's kernel): every V and S value the block stores is
+// tested against the double-float range, and a block that stored one outside
+// it marks its tile for the FP64 path in the next step (range_flags_write).
+template <typename K, int SYM, int TY, bool BATCH = false, bool RANGE = false>
+__device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::S> &a, const GridMaps *M,
                                                int bx, int by, int bz, int gxc, int step) {
-  using N = GNum<R>;
+  using N = GNum<K>;
+  using R = typename N::R;
   using St = typename N::S;
+  using Sm = typename N::T;
+  static_assert(sizeof(Sm) == sizeof(St), "shared tiles hold one storage element per value");
   using G = Geo<(int)sizeof(St), TY>;
   constexpr int NT = G::NT;
   // SYM: material symmetry class (bits 0-1, see c_used) | 4 when the lattice is
@@ -220,8 +260,8 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
   // the generic pointer.
   unsigned char *base = BATCH ? (unsigned char *)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127)
                               : smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
-  St *sVt = reinterpret_cast<St *>(base + G::OFF_VT);
-  St *sC = reinterpret_cast<St *>(base + G::OFF_C);
+  Sm *sVt = reinterpret_cast<Sm *>(base + G::OFF_VT);
+  Sm *sC = reinterpret_cast<Sm *>(base + G::OFF_C);
   int2 *sRf = reinterpret_cast<int2 *>(base + G::OFF_R);
   int2 *sRs = sRf + (KC_MAX + 2);
   int2 *sRm = sRs + (KC_MAX + 2);
@@ -286,7 +326,7 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
     mbar_init_fence();
   }
   // per-chunk tables: stiffness rows, source and sensor ranges
-  for (int q = t; q < a.n_rows * 36; q += NT) sC[q] = a.ctab[q];
+  for (int q = t; q < a.n_rows * 36; q += NT) sC[q] = N::tsto(N::val(a.ctab[q]));
   const int nL = k1 - k0 + 2;  // node layers k0-1 .. k1
   for (int q = t; q < nL; q += NT) {
     const int k = k0 - 1 + q;
@@ -304,6 +344,21 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
     for (int d = 0; d <= G::PD; d++)
       if (k0 - 1 + d <= k1) issue(k0 - 1 + d);
   }
+  // split the stress slot of layer L in place (df64d): each stored double
+  // becomes its double-float pair, so the velocity half reads pairs; the
+  // slot is waited for first (false: the wait gave up)
+  constexpr int BOXE = G::BWC * (TY + 1);  // elements of one field's stress box
+  auto split_slot = [&](int L) {
+    if (!mbar_wait(bar_of(L), parity(L))) return false;
+    double *sl = reinterpret_cast<double *>(sslot(L));
+    for (int q = t; q < 6 * BOXE; q += NT) {
+      const int f = q / BOXE;
+      double *pd = sl + f * SB + (q - f * BOXE);
+      const df64 v = split_double(*pd);
+      *reinterpret_cast<float2 *>(pd) = make_float2(v.hi, v.lo);
+    }
+    return true;
+  };
 
   // per cell layer: A = (x, y differences) + z sum, B = the same - z sum; a
   // node's acceleration is A of the layer above + B of the layer below
@@ -315,6 +370,28 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
   const int rv = ty * G::BWN + on + tx;  // node (i, j) in the node tile
   int waited = k0 - 2;                   // last layer this thread has waited for
   bool fail = false;
+  bool oor = false;  // RANGE: a stored value outside the double-float range
+  auto store = [&](St *p, int64_t i, R v) {
+    if constexpr (RANGE) {
+      const double d = N::dbl(v);
+      oor = oor || !in_df64_range(d, (uint32_t)a.r_elo, (uint32_t)a.r_ehi);
+      p[i] = (St)d;
+    } else {
+      N::st(p, i, v);
+    }
+  };
+
+  if constexpr (N::SPLIT) {
+    bool ok = split_slot(k0 - 1);
+    if (ok) waited = k0 - 1;
+    if (__syncthreads_or(!ok)) {
+      if (t == ISSUER) {
+        if (a.err) atomicExch(a.err, kErrWait);
+        for (int L = k0; L <= min(k1, k0 - 1 + G::PD); L++) (void)mbar_wait(bar_of(L), parity(L));
+      }
+      return;
+    }
+  }
 
   // FP32 storage: two layers per unrolled body, so the values carried from
   // one layer to the next alternate registers instead of moving
@@ -328,8 +405,8 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
     if (k <= k1) {
       if (BATCH ? mbar_wait_call(bar_of(k), parity(k)) : mbar_wait(bar_of(k), parity(k))) waited = k;
       else fail = true;
-      const St *Sk = reinterpret_cast<const St *>(sslot(k));
-      auto cellv = [&](int f, int q) { return N::val(Sk[f * SB + q]); };
+      const Sm *Sk = reinterpret_cast<const Sm *>(sslot(k));
+      auto cellv = [&](int f, int q) { return N::tval(Sk[f * SB + q]); };
       const int ib = ra + 1, id = ra + G::BWC, ic = id + 1;
       R A, B, C, D;
       A = cellv(0, ra); B = cellv(0, ib); C = cellv(0, ic); D = cellv(0, id);
@@ -394,13 +471,13 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
         vn[0] = madd(cf, ax, vn[0]);
         vn[1] = madd(cf, ay, vn[1]);
         vn[2] = madd(cf, az, vn[2]);
-        St *Vt = sVt + (k & 1) * 3 * NT;
+        Sm *Vt = sVt + (k & 1) * 3 * NT;
 #pragma unroll
-        for (int c = 0; c < 3; c++) Vt[c * NT + t] = N::sto(vn[c]);
+        for (int c = 0; c < 3; c++) Vt[c * NT + t] = N::tsto(vn[c]);
         if (node_own && (k < k1 || last_chunk)) {
           const int64_t n = (int64_t)k * nplane + nidx0;
 #pragma unroll
-          for (int c = 0; c < 3; c++) N::st(a.V_out[c], n, vn[c]);
+          for (int c = 0; c < 3; c++) store(a.V_out[c], n, vn[c]);
           const int2 sr = sRs[k - k0 + 1];
           if (rec < a.rec_cap) {
             for (int e = sr.x; e < sr.y; e++) {  // sensor traces
@@ -420,13 +497,13 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
 
     // ---- C: partial sums of node layer k-1, stress of cell layer k-2
     if (k - 1 >= k0 && k - 1 <= k1 && tx < TX - 1 && ty < TY - 1) {
-      const St *Vt = sVt + ((k - 1) & 1) * 3 * NT;
+      const Sm *Vt = sVt + ((k - 1) & 1) * 3 * NT;
       const int ia = t, ib = t + 1, ic = t + TX + 1, id = t + TX;
       R px[3], py[3], s[3];
 #pragma unroll
       for (int c = 0; c < 3; c++) {
-        const R A = N::val(Vt[c * NT + ia]), B = N::val(Vt[c * NT + ib]);
-        const R C = N::val(Vt[c * NT + ic]), D = N::val(Vt[c * NT + id]);
+        const R A = N::tval(Vt[c * NT + ia]), B = N::tval(Vt[c * NT + ib]);
+        const R C = N::tval(Vt[c * NT + ic]), D = N::tval(Vt[c * NT + id]);
         px[c] = diff22(B, C, A, D);
         diffsum22(A, B, C, D, py[c], s[c]);
       }
@@ -453,13 +530,13 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
         }
         const int64_t cg = (int64_t)kc * cplane + cidx0;
         const int row = mslot(kc)[ty * G::BWM + om + tx];
-        const St *Cm = sC + 36 * row;
+        const Sm *Cm = sC + 36 * row;
         R acc[6];  // the cell's stress before the update
         if constexpr (G::OWN_SMEM) {
-          const St *Sc = reinterpret_cast<const St *>(sslot(kc));
+          const Sm *Sc = reinterpret_cast<const Sm *>(sslot(kc));
           const int own = ra + G::BWC + 1;  // cell (i, j)
 #pragma unroll
-          for (int f = 0; f < 6; f++) acc[f] = N::val(Sc[f * SB + own]);
+          for (int f = 0; f < 6; f++) acc[f] = N::tval(Sc[f * SB + own]);
         } else {  // in L2: its tile was copied two layers ago
 #pragma unroll
           for (int f = 0; f < 6; f++) acc[f] = N::ld(a.S_in[f], cg);
@@ -486,16 +563,16 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
           for (int kk = 0; kk < 6; kk++) {
 #pragma unroll
             for (int jj = 0; jj < 6; jj++)
-              if (c_used(2, kk, jj)) acc[kk] = madd(N::val(Cm[6 * kk + jj]), e[jj], acc[kk]);
-            N::st(a.S_out[kk], cg, acc[kk]);
+              if (c_used(2, kk, jj)) acc[kk] = madd(N::tval(Cm[6 * kk + jj]), e[jj], acc[kk]);
+            store(a.S_out[kk], cg, acc[kk]);
           }
         } else {
 #pragma unroll
           for (int kk = 0; kk < 6; kk++) {
 #pragma unroll
             for (int jj = 0; jj < 6; jj++)
-              if (c_used(SYM & 3, kk, jj)) acc[kk] = madd(N::val(Cm[6 * kk + jj]), e[jj], acc[kk]);
-            N::st(a.S_out[kk], cg, acc[kk]);
+              if (c_used(SYM & 3, kk, jj)) acc[kk] = madd(N::tval(Cm[6 * kk + jj]), e[jj], acc[kk]);
+            store(a.S_out[kk], cg, acc[kk]);
           }
         }
       }
@@ -504,6 +581,14 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
         spx[c] = px[c];
         spy[c] = py[c];
         ss[c] = s[c];
+      }
+    }
+    if constexpr (N::SPLIT) {
+      // layer k+1 (copied since the start of this iteration; its slot's
+      // previous layer k-1 is no longer read) becomes pairs for the next one
+      if (k + 1 <= k1) {
+        if (split_slot(k + 1)) waited = max(waited, k + 1);
+        else fail = true;
       }
     }
     if (__syncthreads_or(fail)) {
@@ -516,6 +601,87 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<R>::
       return;
     }
   }
+  if constexpr (RANGE) {  // a value left the double-float range: the tile's next step runs FP64
+    if (__syncthreads_or(oor) && t == 0) {
+      const int nt = gxc * (a.ny / (TY - 1) + 1);
+      a.rflags[((a.flag_phase + step + 1) % 3) * nt + blk] = 1;
+    }
+  }
+}
+
+// The FP64 form's path for this block: the FP64 path (the tensor-copy kernel
+// in IEEE double) when its tile or one of the eight around it stored a value
+// outside the double-float range in the previous step, or when one of this
+// step's source terms of its layers lies outside it; the double-float path
+// (df64d) otherwise.  Flags rotate through three per-tile buffers: read
+// (flag_phase + step) % 3, written by this step's blocks (+1), cleared for
+// the step after next by each tile's first chunk (+2).  Block-uniform.
+template <int TY>
+__device__ __forceinline__ bool fp64_path(const GridArgs<double> &a, int bx, int by, int bz, int gxc, int step) {
+  constexpr int NT = TX * TY;
+  const int t = threadIdx.x;
+  const int gyc = a.ny / (TY - 1) + 1, nt = gxc * gyc;
+  const int blk = by * gxc + bx;
+  const int phase = (a.flag_phase + step) % 3;
+  if (bz == 0 && t == 0) a.rflags[((phase + 2) % 3) * nt + blk] = 0;
+  bool f = false;
+  if (t < 9) {
+    const int x = bx + t % 3 - 1, y = by + t / 3 - 1;
+    if (x >= 0 && x < gxc && y >= 0 && y < gyc) f = a.rflags[phase * nt + y * gxc + x] != 0;
+  }
+  const int nz = a.nz;
+  const int ktop = a.ktop ? min(nz, __ldg(a.ktop + blk)) : nz;
+  const int k0 = bz * a.kchunk, k1 = min(ktop, k0 + a.kchunk);
+  if (k0 < ktop && a.sigval) {
+    const double *sigrow = a.sigval + (int64_t)min(step, a.sig_rows - 1) * a.sig_stride;
+    const uint32_t lo = (uint32_t)a.r_elo, hi = (uint32_t)a.r_ehi;
+    auto bad = [&](double w, double sg) { return !in_df64_range(sg, lo, hi) || !in_df64_range(w * sg, lo, hi); };
+    if (a.f_rng) {  // force entries of node layers k0-1 .. k1 (contiguous per block)
+      const int64_t r0 = (int64_t)blk * (nz + 1);
+      const int e0 = a.f_rng[r0 + max(k0 - 1, 0)].x, e1 = a.f_rng[r0 + k1].y;
+      for (int e = e0 + t; e < e1; e += NT) f = f || bad(a.f_w[e], sigrow[a.f_sig[e]]);
+    }
+    if (a.m_rng) {  // moment entries of cell layers k0 .. k1-1
+      const int64_t r0 = (int64_t)blk * nz;
+      const int e0 = a.m_rng[r0 + k0].x, e1 = a.m_rng[r0 + k1 - 1].y;
+      for (int e = e0 + t; e < e1; e += NT) f = f || bad(a.m_w[e], sigrow[a.m_sig[e]]);
+    }
+  }
+  const bool fp64 = __syncthreads_or(f) != 0;
+  if (t == 0 && a.path_count) atomicAdd(a.path_count + (fp64 ? 0 : 1), 1ull);
+  return fp64;
+}
+
+template <int SYM>
+__global__ void __launch_bounds__(TX * 8, 3) k_grid_tma_f64h(const GridArgs<double> a, int step) {
+  const GridMaps *M = reinterpret_cast<const GridMaps *>(a.tmaps);
+  const int bx = blockIdx.x, by = blockIdx.y, bz = blockIdx.z, gxc = gridDim.x;
+  if (fp64_path<8>(a, bx, by, bz, gxc, step))
+    grid_block_tma<double, SYM, 8, false, true>(a, M, bx, by, bz, gxc, step);
+  else
+    grid_block_tma<df64d, SYM, 8, false, true>(a, M, bx, by, bz, gxc, step);
+}
+
+template <int SYM>
+__global__ void __launch_bounds__(TX * 8, 3)
+    k_grid_tma_f64h_batch(const GridArgs<double> *__restrict__ args, const int *__restrict__ block_start,
+                          int n_members, int step) {
+  const int id = blockIdx.x;
+  int lo = 0, hi = n_members;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(block_start + mid) <= id) lo = mid;
+    else hi = mid;
+  }
+  const GridArgs<double> &a = args[lo];
+  const GridMaps *M = reinterpret_cast<const GridMaps *>(a.tmaps);
+  const int local = id - __ldg(block_start + lo);
+  const int gxc = a.nx / (TX - 1) + 1, gyc = a.ny / 7 + 1;
+  const int bx = local % gxc, by = (local / gxc) % gyc, bz = local / (gxc * gyc);
+  if (fp64_path<8>(a, bx, by, bz, gxc, step))
+    grid_block_tma<double, SYM, 8, true, true>(a, M, bx, by, bz, gxc, step);
+  else
+    grid_block_tma<df64d, SYM, 8, true, true>(a, M, bx, by, bz, gxc, step);
 }
 
 // minimum blocks per SM each storage type is compiled for (the register cap
@@ -607,6 +773,53 @@ cudaError_t launch_batch_t(const GridBatchLaunch &b, int step, cudaStream_t st) 
   return cudaGetLastError();
 }
 
+// the FP64 form's kernels (k_grid_tma_f64h*): the FP64 path's shared-memory geometry
+template <int SYM>
+struct SetupH {
+  static constexpr size_t smem = Geo<8, 8>::SMEM;
+  static cudaError_t ensure() {
+    static unsigned long long done = 0;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const int d = dev & 63;
+    if (!(done & (1ull << d))) {
+      e = cudaFuncSetAttribute(k_grid_tma_f64h<SYM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_grid_tma_f64h_batch<SYM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+      if (e != cudaSuccess) return e;
+      done |= 1ull << d;
+    }
+    return cudaSuccess;
+  }
+};
+
+template <int SYM>
+cudaError_t launch_h(const GridArgs<double> &a, cudaStream_t st) {
+  int sms = 0, per_sm = 0;
+  cudaError_t e = SetupT<double, SYM, 8>::ensure(sms, per_sm);
+  if (e == cudaSuccess) e = SetupH<SYM>::ensure();
+  if (e != cudaSuccess) return e;
+  GridArgs<double> b = a;
+  const unsigned gx = (unsigned)(a.nx / (TX - 1) + 1), gy = (unsigned)(a.ny / 7 + 1);
+  if (b.kchunk <= 0) b.kchunk = grid_chunk_for(a.nz, (long long)gx * gy, sms, per_sm);
+  if (b.kchunk > KC_MAX) return cudaErrorInvalidValue;
+  const dim3 grid(gx, gy, (unsigned)((a.nz + b.kchunk - 1) / b.kchunk));
+  k_grid_tma_f64h<SYM><<<grid, TX * 8, SetupH<SYM>::smem, st>>>(b, 0);
+  return cudaGetLastError();
+}
+
+template <int SYM>
+cudaError_t launch_batch_h(const GridBatchLaunch &b, int step, cudaStream_t st) {
+  cudaError_t e = SetupH<SYM>::ensure();
+  if (e != cudaSuccess) return e;
+  if (b.total_blocks <= 0) return cudaSuccess;
+  k_grid_tma_f64h_batch<SYM><<<b.total_blocks, TX * 8, SetupH<SYM>::smem, st>>>(
+      (const GridArgs<double> *)b.args, b.block_start, b.n_members, step);
+  return cudaGetLastError();
+}
+
 template <typename T> inline bool is_one(T v) { return v == T(1); }
 template <> inline bool is_one<float2>(float2 v) { return v.x == 1.0f && v.y == 0.0f; }
 
@@ -622,6 +835,31 @@ cudaError_t launch_sym(const GridArgs<typename GNum<R>::S> &a, int sym, cudaStre
     case 6: return launch_t<R, 6, TY>(a, st);
     case 5: return launch_t<R, 5, TY>(a, st);
     default: return launch_t<R, 4, TY>(a, st);
+  }
+}
+
+inline cudaError_t launch_sym_h(const GridArgs<double> &a, int sym, cudaStream_t st) {
+  if (a.nx <= 0 || a.ny <= 0 || a.nz <= 0) return cudaSuccess;
+  if (!a.tmaps || a.n_rows > ROWS_MAX || !a.rflags) return cudaErrorInvalidValue;
+  const bool cubic = is_one(a.g[0]) && is_one(a.g[1]) && is_one(a.g[2]);
+  switch ((sym & 3) | (cubic ? 4 : 0)) {
+    case 2: return launch_h<2>(a, st);
+    case 1: return launch_h<1>(a, st);
+    case 0: return launch_h<0>(a, st);
+    case 6: return launch_h<6>(a, st);
+    case 5: return launch_h<5>(a, st);
+    default: return launch_h<4>(a, st);
+  }
+}
+
+inline cudaError_t launch_batch_sym_h(const GridBatchLaunch &b, int step, cudaStream_t st) {
+  switch (b.sym) {
+    case 2: return launch_batch_h<2>(b, step, st);
+    case 1: return launch_batch_h<1>(b, step, st);
+    case 0: return launch_batch_h<0>(b, step, st);
+    case 6: return launch_batch_h<6>(b, step, st);
+    case 5: return launch_batch_h<5>(b, step, st);
+    default: return launch_batch_h<4>(b, step, st);
   }
 }
 

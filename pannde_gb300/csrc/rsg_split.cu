@@ -44,6 +44,17 @@ template <> struct SN<float2> {
 
 constexpr int TPB = 128;
 
+// FP64 form (a.rflags set): a stored value outside the double-float range
+// puts the tile of lattice column (i, j) on the FP64 path for the next step
+// (the tensor-copy kernel's flags, rsg_grid_tma.cuh fp64_path)
+template <typename S>
+__device__ __forceinline__ void flag_range(const GridArgs<S> &a, double v, int64_t i, int64_t j, int step) {
+  if (!a.rflags || in_df64_range(v, (uint32_t)a.r_elo, (uint32_t)a.r_ehi)) return;
+  const int gxc = a.nx / (kGridTileX - 1) + 1, gyc = a.ny / (a.tile_rows - 1) + 1;
+  const int64_t blk = (j / (a.tile_rows - 1)) * gxc + i / (kGridTileX - 1);
+  a.rflags[((a.flag_phase + step + 1) % 3) * (int64_t)gxc * gyc + blk] = 1;
+}
+
 template <typename S>
 __device__ __forceinline__ const S *signal_row(const GridArgs<S> &a, int step) {
   return a.sigval ? a.sigval + (int64_t)min(step, a.sig_rows - 1) * a.sig_stride : nullptr;
@@ -89,6 +100,7 @@ __device__ void copy_velocity(const GridArgs<S> &a, int q, int step) {
     vn[c] = N::val(a.V_in[c][cp.v]);
     if (!(cf == R())) vn[c] = madd(cf, acc[c], vn[c]);
     a.V_out[c][cp.v] = N::sto(vn[c]);
+    flag_range(a, N::dbl(vn[c]), cp.i, cp.j, step);
   }
   const int64_t rec = a.rec + step;
   if (rec < a.rec_cap)
@@ -147,6 +159,7 @@ __device__ void fix_stress(const GridArgs<S> &a, int q, int step) {
 #pragma unroll
     for (int j = 0; j < 6; j++) acc[k] = madd(N::val(Cm[6 * k + j]), e[j], acc[k]);
     a.S_out[k][fc.cell] = N::sto(acc[k]);
+    flag_range(a, N::dbl(acc[k]), fc.cell % a.pcx, (fc.cell / a.pcx) % a.ny, step);
   }
 }
 

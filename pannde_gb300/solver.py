@@ -187,6 +187,13 @@ class Solver:
     def synchronize(self):
         N.check(self._lib.pn_solver_synchronize(self._h))
 
+    def path_counts(self) -> tuple[int, int]:
+        """(FP64-path blocks, double-float-path blocks) of the FP64 grid
+        form's steps so far (pn_solver_path_counts)."""
+        a, b = c_int64(0), c_int64(0)
+        N.check(self._lib.pn_solver_path_counts(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
 
 class Batch:
     """Solvers advanced together by shared launches (pn_batch_*).
