@@ -219,6 +219,7 @@ def time_device(case, prec, steps, warmup, torch, dist, energy=False):
         dist.barrier()
     torch.cuda.synchronize()
     s.enable_kernel_timing(True)
+    p0 = s.path_counts()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -228,6 +229,8 @@ def time_device(case, prec, steps, warmup, torch, dist, energy=False):
     ms = reduce_max(e0.elapsed_time(e1), dist, torch)
     kt = s.kernel_times()
     info = s.info()
+    p1 = s.path_counts()
+    info["path_counts"] = (p1[0] - p0[0], p1[1] - p0[1])
     if energy:  # FP64 energy audit of the final state
         info["energy"] = s.energy()
     s.close()
@@ -261,6 +264,11 @@ def roofline(case, info, kt, prec, peak, peak_kind):
            "traffic": traffic, "algorithmic_bytes": alg[dom],
            "avg_ms": {k: round(v, 4) for k, v in avg.items()},
            "step_bytes_frac": round(sum(alg.values()) / (step_ms * 1e-3) / 1e9 / peak, 4)}
+    if prec == "f64" and sum(info.get("path_counts", (0, 0))) > 0:
+        fp64, df = info["path_counts"]
+        out["f64_paths"] = {"fp64_blocks": fp64, "double_float_blocks": df,
+                            "double_float_share": round(df / (fp64 + df), 4),
+                            "note": "blocks of the timed steps by arithmetic path (pn_solver_path_counts)"}
     if prec == "f64":
         # the FP64 form is bound by GB300's FP64 pipe, not by HBM: its operation
         # count per cell-step and the pipe's busy fraction come from ncu
@@ -309,6 +317,51 @@ def e2e_run(case, prec, steps, torch, dist=None):
     d2h = (3 * nn + 6 * nc) * 8 + tr.size * 8
     s.close()
     return reduce_max(t1 - t0, dist, torch), h2d, d2h
+
+
+def state_transfer_leg(case, prec, torch, reps=3):
+    """pn_solver_set_state / pn_solver_get_state of the whole state between
+    page-locked host buffers and the device, two ways: the conversion kernels
+    reading and writing the mapped host buffers directly over the CPU-GPU
+    link, and (PN_STATE_COPY=dma) a copy-engine transfer to a device staging
+    buffer with the conversion kernel on device memory.  Best of `reps`,
+    wall clock around each call (each waits for its transfers)."""
+    from pannde_gb300.solver import Solver
+    nn, nc = case.mesh.n_nodes, case.mesh.n_cells
+    nbytes = (3 * nn + 6 * nc) * 8
+
+    def pinned(n):
+        return torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+
+    V = [pinned(nn) for _ in range(3)]
+    S = [pinned(nc) for _ in range(6)]
+    rng = np.random.default_rng(1)
+    for a in V + S:
+        a[:] = rng.uniform(-1.0, 1.0, a.size)
+    out = {}
+    with Solver.from_case(case, precision=prec, capacity=1, form=FORM) as s:
+        for mode in ("kernel", "dma"):
+            if mode == "dma":
+                os.environ["PN_STATE_COPY"] = "dma"
+            try:
+                put, get = [], []
+                for _ in range(reps):
+                    t0 = time.perf_counter()
+                    s.set_state(V, S)
+                    t1 = time.perf_counter()
+                    s.get_state_into(V, S)
+                    t2 = time.perf_counter()
+                    put.append(t1 - t0)
+                    get.append(t2 - t1)
+            finally:
+                os.environ.pop("PN_STATE_COPY", None)
+            out[mode] = {"set_state_GBps": round(nbytes / min(put) / 1e9, 1),
+                         "get_state_GBps": round(nbytes / min(get) / 1e9, 1),
+                         "set_state_ms": round(min(put) * 1e3, 3), "get_state_ms": round(min(get) * 1e3, 3)}
+    out["bytes_each_way"] = nbytes
+    out["how"] = ("kernel: conversion kernels on mapped page-locked buffers; dma: cudaMemcpyAsync to a device "
+                  "staging buffer + conversion kernel (PN_STATE_COPY=dma); best of %d" % reps)
+    return out
 
 
 def batch_leg(n_members, sample_steps, torch, steps_total=3000, form="auto"):
@@ -541,6 +594,8 @@ def main():
                        "how": "pn_solver_set_state from pinned host, one pn_solver_solve per step, "
                               "pn_solver_get_traces + pn_solver_get_state to pinned host; wall clock, "
                               "max over ranks; bytes summed over ranks"}
+        if rank == 0 and ws == 1:
+            line["e2e"]["state_transfer"] = state_transfer_leg(case, head, torch)
     if rank == 0:
         if ws == 1 and not args.no_holes:
             line["configs"] = {"holes": holes_leg(args.steps, args.warmup, torch, peak, peak_kind)}

@@ -366,6 +366,12 @@ void grid_create(pn_solver *s) {
     s->r_cmin = cmin;
     s->r_cmax = cmax;
     range_bounds(cmin, cmax, s->r_elo, s->r_ehi);
+  }
+  // coefficients themselves outside the split's exact range: IEEE double only
+  if (s->precision == PN_PREC_F64 && s->d_tmaps && s->r_elo <= s->r_ehi &&
+      (s->r_cmin < std::ldexp(1.0, -90) || s->r_cmax > std::ldexp(1.0, 90)))
+    s->r_elo = 1, s->r_ehi = 0;
+  if (s->precision == PN_PREC_F64 && s->d_tmaps && s->r_elo <= s->r_ehi) {
     const int64_t tiles = (int64_t)(g.nx / (kGridTileX - 1) + 1) * (g.ny / (kGridTileRows - 1) + 1);
     s->d_rflags = s->alloc<uint8_t>((size_t)(3 * tiles));
     s->d_pathcnt = s->alloc<unsigned long long>(2 * sizeof(unsigned long long));

@@ -237,7 +237,11 @@ struct pn_solver {
   // read or write it directly over the CPU-GPU link, without the staging
   // copy.  Null for any other memory (staged through device memory).  The
   // calls that use it wait for the stream before returning.
+  // PN_STATE_COPY=dma stages page-locked buffers too (copy engine, then the
+  // conversion kernel on device memory): for comparing the two paths.
   static void *device_view(const void *host) {
+    const char *mode = std::getenv("PN_STATE_COPY");
+    if (mode && mode[0] == 'd') return nullptr;
     cudaPointerAttributes at{};
     if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
       (void)cudaGetLastError();

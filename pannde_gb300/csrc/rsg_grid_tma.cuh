@@ -371,14 +371,13 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
   int waited = k0 - 2;                   // last layer this thread has waited for
   bool fail = false;
   bool oor = false;  // RANGE: a stored value outside the double-float range
+  auto store_d = [&](St *p, int64_t i, double d) {  // a double value (RANGE: tested)
+    if constexpr (RANGE) oor = oor || !in_df64_range(d, (uint32_t)a.r_elo, (uint32_t)a.r_ehi);
+    p[i] = (St)d;
+  };
   auto store = [&](St *p, int64_t i, R v) {
-    if constexpr (RANGE) {
-      const double d = N::dbl(v);
-      oor = oor || !in_df64_range(d, (uint32_t)a.r_elo, (uint32_t)a.r_ehi);
-      p[i] = (St)d;
-    } else {
-      N::st(p, i, v);
-    }
+    if constexpr (RANGE) store_d(p, i, N::dbl(v));
+    else N::st(p, i, v);
   };
 
   if constexpr (N::SPLIT) {
@@ -476,16 +475,28 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
         for (int c = 0; c < 3; c++) Vt[c * NT + t] = N::tsto(vn[c]);
         if (node_own && (k < k1 || last_chunk)) {
           const int64_t n = (int64_t)k * nplane + nidx0;
+          // the value stored and recorded: with split storage, a node the step
+          // leaves alone (dt/rho 0: void, or another partition's) keeps its
+          // stored double bit for bit instead of its split's 47 bits
+          auto out = [&](int c) -> double {
+            if constexpr (N::SPLIT) return cf.hi == 0.f ? (double)Vk[c * VB + rv] : N::dbl(vn[c]);
+            else return N::dbl(vn[c]);
+          };
+          if constexpr (N::SPLIT) {
 #pragma unroll
-          for (int c = 0; c < 3; c++) store(a.V_out[c], n, vn[c]);
+            for (int c = 0; c < 3; c++) store_d(a.V_out[c], n, out(c));
+          } else {
+#pragma unroll
+            for (int c = 0; c < 3; c++) store(a.V_out[c], n, vn[c]);
+          }
           const int2 sr = sRs[k - k0 + 1];
           if (rec < a.rec_cap) {
             for (int e = sr.x; e < sr.y; e++) {  // sensor traces
               if (__ldg(a.s_key + e) != t) continue;
               double *tr = a.traces + (rec * a.n_sens + __ldg(a.s_idx + e)) * 3;
-              tr[0] = N::dbl(vn[0]);
-              tr[1] = N::dbl(vn[1]);
-              tr[2] = N::dbl(vn[2]);
+              tr[0] = out(0);
+              tr[1] = out(1);
+              tr[2] = out(2);
             }
           }
         }
@@ -652,8 +663,14 @@ __device__ __forceinline__ bool fp64_path(const GridArgs<double> &a, int bx, int
   return fp64;
 }
 
+// resident blocks per SM the FP64 form's kernel is compiled for (its register
+// cap: 3 -> 80 registers, 2 -> 128)
+#ifndef PN_F64H_MIN_BLOCKS
+#define PN_F64H_MIN_BLOCKS 3
+#endif
+
 template <int SYM>
-__global__ void __launch_bounds__(TX * 8, 3) k_grid_tma_f64h(const GridArgs<double> a, int step) {
+__global__ void __launch_bounds__(TX * 8, PN_F64H_MIN_BLOCKS) k_grid_tma_f64h(const GridArgs<double> a, int step) {
   const GridMaps *M = reinterpret_cast<const GridMaps *>(a.tmaps);
   const int bx = blockIdx.x, by = blockIdx.y, bz = blockIdx.z, gxc = gridDim.x;
   if (fp64_path<8>(a, bx, by, bz, gxc, step))
@@ -663,7 +680,7 @@ __global__ void __launch_bounds__(TX * 8, 3) k_grid_tma_f64h(const GridArgs<doub
 }
 
 template <int SYM>
-__global__ void __launch_bounds__(TX * 8, 3)
+__global__ void __launch_bounds__(TX * 8, PN_F64H_MIN_BLOCKS)
     k_grid_tma_f64h_batch(const GridArgs<double> *__restrict__ args, const int *__restrict__ block_start,
                           int n_members, int step) {
   const int id = blockIdx.x;
