@@ -371,9 +371,11 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
   int waited = k0 - 2;                   // last layer this thread has waited for
   bool fail = false;
   bool oor = false;  // RANGE: a stored value outside the double-float range
-  auto store_d = [&](St *p, int64_t i, double d) {  // a double value (RANGE: tested)
+  // a double value into double storage (RANGE: tested); generic, so that it
+  // is instantiated only where called (double storage)
+  auto store_d = [&](auto *p, int64_t i, double d) {
     if constexpr (RANGE) oor = oor || !in_df64_range(d, (uint32_t)a.r_elo, (uint32_t)a.r_ehi);
-    p[i] = (St)d;
+    p[i] = d;
   };
   auto store = [&](St *p, int64_t i, R v) {
     if constexpr (RANGE) store_d(p, i, N::dbl(v));
