@@ -130,6 +130,25 @@ template <typename T> __device__ __forceinline__ void diffsum22(T a, T b, T c, T
   sum = ab + cd;
 }
 
+// c + sum_j a_j * b_j with one renormalisation at the end (the rows of the
+// stiffness product): each product's high part joins the running sum through
+// an error-free two_sum, its error terms and the low words are summed as
+// floats (12 flops per term against madd's 15, the same "sloppy" bound)
+struct df64_acc {
+  float hi, lo;
+};
+__device__ __forceinline__ df64_acc acc_start(df64 c) { return {c.hi, c.lo}; }
+__device__ __forceinline__ void acc_madd(df64_acc &s, df64 a, df64 b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  const df64 t = two_sum(s.hi, p);
+  s.hi = t.hi;
+  s.lo = __fadd_rn(s.lo, __fadd_rn(t.lo, e));
+}
+__device__ __forceinline__ df64 acc_end(df64_acc s) { return quick_two_sum(s.hi, s.lo); }
+
 // the same for the native types: the compiler contracts a*b + c into one FMA
 __device__ __forceinline__ float madd(float a, float b, float c) { return a * b + c; }
 __device__ __forceinline__ double madd(double a, double b, double c) { return a * b + c; }
@@ -165,6 +184,32 @@ __device__ __forceinline__ df64 split_double(double d) {
 // join_double: hi + lo rounded once to the nearest double (both convert
 // exactly; the FP64 add rounds the exact sum)
 __device__ __forceinline__ double join_double(df64 v) { return __dadd_rn((double)v.hi, (double)v.lo); }
+
+// join_double_int: hi + lo to a double within one unit in the last place,
+// on the integer and FP32 pipes (the FP64 unit converts at its FMA rate).
+// For a normalised pair (|lo| <= ulp(hi) / 2) the double of hi is its bits
+// rebiased (exponent + 896, fraction moved 29 bits down), and lo adds
+// k = lo * 2^(52 - E) units of that double's last place (|k| <= 2^28, the 29
+// zero bits below hi's fraction: no carry into the exponent).  When hi is a
+// power of two and lo of the other sign the sum falls into the binade below,
+// whose unit is half as large: k is counted in those units.  k is formed at
+// 2^(53 - E) and halved (rounding half up) otherwise.  Zero gives +0; hi below
+// 2^-74 (where the scale factor would leave float's range) takes join_double.
+__device__ __forceinline__ double join_double_int(df64 v) {
+  const uint32_t hb = __float_as_uint(v.hi), lb = __float_as_uint(v.lo);
+  const uint32_t u = hb & 0x7fffffffu;
+  if (u == 0u) return 0.0;
+  const uint32_t e8 = u >> 23;
+  if (e8 < 53u) return join_double(v);
+  const uint32_t hw = ((u >> 3) + 0x38000000u) | (hb & 0x80000000u);
+  const uint32_t lw = hb << 29;
+  const int kk = __float2int_rn(__fmul_rn(v.lo, __uint_as_float((307u - e8) << 23)));
+  const bool opposite = ((hb ^ lb) & 0x80000000u) != 0u;
+  const int mag = abs(kk);
+  const int step = ((u & 0x7fffffu) == 0u && opposite) ? mag : (mag + 1) >> 1;
+  const long long bits = (long long)(((unsigned long long)hw << 32) | lw) + (opposite ? -step : step);
+  return __longlong_as_double(bits);
+}
 
 // whether d is 0 or its biased exponent lies in [e_lo, e_hi]: the values the
 // double-float path of the FP64 form takes (bounds chosen by the host so that

@@ -147,17 +147,25 @@ template <> struct GNum<df64> {
   static __device__ __forceinline__ void st(float2 *p, int64_t i, df64 v) { p[i] = make_float2(v.hi, v.lo); }
   static __device__ __forceinline__ double dbl(df64 v) { return (double)v.hi + (double)v.lo; }
 };
+// stores of the FP64 form's double-float path: 1 joins on the integer and
+// FP32 pipes (join_double_int), 0 on the FP64 unit (join_double)
+#ifndef PN_F64H_JOIN_INT
+#define PN_F64H_JOIN_INT 1
+#endif
 template <> struct GNum<df64d> {
   using S = double;
   using T = float2;
   using R = df64;
   static constexpr bool SPLIT = true;
+  static __device__ __forceinline__ double join(df64 v) {
+    return PN_F64H_JOIN_INT ? join_double_int(v) : join_double(v);
+  }
   static __device__ __forceinline__ df64 ld(const double *p, int64_t i) { return split_double(__ldg(p + i)); }
   static __device__ __forceinline__ df64 val(double v) { return split_double(v); }
   static __device__ __forceinline__ df64 tval(float2 v) { return df64(v.x, v.y); }
   static __device__ __forceinline__ float2 tsto(df64 v) { return make_float2(v.hi, v.lo); }
-  static __device__ __forceinline__ void st(double *p, int64_t i, df64 v) { p[i] = join_double(v); }
-  static __device__ __forceinline__ double dbl(df64 v) { return join_double(v); }
+  static __device__ __forceinline__ void st(double *p, int64_t i, df64 v) { p[i] = join(v); }
+  static __device__ __forceinline__ double dbl(df64 v) { return join(v); }
 };
 
 __host__ __device__ constexpr bool c_used(int sym, int k, int j) {
@@ -571,22 +579,27 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
         bool ortho = (SYM & 3) == 2;
         if constexpr ((SYM & 3) != 2 && std::is_same<R, double>::value)
           ortho = __all_sync(__activemask(), (a.ortho_rows >> row) & 1u);
+        // one row of the stiffness product (double-float: one renormalisation per row)
+        auto prod_row = [&](int kk, int cls) {
+          if constexpr (std::is_same<R, df64>::value) {
+            df64_acc sacc = acc_start(acc[kk]);
+#pragma unroll
+            for (int jj = 0; jj < 6; jj++)
+              if (c_used(cls, kk, jj)) acc_madd(sacc, N::tval(Cm[6 * kk + jj]), e[jj]);
+            acc[kk] = acc_end(sacc);
+          } else {
+#pragma unroll
+            for (int jj = 0; jj < 6; jj++)
+              if (c_used(cls, kk, jj)) acc[kk] = madd(N::tval(Cm[6 * kk + jj]), e[jj], acc[kk]);
+          }
+          store(a.S_out[kk], cg, acc[kk]);
+        };
         if (ortho) {
 #pragma unroll
-          for (int kk = 0; kk < 6; kk++) {
-#pragma unroll
-            for (int jj = 0; jj < 6; jj++)
-              if (c_used(2, kk, jj)) acc[kk] = madd(N::tval(Cm[6 * kk + jj]), e[jj], acc[kk]);
-            store(a.S_out[kk], cg, acc[kk]);
-          }
+          for (int kk = 0; kk < 6; kk++) prod_row(kk, 2);
         } else {
 #pragma unroll
-          for (int kk = 0; kk < 6; kk++) {
-#pragma unroll
-            for (int jj = 0; jj < 6; jj++)
-              if (c_used(SYM & 3, kk, jj)) acc[kk] = madd(N::tval(Cm[6 * kk + jj]), e[jj], acc[kk]);
-            store(a.S_out[kk], cg, acc[kk]);
-          }
+          for (int kk = 0; kk < 6; kk++) prod_row(kk, SYM & 3);
         }
       }
 #pragma unroll
@@ -660,9 +673,29 @@ __device__ __forceinline__ bool fp64_path(const GridArgs<double> &a, int bx, int
       for (int e = e0 + t; e < e1; e += NT) f = f || bad(a.m_w[e], sigrow[a.m_sig[e]]);
     }
   }
-  const bool fp64 = __syncthreads_or(f) != 0;
-  if (t == 0 && a.path_count) atomicAdd(a.path_count + (fp64 ? 0 : 1), 1ull);
-  return fp64;
+  return __syncthreads_or(f) != 0;
+}
+
+// The FP64 form's kernels: MODE 0 runs each block on its path; with the two
+// paths as two launches (PN_F64H_TWO_LAUNCHES), MODE 1 runs the double-float
+// blocks and MODE 2 the FP64 ones (the other blocks return at once), so each
+// kernel gets registers for one path only.  Both launches decide alike.
+#ifndef PN_F64H_TWO_LAUNCHES
+#define PN_F64H_TWO_LAUNCHES 1
+#endif
+template <int SYM, bool BATCH, int MODE>
+__device__ __forceinline__ void f64h_block(const GridArgs<double> &a, int bx, int by, int bz, int gxc, int step) {
+  const GridMaps *M = reinterpret_cast<const GridMaps *>(a.tmaps);
+  const bool fp64 = fp64_path<8>(a, bx, by, bz, gxc, step);
+  if ((MODE == 1 && fp64) || (MODE == 2 && !fp64)) return;
+  if (threadIdx.x == 0 && a.path_count) atomicAdd(a.path_count + (fp64 ? 0 : 1), 1ull);
+  if constexpr (MODE != 1) {
+    if (fp64) {
+      grid_block_tma<double, SYM, 8, BATCH, true>(a, M, bx, by, bz, gxc, step);
+      return;
+    }
+  }
+  if constexpr (MODE != 2) grid_block_tma<df64d, SYM, 8, BATCH, true>(a, M, bx, by, bz, gxc, step);
 }
 
 // resident blocks per SM the FP64 form's kernel is compiled for (its register
@@ -671,17 +704,12 @@ __device__ __forceinline__ bool fp64_path(const GridArgs<double> &a, int bx, int
 #define PN_F64H_MIN_BLOCKS 3
 #endif
 
-template <int SYM>
+template <int SYM, int MODE>
 __global__ void __launch_bounds__(TX * 8, PN_F64H_MIN_BLOCKS) k_grid_tma_f64h(const GridArgs<double> a, int step) {
-  const GridMaps *M = reinterpret_cast<const GridMaps *>(a.tmaps);
-  const int bx = blockIdx.x, by = blockIdx.y, bz = blockIdx.z, gxc = gridDim.x;
-  if (fp64_path<8>(a, bx, by, bz, gxc, step))
-    grid_block_tma<double, SYM, 8, false, true>(a, M, bx, by, bz, gxc, step);
-  else
-    grid_block_tma<df64d, SYM, 8, false, true>(a, M, bx, by, bz, gxc, step);
+  f64h_block<SYM, false, MODE>(a, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x, step);
 }
 
-template <int SYM>
+template <int SYM, int MODE>
 __global__ void __launch_bounds__(TX * 8, PN_F64H_MIN_BLOCKS)
     k_grid_tma_f64h_batch(const GridArgs<double> *__restrict__ args, const int *__restrict__ block_start,
                           int n_members, int step) {
@@ -693,14 +721,9 @@ __global__ void __launch_bounds__(TX * 8, PN_F64H_MIN_BLOCKS)
     else hi = mid;
   }
   const GridArgs<double> &a = args[lo];
-  const GridMaps *M = reinterpret_cast<const GridMaps *>(a.tmaps);
   const int local = id - __ldg(block_start + lo);
   const int gxc = a.nx / (TX - 1) + 1, gyc = a.ny / 7 + 1;
-  const int bx = local % gxc, by = (local / gxc) % gyc, bz = local / (gxc * gyc);
-  if (fp64_path<8>(a, bx, by, bz, gxc, step))
-    grid_block_tma<double, SYM, 8, true, true>(a, M, bx, by, bz, gxc, step);
-  else
-    grid_block_tma<df64d, SYM, 8, true, true>(a, M, bx, by, bz, gxc, step);
+  f64h_block<SYM, true, MODE>(a, local % gxc, (local / gxc) % gyc, local / (gxc * gyc), gxc, step);
 }
 
 // minimum blocks per SM each storage type is compiled for (the register cap
@@ -793,7 +816,7 @@ cudaError_t launch_batch_t(const GridBatchLaunch &b, int step, cudaStream_t st) 
 }
 
 // the FP64 form's kernels (k_grid_tma_f64h*): the FP64 path's shared-memory geometry
-template <int SYM>
+template <int SYM, int MODE>
 struct SetupH {
   static constexpr size_t smem = Geo<8, 8>::SMEM;
   static cudaError_t ensure() {
@@ -803,9 +826,9 @@ struct SetupH {
     if (e != cudaSuccess) return e;
     const int d = dev & 63;
     if (!(done & (1ull << d))) {
-      e = cudaFuncSetAttribute(k_grid_tma_f64h<SYM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      e = cudaFuncSetAttribute(k_grid_tma_f64h<SYM, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_grid_tma_f64h_batch<SYM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(k_grid_tma_f64h_batch<SYM, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem);
       if (e != cudaSuccess) return e;
       done |= 1ull << d;
@@ -814,29 +837,50 @@ struct SetupH {
   }
 };
 
+template <int SYM, int MODE>
+cudaError_t launch_h_mode(const GridArgs<double> &b, const dim3 &grid, cudaStream_t st) {
+  cudaError_t e = SetupH<SYM, MODE>::ensure();
+  if (e != cudaSuccess) return e;
+  k_grid_tma_f64h<SYM, MODE><<<grid, TX * 8, SetupH<SYM, MODE>::smem, st>>>(b, 0);
+  return cudaGetLastError();
+}
+
 template <int SYM>
 cudaError_t launch_h(const GridArgs<double> &a, cudaStream_t st) {
   int sms = 0, per_sm = 0;
   cudaError_t e = SetupT<double, SYM, 8>::ensure(sms, per_sm);
-  if (e == cudaSuccess) e = SetupH<SYM>::ensure();
   if (e != cudaSuccess) return e;
   GridArgs<double> b = a;
   const unsigned gx = (unsigned)(a.nx / (TX - 1) + 1), gy = (unsigned)(a.ny / 7 + 1);
   if (b.kchunk <= 0) b.kchunk = grid_chunk_for(a.nz, (long long)gx * gy, sms, per_sm);
   if (b.kchunk > KC_MAX) return cudaErrorInvalidValue;
   const dim3 grid(gx, gy, (unsigned)((a.nz + b.kchunk - 1) / b.kchunk));
-  k_grid_tma_f64h<SYM><<<grid, TX * 8, SetupH<SYM>::smem, st>>>(b, 0);
+  if constexpr (PN_F64H_TWO_LAUNCHES != 0) {
+    e = launch_h_mode<SYM, 1>(b, grid, st);
+    return e == cudaSuccess ? launch_h_mode<SYM, 2>(b, grid, st) : e;
+  } else {
+    return launch_h_mode<SYM, 0>(b, grid, st);
+  }
+}
+
+template <int SYM, int MODE>
+cudaError_t launch_batch_h_mode(const GridBatchLaunch &b, int step, cudaStream_t st) {
+  cudaError_t e = SetupH<SYM, MODE>::ensure();
+  if (e != cudaSuccess) return e;
+  k_grid_tma_f64h_batch<SYM, MODE><<<b.total_blocks, TX * 8, SetupH<SYM, MODE>::smem, st>>>(
+      (const GridArgs<double> *)b.args, b.block_start, b.n_members, step);
   return cudaGetLastError();
 }
 
 template <int SYM>
 cudaError_t launch_batch_h(const GridBatchLaunch &b, int step, cudaStream_t st) {
-  cudaError_t e = SetupH<SYM>::ensure();
-  if (e != cudaSuccess) return e;
   if (b.total_blocks <= 0) return cudaSuccess;
-  k_grid_tma_f64h_batch<SYM><<<b.total_blocks, TX * 8, SetupH<SYM>::smem, st>>>(
-      (const GridArgs<double> *)b.args, b.block_start, b.n_members, step);
-  return cudaGetLastError();
+  if constexpr (PN_F64H_TWO_LAUNCHES != 0) {
+    const cudaError_t e = launch_batch_h_mode<SYM, 1>(b, step, st);
+    return e == cudaSuccess ? launch_batch_h_mode<SYM, 2>(b, step, st) : e;
+  } else {
+    return launch_batch_h_mode<SYM, 0>(b, step, st);
+  }
 }
 
 template <typename T> inline bool is_one(T v) { return v == T(1); }
