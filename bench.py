@@ -207,12 +207,15 @@ def whole_job_rate(units_per_rank, seconds, ws):
     return ws * units_per_rank / seconds
 
 
-def time_device(case, prec, steps, warmup, torch, dist, energy=False):
-    """Device throughput of the hot path with inputs resident in HBM."""
+def time_device(case, prec, steps, warmup, torch, dist, energy=False, state=None):
+    """Device throughput of the hot path with inputs resident in HBM (from
+    rest, or from `state` = (V, S))."""
     from pannde_gb300.solver import Solver
     s = Solver.from_case(case, precision=prec, capacity=warmup + steps, form=FORM)
     stream = torch.cuda.Stream()
     s.set_stream(stream)
+    if state is not None:
+        s.set_state(*state)
     s.solve(warmup)
     s.synchronize()
     if dist:
@@ -575,8 +578,23 @@ def main():
                        "l2": "no flush: each step moves far more than the 129 MB L2",
                        "parallelism": f"{ws} independent replica(s), one per GPU"},
             "roofline": roofline(args.case, info, kt, head, peak, peak_kind),
-            "gpu_launches": int(sum(v[1] for v in kt.values())),
+            "gpu_launches": int(kt["grid_step"][1] * info["launches_per_step"] + kt["velocity"][1] + kt["stress"][1]),
             "clocks": clocks}
+    if head == "f64" and line["roofline"].get("f64_paths"):
+        # the same step from a developed state (every value inside the
+        # double-float range), beside the window from rest above
+        rng = np.random.default_rng(11)
+        state = ([rng.uniform(-1e-3, 1e-3, case.mesh.n_nodes) for _ in range(3)],
+                 [rng.uniform(-1e5, 1e5, case.mesh.n_cells) for _ in range(6)])
+        msd, ktd, infod = time_device(case, head, args.steps, args.warmup, torch, dist, state=state)
+        rd = roofline(args.case, infod, ktd, head, peak, peak_kind)
+        line["roofline"]["f64_developed_state"] = {
+            "value": round(whole_job_rate(cells * args.steps, msd * 1e-3, ws) / 1e9, 4), "unit": UNIT,
+            "ms_per_step": round(msd / args.steps, 4), "frac": rd["frac"],
+            "double_float_share": rd.get("f64_paths", {}).get("double_float_share"),
+            "state": "seeded uniform random velocities (+-1e-3 m/s) and stresses (+-1e5 Pa): a step well "
+                     "into a run, every value inside the double-float range"}
+        del state
     forms = {}
     for prec in precs[1:]:
         msp, ktp, infop = time_device(case, prec, args.steps, args.warmup, torch, dist)

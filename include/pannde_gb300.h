@@ -201,7 +201,9 @@ typedef struct pn_solver_info {
   double time;
   int32_t form;              /* PN_FORM_TABLE or PN_FORM_GRID */
   int32_t grid[3];           /* grid form: cells per axis */
-  int32_t grid_kernel;       /* grid form: 1 classic (register prefetch), 2 tensor-copy staging; 0 table */
+  int32_t grid_kernel;       /* grid form: 1 classic (register prefetch), 2 tensor-copy staging, 3
+                                tensor-copy staging in the FP64 form's two launches per step (its
+                                double-float and its FP64 blocks); 0 table */
 } pn_solver_info;
 
 /* What pn_solver_create would build, computed on the host only. */

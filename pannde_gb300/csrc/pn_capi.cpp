@@ -533,7 +533,7 @@ int pn_solver_get_info(pn_solver *s, pn_solver_info *info) {
     info->grid[0] = s->grid.nx;
     info->grid[1] = s->grid.ny;
     info->grid[2] = s->grid.nz;
-    info->grid_kernel = s->d_tmaps ? 2 : 1;
+    info->grid_kernel = !s->d_tmaps ? 1 : (s->d_rflags && pn::grid_tma_f64_launches() == 2) ? 3 : 2;
   }
   return PN_OK;
 }

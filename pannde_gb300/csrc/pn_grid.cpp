@@ -349,29 +349,31 @@ void grid_create(pn_solver *s) {
   // (PN_F64_PATH=fp64 keeps every block on the FP64 path, for comparisons)
   const char *path = std::getenv("PN_F64_PATH");
   if (s->precision == PN_PREC_F64 && s->d_tmaps && !(path && std::strcmp(path, "fp64") == 0)) {
-    double cmin = 1.0, cmax = 1.0;
-    auto see = [&](double v) {
+    double vmin = 1.0, vmax = 1.0, smin = 1.0, smax = 1.0;
+    auto see = [](double v, double &lo, double &hi) {
       v = std::fabs(v);
       if (v == 0.0) return;
-      cmin = std::min(cmin, v);
-      cmax = std::max(cmax, v);
+      lo = std::min(lo, v);
+      hi = std::max(hi, v);
     };
-    for (int64_t q = 0; q < gn; q++) see(coef[q]);
-    for (double v : ct) see(v);
-    if (s->gfold == 1.0) {
-      see(0.25 / s->mesh.hx);
-      see(0.25 / s->mesh.hy);
-      see(0.25 / s->mesh.hz);
-    }
-    s->r_cmin = cmin;
-    s->r_cmax = cmax;
-    range_bounds(cmin, cmax, s->r_elo, s->r_ehi);
+    for (double v : ct) see(v, vmin, vmax);                            // velocities x dt*C*g
+    for (int64_t q = 0; q < gn; q++) see(coef[q], smin, smax);          // stresses x dt/rho*g
+    if (s->gfold == 1.0)
+      for (double h : {s->mesh.hx, s->mesh.hy, s->mesh.hz}) {
+        see(0.25 / h, vmin, vmax);
+        see(0.25 / h, smin, smax);
+      }
+    s->r_cmin = vmin;
+    s->r_cmax = vmax;
+    s->r_cmin_s = smin;
+    s->r_cmax_s = smax;
+    range_bounds(vmin, vmax, s->r_elo, s->r_ehi);
+    range_bounds(smin, smax, s->r_elo_s, s->r_ehi_s);
   }
   // coefficients themselves outside the split's exact range: IEEE double only
-  if (s->precision == PN_PREC_F64 && s->d_tmaps && s->r_elo <= s->r_ehi &&
-      (s->r_cmin < std::ldexp(1.0, -90) || s->r_cmax > std::ldexp(1.0, 90)))
-    s->r_elo = 1, s->r_ehi = 0;
-  if (s->precision == PN_PREC_F64 && s->d_tmaps && s->r_elo <= s->r_ehi) {
+  const bool extreme = std::min(s->r_cmin, s->r_cmin_s) < std::ldexp(1.0, -90) ||
+                       std::max(s->r_cmax, s->r_cmax_s) > std::ldexp(1.0, 90);
+  if (s->precision == PN_PREC_F64 && s->d_tmaps && s->r_elo <= s->r_ehi && s->r_elo_s <= s->r_ehi_s && !extreme) {
     const int64_t tiles = (int64_t)(g.nx / (kGridTileX - 1) + 1) * (g.ny / (kGridTileRows - 1) + 1);
     s->d_rflags = s->alloc<uint8_t>((size_t)(3 * tiles));
     s->d_pathcnt = s->alloc<unsigned long long>(2 * sizeof(unsigned long long));
@@ -577,8 +579,8 @@ void grid_sources(pn_solver *s) {
   }
   upload(F, g.nz + 1, s->d_frng, s->d_fkey, s->d_fsig, s->d_fw);
   upload(M, g.nz, s->d_mrng, s->d_mkey, s->d_msig, s->d_mw);
-  if (s->d_rflags) {  // the double-float range also covers the source weights
-    double cmin = s->r_cmin, cmax = s->r_cmax;
+  if (s->d_rflags) {  // the stresses' double-float range also covers the source weights
+    double cmin = s->r_cmin_s, cmax = s->r_cmax_s;
     for (const std::vector<Keyed> *L : {&F, &M})
       for (const Keyed &k : *L) {
         const double v = std::fabs(k.w);
@@ -588,7 +590,7 @@ void grid_sources(pn_solver *s) {
       }
     for (auto &f : s->split_forces) if (f.w != 0.0) { cmin = std::min(cmin, std::fabs(f.w)); cmax = std::max(cmax, std::fabs(f.w)); }
     for (auto &m : s->fix_moments) if (m.w != 0.0) { cmin = std::min(cmin, std::fabs(m.w)); cmax = std::max(cmax, std::fabs(m.w)); }
-    range_bounds(cmin, cmax, s->r_elo, s->r_ehi);
+    range_bounds(cmin, cmax, s->r_elo_s, s->r_ehi_s);
     grid_reset_range_flags(s);  // tiles judged under the old bounds: FP64 for one step
   }
   grid_split_upload(s);
@@ -690,6 +692,8 @@ void grid_args(pn_solver *s, GridArgs<T> &a) {
   a.flag_phase = (int32_t)(s->step % 3);
   a.r_elo = s->r_elo;
   a.r_ehi = s->r_ehi;
+  a.r_elo_s = s->r_elo_s;
+  a.r_ehi_s = s->r_ehi_s;
   a.path_count = s->d_pathcnt;
 }
 

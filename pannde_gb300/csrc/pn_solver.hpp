@@ -89,11 +89,13 @@ struct pn_solver {
   mutable int64_t step_bytes_cached = 0;  // grid form: algorithmic bytes of one step (0: not yet)
   int tile_rows = pn::kGridTileRows;      // grid form: rows TY of the 32 x TY block tiles
   // FP64 form with the tensor-copy kernel: per-tile path flags [3][tiles] and
-  // the double-float range (biased double exponents), from the coefficient
-  // magnitudes r_cmin..r_cmax; block counts of the two paths [fp64, df64]
+  // the double-float ranges (biased double exponents) of velocities and of
+  // stresses, from the magnitudes of the coefficients each is multiplied by
+  // (velocities: dt*C*g and g; stresses: dt/rho*g, g and source weights);
+  // block counts of the two paths [fp64, df64]
   uint8_t *d_rflags = nullptr;
-  int32_t r_elo = 1, r_ehi = 0;
-  double r_cmin = 1.0, r_cmax = 1.0;
+  int32_t r_elo = 1, r_ehi = 0, r_elo_s = 1, r_ehi_s = 0;
+  double r_cmin = 1.0, r_cmax = 1.0, r_cmin_s = 1.0, r_cmax_s = 1.0;
   unsigned long long *d_pathcnt = nullptr;
   std::vector<std::pair<int32_t, int32_t>> sensor_pairs;  // grid form: (node, sensor) sorted, for re-tiling
   // cubic lattice with the tensor-copy kernel: 0.25/h folded into dt/rho, dt*C

@@ -84,11 +84,13 @@ struct GridArgs {
   int32_t test_skip_layer;  // failure-path test: the layer whose copies are never issued (kNoLayer: none)
   int32_t tile_rows;        // rows TY of the 32 x TY block tile (8, or 16 with the tensor-copy kernel)
   // FP64 form with the tensor-copy kernel: per-tile path flags [3][tiles]
-  // (rsg_grid_tma.cuh fp64_path) and the double-float range as biased double
-  // exponents [r_elo, r_ehi]; rflags null: no path choice (the other forms)
+  // (rsg_grid_tma.cuh fp64_path) and the double-float ranges as biased double
+  // exponents, [r_elo, r_ehi] for velocities and [r_elo_s, r_ehi_s] for
+  // stresses and source terms; rflags null: no path choice (the other forms)
   uint8_t *rflags;
   int32_t flag_phase;       // (step of this launch's step 0) % 3
   int32_t r_elo, r_ehi;
+  int32_t r_elo_s, r_ehi_s;
   unsigned long long *path_count;  // [2] blocks that took the FP64 / double-float path, or null
 };
 
@@ -137,6 +139,9 @@ int grid_tma_blocks_per_sm(int precision, int tile_rows = kGridTileRows);
 cudaError_t launch_grid_tma(const void *args /* GridArgs<storage type> */, int precision, int sym,
                             cudaStream_t st);
 cudaError_t launch_grid_tma_batch(const GridBatchLaunch &b, int precision, int step, cudaStream_t st);
+// kernel launches of one FP64-form step (the double-float and the FP64 blocks
+// in one launch or in two)
+int grid_tma_f64_launches();
 
 // fix-up of split sites after a step launch (rsg_split.cu): the copies'
 // velocities, then the fix cells' stresses, from the step's input buffers

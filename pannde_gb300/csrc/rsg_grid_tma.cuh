@@ -379,14 +379,17 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
   int waited = k0 - 2;                   // last layer this thread has waited for
   bool fail = false;
   bool oor = false;  // RANGE: a stored value outside the double-float range
-  // a double value into double storage (RANGE: tested); generic, so that it
-  // is instantiated only where called (double storage)
-  auto store_d = [&](auto *p, int64_t i, double d) {
-    if constexpr (RANGE) oor = oor || !in_df64_range(d, (uint32_t)a.r_elo, (uint32_t)a.r_ehi);
+  // a double value into double storage (RANGE: tested against the velocity
+  // range, field 0, or the stress range, field 1); generic, so that it is
+  // instantiated only where called (double storage)
+  auto store_d = [&](auto *p, int64_t i, double d, int field) {
+    if constexpr (RANGE)
+      oor = oor || !in_df64_range(d, (uint32_t)(field ? a.r_elo_s : a.r_elo),
+                                  (uint32_t)(field ? a.r_ehi_s : a.r_ehi));
     p[i] = d;
   };
-  auto store = [&](St *p, int64_t i, R v) {
-    if constexpr (RANGE) store_d(p, i, N::dbl(v));
+  auto store = [&](St *p, int64_t i, R v, int field) {
+    if constexpr (RANGE) store_d(p, i, N::dbl(v), field);
     else N::st(p, i, v);
   };
 
@@ -494,10 +497,10 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
           };
           if constexpr (N::SPLIT) {
 #pragma unroll
-            for (int c = 0; c < 3; c++) store_d(a.V_out[c], n, out(c));
+            for (int c = 0; c < 3; c++) store_d(a.V_out[c], n, out(c), 0);
           } else {
 #pragma unroll
-            for (int c = 0; c < 3; c++) store(a.V_out[c], n, vn[c]);
+            for (int c = 0; c < 3; c++) store(a.V_out[c], n, vn[c], 0);
           }
           const int2 sr = sRs[k - k0 + 1];
           if (rec < a.rec_cap) {
@@ -592,7 +595,7 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
             for (int jj = 0; jj < 6; jj++)
               if (c_used(cls, kk, jj)) acc[kk] = madd(N::tval(Cm[6 * kk + jj]), e[jj], acc[kk]);
           }
-          store(a.S_out[kk], cg, acc[kk]);
+          store(a.S_out[kk], cg, acc[kk], 1);
         };
         if (ortho) {
 #pragma unroll
@@ -660,7 +663,7 @@ __device__ __forceinline__ bool fp64_path(const GridArgs<double> &a, int bx, int
   const int k0 = bz * a.kchunk, k1 = min(ktop, k0 + a.kchunk);
   if (k0 < ktop && a.sigval) {
     const double *sigrow = a.sigval + (int64_t)min(step, a.sig_rows - 1) * a.sig_stride;
-    const uint32_t lo = (uint32_t)a.r_elo, hi = (uint32_t)a.r_ehi;
+    const uint32_t lo = (uint32_t)a.r_elo_s, hi = (uint32_t)a.r_ehi_s;
     auto bad = [&](double w, double sg) { return !in_df64_range(sg, lo, hi) || !in_df64_range(w * sg, lo, hi); };
     if (a.f_rng) {  // force entries of node layers k0-1 .. k1 (contiguous per block)
       const int64_t r0 = (int64_t)blk * (nz + 1);
@@ -680,8 +683,12 @@ __device__ __forceinline__ bool fp64_path(const GridArgs<double> &a, int bx, int
 // paths as two launches (PN_F64H_TWO_LAUNCHES), MODE 1 runs the double-float
 // blocks and MODE 2 the FP64 ones (the other blocks return at once), so each
 // kernel gets registers for one path only.  Both launches decide alike.
+// Measured on the laminate bench step (15% FP64 blocks): one launch 0.663 ms,
+// two launches 1.049 ms -- in one launch the FP64 blocks share the SMs with
+// double-float ones and the two pipes work at once; alone, the FP64 blocks
+// are a serial tail on a few SMs.  One launch is the default.
 #ifndef PN_F64H_TWO_LAUNCHES
-#define PN_F64H_TWO_LAUNCHES 1
+#define PN_F64H_TWO_LAUNCHES 0
 #endif
 template <int SYM, bool BATCH, int MODE>
 __device__ __forceinline__ void f64h_block(const GridArgs<double> &a, int bx, int by, int bz, int gxc, int step) {

@@ -15,4 +15,6 @@ cudaError_t launch_grid_tma_batch_f64h(const GridBatchLaunch &b, int step, cudaS
   return launch_batch_sym_h(b, step, st);
 }
 
+int grid_tma_f64_launches() { return PN_F64H_TWO_LAUNCHES ? 2 : 1; }
+
 }  // namespace pn

@@ -48,8 +48,10 @@ constexpr int TPB = 128;
 // puts the tile of lattice column (i, j) on the FP64 path for the next step
 // (the tensor-copy kernel's flags, rsg_grid_tma.cuh fp64_path)
 template <typename S>
-__device__ __forceinline__ void flag_range(const GridArgs<S> &a, double v, int64_t i, int64_t j, int step) {
-  if (!a.rflags || in_df64_range(v, (uint32_t)a.r_elo, (uint32_t)a.r_ehi)) return;
+__device__ __forceinline__ void flag_range(const GridArgs<S> &a, double v, int64_t i, int64_t j, int step,
+                                           bool stress) {
+  if (!a.rflags || in_df64_range(v, (uint32_t)(stress ? a.r_elo_s : a.r_elo), (uint32_t)(stress ? a.r_ehi_s : a.r_ehi)))
+    return;
   const int gxc = a.nx / (kGridTileX - 1) + 1, gyc = a.ny / (a.tile_rows - 1) + 1;
   const int64_t blk = (j / (a.tile_rows - 1)) * gxc + i / (kGridTileX - 1);
   a.rflags[((a.flag_phase + step + 1) % 3) * (int64_t)gxc * gyc + blk] = 1;
@@ -100,7 +102,7 @@ __device__ void copy_velocity(const GridArgs<S> &a, int q, int step) {
     vn[c] = N::val(a.V_in[c][cp.v]);
     if (!(cf == R())) vn[c] = madd(cf, acc[c], vn[c]);
     a.V_out[c][cp.v] = N::sto(vn[c]);
-    flag_range(a, N::dbl(vn[c]), cp.i, cp.j, step);
+    flag_range(a, N::dbl(vn[c]), cp.i, cp.j, step, false);
   }
   const int64_t rec = a.rec + step;
   if (rec < a.rec_cap)
@@ -159,7 +161,7 @@ __device__ void fix_stress(const GridArgs<S> &a, int q, int step) {
 #pragma unroll
     for (int j = 0; j < 6; j++) acc[k] = madd(N::val(Cm[6 * k + j]), e[j], acc[k]);
     a.S_out[k][fc.cell] = N::sto(acc[k]);
-    flag_range(a, N::dbl(acc[k]), fc.cell % a.pcx, (fc.cell / a.pcx) % a.ny, step);
+    flag_range(a, N::dbl(acc[k]), fc.cell % a.pcx, (fc.cell / a.pcx) % a.ny, step, true);
   }
 }
 

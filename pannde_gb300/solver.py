@@ -159,7 +159,8 @@ class Solver:
         d = {k: getattr(inf, k) for k, _ in N.PnSolverInfo._fields_}
         d["grid"] = tuple(d["grid"])
         d["form_name"] = {N.PN_FORM_GRID: "grid", N.PN_FORM_TABLE: "table"}.get(d["form"], "?")
-        d["kernel_name"] = {1: "classic", 2: "tma"}.get(d["grid_kernel"], "table")
+        d["kernel_name"] = {1: "classic", 2: "tma", 3: "tma-f64-two-launch"}.get(d["grid_kernel"], "table")
+        d["launches_per_step"] = 2 if d["grid_kernel"] == 3 else (1 if d["form"] == N.PN_FORM_GRID else 2)
         return d
 
     def device_state(self):
