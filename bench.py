@@ -367,7 +367,7 @@ def state_transfer_leg(case, prec, torch, reps=3):
     return out
 
 
-def batch_leg(n_members, sample_steps, torch, steps_total=3000, form="auto"):
+def batch_leg(n_members, sample_steps, torch, steps_total=3000, form="auto", peak=None, peak_kind=None):
     """Batched sims/hour: n_members seeded L-brackets (legs 60-220 cells, 12-30
     thick, 40-160 deep, 0.1 mm voxels, a 1-6 mm crack at the inner fillet as
     disconnected faces; every sixth with an acoustic-fluid column and a
@@ -391,6 +391,7 @@ def batch_leg(n_members, sample_steps, torch, steps_total=3000, form="auto"):
     setup_s = time.perf_counter() - t0
     cells = sum(c.mesh.n_cells for c in cs)
     forms = sorted({s.info()["form_name"] for s in solvers})
+    alg = sum(s.info()["algorithmic_bytes_per_step"] for s in solvers)
     with Batch() as b:
         for s in solvers:
             b.add(s)
@@ -412,13 +413,21 @@ def batch_leg(n_members, sample_steps, torch, steps_total=3000, form="auto"):
     for s in solvers:
         s.close()
     per_step_s = ms * 1e-3 / sample_steps
+    roof = None
+    if peak:
+        achieved = alg / per_step_s / 1e9
+        traffic = profile_figures("brackets%d" % n_members, forms[0], "f32", "traffic").get("batch_step")
+        roof = {"bound": "hbm", "kernel": "batch step (fused step launch + split-site fix-up)",
+                "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "peak_source": peak_kind, "traffic": traffic, "algorithmic_bytes": alg,
+                "note": "algorithmic bytes: every member's marched lattice (12e+1 per cell, 7e per node, e=4)"}
     return {"sims_per_hour": round(n_members / (per_step_s * steps_total) * 3600.0, 1),
             "gcell_steps_per_s": round(cells / per_step_s / 1e9, 4),
             "members": n_members, "cells_total": cells, "steps_per_sim": steps_total,
             "timed_steps": sample_steps, "ms_per_batch_step": round(ms / sample_steps, 4),
             "steps_per_call": quantum, "graph_launches": plan["graph_launches"],
             "tuned_shape": {"tile": f"32x{plan['tile_rows']}", "z_chunks_per_column": plan["shape"] or "launcher"},
-            "dtype": "f32", "form": ",".join(forms), "setup_s": round(setup_s, 1),
+            "dtype": "f32", "form": ",".join(forms), "setup_s": round(setup_s, 1), "roofline": roof,
             "workload": f"{n_members} seeded L-brackets with a disconnected-face crack, every sixth with a "
                         "water column (pressure source), FP32, one pn_batch_solve over all members"}
 
@@ -618,7 +627,8 @@ def main():
         if ws == 1 and not args.no_holes:
             line["configs"] = {"holes": holes_leg(args.steps, args.warmup, torch, peak, peak_kind)}
         if ws == 1 and not args.no_batch:
-            line["batch"] = batch_leg(args.batch_members, args.batch_sample_steps, torch, form=args.batch_form)
+            line["batch"] = batch_leg(args.batch_members, args.batch_sample_steps, torch, form=args.batch_form,
+                                      peak=peak, peak_kind=peak_kind)
         if ws == 1 and not args.no_serving:
             line["serving"] = serving_leg(args.serving_requests, args.serving_rate, torch,
                                          subset=args.serving_fp64_subset)

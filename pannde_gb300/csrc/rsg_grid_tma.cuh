@@ -690,6 +690,12 @@ __device__ __forceinline__ bool fp64_path(const GridArgs<double> &a, int bx, int
 #ifndef PN_F64H_TWO_LAUNCHES
 #define PN_F64H_TWO_LAUNCHES 0
 #endif
+template <typename K, int SYM, bool BATCH>
+__device__ __forceinline__ void f64h_path(const GridArgs<double> &a, const GridMaps *M, int bx, int by, int bz,
+                                          int gxc, int step) {
+  grid_block_tma<K, SYM, 8, BATCH, true>(a, M, bx, by, bz, gxc, step);
+}
+
 template <int SYM, bool BATCH, int MODE>
 __device__ __forceinline__ void f64h_block(const GridArgs<double> &a, int bx, int by, int bz, int gxc, int step) {
   const GridMaps *M = reinterpret_cast<const GridMaps *>(a.tmaps);
@@ -698,11 +704,11 @@ __device__ __forceinline__ void f64h_block(const GridArgs<double> &a, int bx, in
   if (threadIdx.x == 0 && a.path_count) atomicAdd(a.path_count + (fp64 ? 0 : 1), 1ull);
   if constexpr (MODE != 1) {
     if (fp64) {
-      grid_block_tma<double, SYM, 8, BATCH, true>(a, M, bx, by, bz, gxc, step);
+      f64h_path<double, SYM, BATCH>(a, M, bx, by, bz, gxc, step);
       return;
     }
   }
-  if constexpr (MODE != 2) grid_block_tma<df64d, SYM, 8, BATCH, true>(a, M, bx, by, bz, gxc, step);
+  if constexpr (MODE != 2) f64h_path<df64d, SYM, BATCH>(a, M, bx, by, bz, gxc, step);
 }
 
 // resident blocks per SM the FP64 form's kernel is compiled for (its register
@@ -712,7 +718,8 @@ __device__ __forceinline__ void f64h_block(const GridArgs<double> &a, int bx, in
 #endif
 
 template <int SYM, int MODE>
-__global__ void __launch_bounds__(TX * 8, PN_F64H_MIN_BLOCKS) k_grid_tma_f64h(const GridArgs<double> a, int step) {
+__global__ void __launch_bounds__(TX * 8, PN_F64H_MIN_BLOCKS)
+    k_grid_tma_f64h(const __grid_constant__ GridArgs<double> a, int step) {
   f64h_block<SYM, false, MODE>(a, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x, step);
 }
 
