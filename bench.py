@@ -273,15 +273,14 @@ def roofline(case, info, kt, prec, peak, peak_kind):
                             "double_float_share": round(df / (fp64 + df), 4),
                             "note": "blocks of the timed steps by arithmetic path (pn_solver_path_counts)"}
     if prec == "f64":
-        # the FP64 form is bound by GB300's FP64 pipe, not by HBM: its operation
-        # count per cell-step and the pipe's busy fraction come from ncu
-        dp = profile_figures(case, form, prec, "dpops").get(dom)
-        busy = profile_figures(case, form, prec, "fp64pipe").get(dom)
-        if dp:
-            rate = dp * nc / (avg[dom] * 1e-3)
-            out["fp64_pipe"] = {"ops_per_cell_step_ncu": dp, "achieved_ops_per_s": round(rate, 0),
-                                "busy_frac_ncu": busy,
-                                "note": "DFMA-bound: GB300 runs FP64 at about 1/30 of its FP32 rate"}
+        # pipe use of the FP64 form's step from the committed ncu summary
+        # (profiles/*.txt lines 'fp64pipe' / 'fmapipe' / 'issue' for this key)
+        fig = {w: profile_figures(case, form, prec, w).get(dom) for w in ("fp64pipe", "fmapipe", "issue")}
+        if any(v is not None for v in fig.values()):
+            out["pipes_ncu"] = {"fp64_pipe_busy": fig["fp64pipe"], "fma_pipe_busy": fig["fmapipe"],
+                                "issue_active": fig["issue"],
+                                "note": "FP64 form: double-float blocks on the FP32/integer pipes beside IEEE-double "
+                                        "blocks on the FP64 pipe, one launch"}
     return out
 
 

@@ -211,6 +211,22 @@ __device__ __forceinline__ double join_double_int(df64 v) {
   return __longlong_as_double(bits);
 }
 
+// float_bits_to_double: a normal float's exact double by its bits (exponent
+// rebiased by +896, fraction moved 29 bits down); 0 for +-0.  A subnormal
+// float (below 2^-126, outside every range the double-float path admits)
+// comes out wrong by at most 2^-126.
+__device__ __forceinline__ double float_bits_to_double(float f) {
+  const uint32_t b = __float_as_uint(f), u = b & 0x7fffffffu;
+  const uint32_t hw = u ? (((u >> 3) + 0x38000000u) | (b & 0x80000000u)) : 0u;
+  return __hiloint2double((int)hw, (int)(b << 29));
+}
+
+// base + (hi + lo): the pair added to a double by two FP64 adds of its exact
+// halves (within one unit in the last place of the sum)
+__device__ __forceinline__ double add_pair(double base, df64 inc) {
+  return __dadd_rn(__dadd_rn(base, float_bits_to_double(inc.hi)), float_bits_to_double(inc.lo));
+}
+
 // whether d is 0 or its biased exponent lies in [e_lo, e_hi]: the values the
 // double-float path of the FP64 form takes (bounds chosen by the host so that
 // every product with the step's coefficients stays within 2^+-100)

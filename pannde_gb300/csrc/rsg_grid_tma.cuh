@@ -152,6 +152,15 @@ template <> struct GNum<df64> {
 #ifndef PN_F64H_JOIN_INT
 #define PN_F64H_JOIN_INT 1
 #endif
+// the path's increments onto the stored doubles: 1 by the pair's exact halves
+// and two FP64 adds (add_pair), 0 by one join and one FP64 add
+#ifndef PN_F64H_ADD_PAIR
+#define PN_F64H_ADD_PAIR 1
+#endif
+__device__ __forceinline__ double add_increment(double base, df64 inc) {
+  if (PN_F64H_ADD_PAIR) return add_pair(base, inc);
+  return __dadd_rn(base, PN_F64H_JOIN_INT ? join_double_int(inc) : join_double(inc));
+}
 template <> struct GNum<df64d> {
   using S = double;
   using T = float2;
@@ -354,16 +363,17 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
   }
   // split the stress slot of layer L in place (df64d): each stored double
   // becomes its double-float pair, so the velocity half reads pairs; the
-  // slot is waited for first (false: the wait gave up)
-  constexpr int BOXE = G::BWC * (TY + 1);  // elements of one field's stress box
+  // slot is waited for first (false: the wait gave up).  Two elements per
+  // 16-byte shared access over the whole slot (6 fields x SB elements, SB
+  // even; the few padding elements past each box are split too and never read)
   auto split_slot = [&](int L) {
     if (!mbar_wait(bar_of(L), parity(L))) return false;
-    double *sl = reinterpret_cast<double *>(sslot(L));
-    for (int q = t; q < 6 * BOXE; q += NT) {
-      const int f = q / BOXE;
-      double *pd = sl + f * SB + (q - f * BOXE);
-      const df64 v = split_double(*pd);
-      *reinterpret_cast<float2 *>(pd) = make_float2(v.hi, v.lo);
+    double2 *sl = reinterpret_cast<double2 *>(sslot(L));
+    static_assert(SB % 2 == 0, "pairs of elements");
+    for (int q = t; q < 3 * SB; q += NT) {
+      const double2 d = sl[q];
+      const df64 u = split_double(d.x), w = split_double(d.y);
+      reinterpret_cast<float4 *>(sl)[q] = make_float4(u.hi, u.lo, w.hi, w.lo);
     }
     return true;
   };
@@ -475,24 +485,36 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
         }
         const St *Vk = reinterpret_cast<const St *>(vslot(k));
         R vn[3];
-#pragma unroll
-        for (int c = 0; c < 3; c++) vn[c] = N::val(Vk[c * VB + rv]);
+        double vd[3];  // split storage: the new velocity as stored and recorded
         // dt/rho is 0 at void and padding sites, whose differences are 0 too:
         // the update leaves them unchanged without a branch
         const R cf = N::val(Vk[3 * VB + rv]);
-        vn[0] = madd(cf, ax, vn[0]);
-        vn[1] = madd(cf, ay, vn[1]);
-        vn[2] = madd(cf, az, vn[2]);
+        if constexpr (N::SPLIT) {
+          // the increment in double-float, added to the stored double by one
+          // FP64 add: the old value enters exactly (a node the step leaves
+          // alone keeps its bits), and only the new one is split, for the
+          // stress half
+          const R acc3[3] = {ax, ay, az};
+#pragma unroll
+          for (int c = 0; c < 3; c++) {
+            vd[c] = add_increment((double)Vk[c * VB + rv], cf * acc3[c]);
+            vn[c] = split_double(vd[c]);
+          }
+        } else {
+#pragma unroll
+          for (int c = 0; c < 3; c++) vn[c] = N::val(Vk[c * VB + rv]);
+          vn[0] = madd(cf, ax, vn[0]);
+          vn[1] = madd(cf, ay, vn[1]);
+          vn[2] = madd(cf, az, vn[2]);
+        }
         Sm *Vt = sVt + (k & 1) * 3 * NT;
 #pragma unroll
         for (int c = 0; c < 3; c++) Vt[c * NT + t] = N::tsto(vn[c]);
         if (node_own && (k < k1 || last_chunk)) {
           const int64_t n = (int64_t)k * nplane + nidx0;
-          // the value stored and recorded: with split storage, a node the step
-          // leaves alone (dt/rho 0: void, or another partition's) keeps its
-          // stored double bit for bit instead of its split's 47 bits
+          // the value stored and recorded
           auto out = [&](int c) -> double {
-            if constexpr (N::SPLIT) return cf.hi == 0.f ? (double)Vk[c * VB + rv] : N::dbl(vn[c]);
+            if constexpr (N::SPLIT) return vd[c];
             else return N::dbl(vn[c]);
           };
           if constexpr (N::SPLIT) {
@@ -555,8 +577,11 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
         const int64_t cg = (int64_t)kc * cplane + cidx0;
         const int row = mslot(kc)[ty * G::BWM + om + tx];
         const Sm *Cm = sC + 36 * row;
-        R acc[6];  // the cell's stress before the update
-        if constexpr (G::OWN_SMEM) {
+        R acc[6];  // the cell's stress before the update (split storage: its increment)
+        if constexpr (N::SPLIT) {  // the old stress joins at the store, by one FP64 add
+#pragma unroll
+          for (int f = 0; f < 6; f++) acc[f] = R();
+        } else if constexpr (G::OWN_SMEM) {
           const Sm *Sc = reinterpret_cast<const Sm *>(sslot(kc));
           const int own = ra + G::BWC + 1;  // cell (i, j)
 #pragma unroll
@@ -595,7 +620,8 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
             for (int jj = 0; jj < 6; jj++)
               if (c_used(cls, kk, jj)) acc[kk] = madd(N::tval(Cm[6 * kk + jj]), e[jj], acc[kk]);
           }
-          store(a.S_out[kk], cg, acc[kk], 1);
+          if constexpr (N::SPLIT) store_d(a.S_out[kk], cg, add_increment(__ldg(a.S_in[kk] + cg), acc[kk]), 1);
+          else store(a.S_out[kk], cg, acc[kk], 1);
         };
         if (ortho) {
 #pragma unroll
