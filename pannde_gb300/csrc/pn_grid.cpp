@@ -375,7 +375,7 @@ void grid_create(pn_solver *s) {
                        std::max(s->r_cmax, s->r_cmax_s) > std::ldexp(1.0, 90);
   if (s->precision == PN_PREC_F64 && s->d_tmaps && s->r_elo <= s->r_ehi && s->r_elo_s <= s->r_ehi_s && !extreme) {
     const int64_t tiles = (int64_t)(g.nx / (kGridTileX - 1) + 1) * (g.ny / (kGridTileRows - 1) + 1);
-    s->d_rflags = s->alloc<uint8_t>((size_t)(3 * tiles));
+    s->d_rflags = s->alloc<uint32_t>((size_t)(3 * tiles) * sizeof(uint32_t));
     // cumulative block counts [2], then per-step counts [3][2] (unsigned int)
     s->d_pathcnt = s->alloc<unsigned long long>(2 * sizeof(unsigned long long) + 6 * sizeof(unsigned int));
     ck(cudaMemsetAsync(s->d_pathcnt, 0, 2 * sizeof(unsigned long long) + 6 * sizeof(unsigned int), s->stream),
@@ -390,8 +390,9 @@ void grid_reset_range_flags(pn_solver *s) {
   if (!s->d_rflags) return;
   const GridMap &g = s->grid;
   const int64_t tiles = (int64_t)(g.nx / (kGridTileX - 1) + 1) * (g.ny / (kGridTileRows - 1) + 1);
-  ck(cudaMemsetAsync(s->d_rflags, 0, (size_t)(3 * tiles), s->stream), "memset");
-  ck(cudaMemsetAsync(s->d_rflags + (s->step % 3) * tiles, 1, (size_t)tiles, s->stream), "memset");
+  ck(cudaMemsetAsync(s->d_rflags, 0, (size_t)(3 * tiles) * sizeof(uint32_t), s->stream), "memset");
+  ck(cudaMemsetAsync(s->d_rflags + (s->step % 3) * tiles, 0xff, (size_t)tiles * sizeof(uint32_t), s->stream),
+     "memset");  // every bit: every tile on the FP64 path
 }
 
 void grid_split_upload(pn_solver *s) {

@@ -93,7 +93,7 @@ struct pn_solver {
   // stresses, from the magnitudes of the coefficients each is multiplied by
   // (velocities: dt*C*g and g; stresses: dt/rho*g, g and source weights);
   // block counts of the two paths [fp64, df64]
-  uint8_t *d_rflags = nullptr;
+  uint32_t *d_rflags = nullptr;
   int32_t r_elo = 1, r_ehi = 0, r_elo_s = 1, r_ehi_s = 0;
   double r_cmin = 1.0, r_cmax = 1.0, r_cmin_s = 1.0, r_cmax_s = 1.0;
   unsigned long long *d_pathcnt = nullptr;

@@ -83,11 +83,11 @@ struct GridArgs {
   const T *cm_w;
   int32_t test_skip_layer;  // failure-path test: the layer whose copies are never issued (kNoLayer: none)
   int32_t tile_rows;        // rows TY of the 32 x TY block tile (8, or 16 with the tensor-copy kernel)
-  // FP64 form with the tensor-copy kernel: per-tile path flags [3][tiles]
+  // FP64 form with the tensor-copy kernel: per-tile path flag words [3][tiles]
   // (rsg_grid_tma.cuh fp64_path) and the double-float ranges as biased double
   // exponents, [r_elo, r_ehi] for velocities and [r_elo_s, r_ehi_s] for
   // stresses and source terms; rflags null: no path choice (the other forms)
-  uint8_t *rflags;
+  uint32_t *rflags;
   int32_t flag_phase;       // (step of this launch's step 0) % 3
   int32_t r_elo, r_ehi;
   int32_t r_elo_s, r_ehi_s;

@@ -393,14 +393,20 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
   const int rv = ty * G::BWN + on + tx;  // node (i, j) in the node tile
   int waited = k0 - 2;                   // last layer this thread has waited for
   bool fail = false;
-  bool oor = false;  // RANGE: a stored value outside the double-float range
+  // RANGE: where this block stored values outside the double-float range, as
+  // the bits its neighbours read (1 any; 2 / 4 the first / last owned column,
+  // 8 / 16 the first / last owned row -- the edges inside another tile's
+  // boxes: nodes are read at the first column and row, cells at all four)
+  uint32_t oorb = 0;
+  const uint32_t vbits = 1u | (tx == 0 ? 2u : 0u) | (ty == 0 ? 8u : 0u);
+  const uint32_t sbits = vbits | (tx == TX - 2 ? 4u : 0u) | (ty == TY - 2 ? 16u : 0u);
   // a double value into double storage (RANGE: tested against the velocity
   // range, field 0, or the stress range, field 1); generic, so that it is
   // instantiated only where called (double storage)
   auto store_d = [&](auto *p, int64_t i, double d, int field) {
     if constexpr (RANGE)
-      oor = oor || !in_df64_range(d, (uint32_t)(field ? a.r_elo_s : a.r_elo),
-                                  (uint32_t)(field ? a.r_ehi_s : a.r_ehi));
+      if (!in_df64_range(d, (uint32_t)(field ? a.r_elo_s : a.r_elo), (uint32_t)(field ? a.r_ehi_s : a.r_ehi)))
+        oorb |= field ? sbits : vbits;
     p[i] = d;
   };
   auto store = [&](St *p, int64_t i, R v, int field) {
@@ -662,21 +668,24 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
       return;
     }
   }
-  if constexpr (RANGE) {  // a value left the double-float range: the tile's next step runs FP64
-    if (__syncthreads_or(oor) && t == 0) {
+  if constexpr (RANGE) {  // values left the double-float range: mark the tile (and its edges)
+    if (oorb) {
       const int nt = gxc * (a.ny / (TY - 1) + 1);
-      a.rflags[((a.flag_phase + step + 1) % 3) * nt + blk] = 1;
+      atomicOr(a.rflags + ((a.flag_phase + step + 1) % 3) * nt + blk, oorb);
     }
   }
 }
 
 // The FP64 form's path for this block: the FP64 path (the tensor-copy kernel
-// in IEEE double) when its tile or one of the eight around it stored a value
-// outside the double-float range in the previous step, or when one of this
-// step's source terms of its layers lies outside it; the double-float path
-// (df64d) otherwise.  Flags rotate through three per-tile buffers: read
-// (flag_phase + step) % 3, written by this step's blocks (+1), cleared for
-// the step after next by each tile's first chunk (+2).  Block-uniform.
+// in IEEE double) when, in the previous step, its tile stored a value outside
+// the double-float range, or a neighbour tile did so on an edge this tile's
+// boxes read (the neighbour's last cell column for the tile on its right,
+// its first node and cell column for the tile on its left, rows likewise, and
+// a corner for a diagonal neighbour: both edge bits), or when one of this
+// step's source terms of its layers lies outside the range; the double-float
+// path (df64d) otherwise.  Flags rotate through three per-tile words: read
+// (flag_phase + step) % 3, or-ed by this step's blocks (+1), cleared for the
+// step after next by each tile's first chunk (+2).  Block-uniform.
 template <int TY>
 __device__ __forceinline__ bool fp64_path(const GridArgs<double> &a, int bx, int by, int bz, int gxc, int step) {
   constexpr int NT = TX * TY;
@@ -688,8 +697,11 @@ __device__ __forceinline__ bool fp64_path(const GridArgs<double> &a, int bx, int
   if (bx == 0 && by == 0 && bz == 0 && t < 2 && a.step_paths) a.step_paths[((phase + 1) % 3) * 2 + t] = 0u;
   bool f = false;
   if (t < 9) {
-    const int x = bx + t % 3 - 1, y = by + t / 3 - 1;
-    if (x >= 0 && x < gxc && y >= 0 && y < gyc) f = a.rflags[phase * nt + y * gxc + x] != 0;
+    const int dx = t % 3 - 1, dy = t / 3 - 1, x = bx + dx, y = by + dy;
+    if (x >= 0 && x < gxc && y >= 0 && y < gyc) {
+      const uint32_t m = (dx == 0 && dy == 0) ? 1u : ((dx < 0 ? 4u : dx > 0 ? 2u : 0u) | (dy < 0 ? 16u : dy > 0 ? 8u : 0u));
+      f = (a.rflags[phase * nt + y * gxc + x] & m) == m;
+    }
   }
   const int nz = a.nz;
   const int ktop = a.ktop ? min(nz, __ldg(a.ktop + blk)) : nz;

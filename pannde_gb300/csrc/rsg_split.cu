@@ -54,7 +54,7 @@ __device__ __forceinline__ void flag_range(const GridArgs<S> &a, double v, int64
     return;
   const int gxc = a.nx / (kGridTileX - 1) + 1, gyc = a.ny / (a.tile_rows - 1) + 1;
   const int64_t blk = (j / (a.tile_rows - 1)) * gxc + i / (kGridTileX - 1);
-  a.rflags[((a.flag_phase + step + 1) % 3) * (int64_t)gxc * gyc + blk] = 1;
+  atomicOr(a.rflags + ((a.flag_phase + step + 1) % 3) * (int64_t)gxc * gyc + blk, 0x1fu);  // the tile, every edge
 }
 
 template <typename S>
