@@ -376,10 +376,8 @@ void grid_create(pn_solver *s) {
   if (s->precision == PN_PREC_F64 && s->d_tmaps && s->r_elo <= s->r_ehi && s->r_elo_s <= s->r_ehi_s && !extreme) {
     const int64_t tiles = (int64_t)(g.nx / (kGridTileX - 1) + 1) * (g.ny / (kGridTileRows - 1) + 1);
     s->d_rflags = s->alloc<uint32_t>((size_t)(3 * tiles) * sizeof(uint32_t));
-    // cumulative block counts [2], then per-step counts [3][2] (unsigned int)
-    s->d_pathcnt = s->alloc<unsigned long long>(2 * sizeof(unsigned long long) + 6 * sizeof(unsigned int));
-    ck(cudaMemsetAsync(s->d_pathcnt, 0, 2 * sizeof(unsigned long long) + 6 * sizeof(unsigned int), s->stream),
-       "memset");
+    s->d_pathcnt = s->alloc<unsigned long long>(2 * sizeof(unsigned long long));
+    ck(cudaMemsetAsync(s->d_pathcnt, 0, 2 * sizeof(unsigned long long), s->stream), "memset");
     grid_reset_range_flags(s);
   }
   grid_split_upload(s);
@@ -698,7 +696,6 @@ void grid_args(pn_solver *s, GridArgs<T> &a) {
   a.r_elo_s = s->r_elo_s;
   a.r_ehi_s = s->r_ehi_s;
   a.path_count = s->d_pathcnt;
-  a.step_paths = s->d_pathcnt ? reinterpret_cast<unsigned int *>(s->d_pathcnt + 2) : nullptr;
 }
 
 const void *grid_maps_for(const pn_solver *s, int in) {

@@ -92,7 +92,6 @@ struct GridArgs {
   int32_t r_elo, r_ehi;
   int32_t r_elo_s, r_ehi_s;
   unsigned long long *path_count;  // [2] blocks that took the FP64 / double-float path, or null
-  unsigned int *step_paths;        // [3][2] the same per step, rotating like rflags, or null
 };
 
 constexpr int32_t kNoLayer = INT32_MIN;  // no layer index (layers run from -1 to nz)

@@ -152,16 +152,20 @@ template <> struct GNum<df64> {
 #ifndef PN_F64H_JOIN_INT
 #define PN_F64H_JOIN_INT 1
 #endif
-// The path's increments onto the stored doubles: by the pair's exact halves
-// and two FP64 adds (add_pair: fewer instructions, two FP64-pipe operations),
-// or by one join on the integer pipe and one FP64 add.  Measured on the
-// laminate: with no FP64-path blocks (a developed state) the two adds are
-// faster (0.495 against 0.531 ms per step), with 15% of the blocks on the
-// FP64 path (the burst's first steps), whose FP64 pipe is then busy, the
-// join (0.571 against 0.600 ms).  Each step takes the two adds while fewer
-// than 1/16 of the previous step's blocks took the FP64 path.
-__device__ __forceinline__ double add_increment(double base, df64 inc, bool pair) {
-  if (pair) return add_pair(base, inc);
+// The path's increments onto the stored doubles: PN_F64H_ADD_PAIR 1 by the
+// pair's exact halves and two FP64 adds (add_pair: fewer instructions, two
+// FP64-pipe operations), 0 by one join on the integer pipe and one FP64 add.
+// Measured on the laminate: with no FP64-path blocks (a developed state) the
+// two adds are faster (0.495 against 0.531 ms per step), with 15% of the
+// blocks on the FP64 path (the burst's first steps), whose FP64 pipe is then
+// busy, the join (0.571 against 0.600 ms).  Choosing per step from the
+// previous step's path counts was slower than either (0.584 / 0.544 ms): the
+// kernel then carries both.
+#ifndef PN_F64H_ADD_PAIR
+#define PN_F64H_ADD_PAIR 1
+#endif
+__device__ __forceinline__ double add_increment(double base, df64 inc) {
+  if (PN_F64H_ADD_PAIR) return add_pair(base, inc);
   return __dadd_rn(base, PN_F64H_JOIN_INT ? join_double_int(inc) : join_double(inc));
 }
 template <> struct GNum<df64d> {
@@ -256,11 +260,9 @@ constexpr int32_t kErrWait = 1;
 // RANGE (the FP64 form's kernel): every V and S value the block stores is
 // tested against the double-float range, and a block that stored one outside
 // it marks its tile for the FP64 path in the next step (range_flags_write).
-// pair_add (split storage): how increments reach the stored doubles (add_increment)
 template <typename K, int SYM, int TY, bool BATCH = false, bool RANGE = false>
 __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::S> &a, const GridMaps *M,
-                                               int bx, int by, int bz, int gxc, int step,
-                                               bool pair_add = true) {
+                                               int bx, int by, int bz, int gxc, int step) {
   using N = GNum<K>;
   using R = typename N::R;
   using St = typename N::S;
@@ -508,7 +510,7 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
           const R acc3[3] = {ax, ay, az};
 #pragma unroll
           for (int c = 0; c < 3; c++) {
-            vd[c] = add_increment((double)Vk[c * VB + rv], cf * acc3[c], pair_add);
+            vd[c] = add_increment((double)Vk[c * VB + rv], cf * acc3[c]);
             vn[c] = split_double(vd[c]);
           }
         } else {
@@ -632,7 +634,7 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
               if (c_used(cls, kk, jj)) acc[kk] = madd(N::tval(Cm[6 * kk + jj]), e[jj], acc[kk]);
           }
           if constexpr (N::SPLIT)
-            store_d(a.S_out[kk], cg, add_increment(__ldg(a.S_in[kk] + cg), acc[kk], pair_add), 1);
+            store_d(a.S_out[kk], cg, add_increment(__ldg(a.S_in[kk] + cg), acc[kk]), 1);
           else store(a.S_out[kk], cg, acc[kk], 1);
         };
         if (ortho) {
@@ -694,7 +696,6 @@ __device__ __forceinline__ bool fp64_path(const GridArgs<double> &a, int bx, int
   const int blk = by * gxc + bx;
   const int phase = (a.flag_phase + step) % 3;
   if (bz == 0 && t == 0) a.rflags[((phase + 2) % 3) * nt + blk] = 0;
-  if (bx == 0 && by == 0 && bz == 0 && t < 2 && a.step_paths) a.step_paths[((phase + 1) % 3) * 2 + t] = 0u;
   bool f = false;
   if (t < 9) {
     const int dx = t % 3 - 1, dy = t / 3 - 1, x = bx + dx, y = by + dy;
@@ -737,8 +738,8 @@ __device__ __forceinline__ bool fp64_path(const GridArgs<double> &a, int bx, int
 #endif
 template <typename K, int SYM, bool BATCH>
 __device__ __forceinline__ void f64h_path(const GridArgs<double> &a, const GridMaps *M, int bx, int by, int bz,
-                                          int gxc, int step, bool pair_add = true) {
-  grid_block_tma<K, SYM, 8, BATCH, true>(a, M, bx, by, bz, gxc, step, pair_add);
+                                          int gxc, int step) {
+  grid_block_tma<K, SYM, 8, BATCH, true>(a, M, bx, by, bz, gxc, step);
 }
 
 template <int SYM, bool BATCH, int MODE>
@@ -746,22 +747,14 @@ __device__ __forceinline__ void f64h_block(const GridArgs<double> &a, int bx, in
   const GridMaps *M = reinterpret_cast<const GridMaps *>(a.tmaps);
   const bool fp64 = fp64_path<8>(a, bx, by, bz, gxc, step);
   if ((MODE == 1 && fp64) || (MODE == 2 && !fp64)) return;
-  const int phase = (a.flag_phase + step) % 3;
   if (threadIdx.x == 0 && a.path_count) atomicAdd(a.path_count + (fp64 ? 0 : 1), 1ull);
-  if (threadIdx.x == 0 && a.step_paths) atomicAdd(a.step_paths + phase * 2 + (fp64 ? 0 : 1), 1u);
-  // the previous step's path counts (complete: that launch has finished)
-  bool pair_add = true;
-  if (a.step_paths) {
-    const unsigned f = a.step_paths[((phase + 2) % 3) * 2], d = a.step_paths[((phase + 2) % 3) * 2 + 1];
-    pair_add = 16u * f < f + d;
-  }
   if constexpr (MODE != 1) {
     if (fp64) {
       f64h_path<double, SYM, BATCH>(a, M, bx, by, bz, gxc, step);
       return;
     }
   }
-  if constexpr (MODE != 2) f64h_path<df64d, SYM, BATCH>(a, M, bx, by, bz, gxc, step, pair_add);
+  if constexpr (MODE != 2) f64h_path<df64d, SYM, BATCH>(a, M, bx, by, bz, gxc, step);
 }
 
 // resident blocks per SM the FP64 form's kernel is compiled for (its register
