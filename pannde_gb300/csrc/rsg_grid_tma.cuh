@@ -160,9 +160,11 @@ template <> struct GNum<df64> {
 // blocks on the FP64 path (the burst's first steps), whose FP64 pipe is then
 // busy, the join (0.571 against 0.600 ms).  Choosing per step from the
 // previous step's path counts was slower than either (0.584 / 0.544 ms): the
-// kernel then carries both.
+// kernel then carries both.  With edge-aware path flags (fewer FP64 blocks)
+// the join measured 0.529 / 0.531 ms against 0.588 / 0.528: the join is the
+// default.
 #ifndef PN_F64H_ADD_PAIR
-#define PN_F64H_ADD_PAIR 1
+#define PN_F64H_ADD_PAIR 0
 #endif
 __device__ __forceinline__ double add_increment(double base, df64 inc) {
   if (PN_F64H_ADD_PAIR) return add_pair(base, inc);
