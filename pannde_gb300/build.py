@@ -53,7 +53,9 @@ def _jobs() -> list[tuple[list[str], Path]]:
     cuda = _cuda_home()
     nvcc = str(cuda / "bin" / "nvcc")
     inc = ["-I", str(CSRC), "-I", str(HERE.parent / "include")]
-    common_cu = [nvcc, "-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC", *inc]
+    # PN_BUILD_DEFINES: extra -D switches for the CUDA units (tuning sweeps)
+    defs = [f"-D{d}" for d in os.environ.get("PN_BUILD_DEFINES", "").split()]
+    common_cu = [nvcc, "-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC", *defs, *inc]
     cxx = os.environ.get("CXX", "g++")
     common_cc = [cxx, "-std=c++17", "-O2", "-fPIC", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
                  "-I", str(cuda / "include"), *inc]

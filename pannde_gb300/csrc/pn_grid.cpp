@@ -98,8 +98,13 @@ struct Keyed {
   double w;
 };
 
+// entries sorted by (slot, local index), stably: a thread finds its own
+// entries of a slot by a binary search (first_local), and one node's entries
+// keep their order (the order their terms are added in)
 void ranges_of(std::vector<Keyed> &L, int64_t n_slots, std::vector<int32_t> &rng) {
-  std::stable_sort(L.begin(), L.end(), [](const Keyed &a, const Keyed &b) { return a.slot < b.slot; });
+  std::stable_sort(L.begin(), L.end(), [](const Keyed &a, const Keyed &b) {
+    return a.slot != b.slot ? a.slot < b.slot : (a.key & 0xffff) < (b.key & 0xffff);
+  });
   rng.assign((size_t)n_slots * 2, 0);
   size_t e = 0;
   for (int64_t sl = 0; sl < n_slots; sl++) {

@@ -195,9 +195,12 @@ __device__ __forceinline__ void grid_block(const GridArgs<typename GNum<R>::S> &
       if (do_vel) {
       if (a.f_rng) {  // force sources of this block and layer
         const int2 r = a.f_rng[(int64_t)blk * (nz + 1) + k];
-        for (int e = r.x; e < r.y; e++) {
+        for (int e = first_local(a.f_key, r.x, r.y, t); e < r.y; e++) {
           const int key = a.f_key[e];
-          if ((key & 0xffff) != t) continue;
+          if ((key & 0xffff) != t) {
+            if ((key & 0xffff) > t) break;
+            continue;
+          }
           const R v = N::val(a.f_w[e]) * N::val(sigrow[a.f_sig[e]]);
           const int d = key >> 16;
           if (d == 0) ax = ax + v;
@@ -219,8 +222,11 @@ __device__ __forceinline__ void grid_block(const GridArgs<typename GNum<R>::S> &
         for (int c = 0; c < 3; c++) N::st(a.V_out[c], n, vn[c]);
         if (a.s_rng && rec < a.rec_cap) {  // sensor traces
           const int2 r = a.s_rng[(int64_t)blk * (nz + 1) + k];
-          for (int e = r.x; e < r.y; e++) {
-            if (a.s_key[e] != t) continue;
+          for (int e = first_local(a.s_key, r.x, r.y, t); e < r.y; e++) {
+            if (a.s_key[e] != t) {
+              if (a.s_key[e] > t) break;
+              continue;
+            }
             double *tr = a.traces + (rec * a.n_sens + a.s_idx[e]) * 3;
             tr[0] = N::dbl(vn[0]);
             tr[1] = N::dbl(vn[1]);
@@ -267,9 +273,12 @@ __device__ __forceinline__ void grid_block(const GridArgs<typename GNum<R>::S> &
         for (int f = 0; f < 6; f++) acc[f] = N::val(Sprev[f * CT + q]);
         if (a.m_rng) {  // moment sources of this block and cell layer
           const int2 r = a.m_rng[(int64_t)blk * nz + kc];
-          for (int ee = r.x; ee < r.y; ee++) {
+          for (int ee = first_local(a.m_key, r.x, r.y, t); ee < r.y; ee++) {
             const int key = a.m_key[ee];
-            if ((key & 0xffff) != t) continue;
+            if ((key & 0xffff) != t) {
+              if ((key & 0xffff) > t) break;
+              continue;
+            }
             const R v = N::val(a.m_w[ee]) * N::val(sigrow[a.m_sig[ee]]);
             const int kk = key >> 16;
 #pragma unroll
@@ -411,6 +420,41 @@ int grid_chunk_for(int nz, long long xy_blocks, int sms, int per_sm) {
   chunks = std::max(1LL, std::min(chunks, (long long)std::max(1, nz / 4)));
   chunks = std::max(chunks, (long long)((nz + kGridChunkMax - 1) / kGridChunkMax));
   return (int)((nz + chunks - 1) / chunks);
+}
+
+// The blocks of a one-chunk launch run in waves of `slots`; whole columns in
+// the last, partial wave keep the GPU as busy as that wave is full (on the
+// 400 x 400 x 40 laminate, FP32: 608 columns over 77 us, then the other 146
+// alone for 50 us more).  The tiles of that wave get their columns cut into c
+// chunks, the c of least modelled time: full waves x (nz + o) + waves of the
+// tail's R c chunks x (nz / c + o), o = 4 layers of a block's fixed cost
+// (start-up, the re-marched layers at each cut).
+void grid_tail_split(int nz, int kchunk, long long tiles, long long slots, int &tail_from, int &tail_chunk) {
+  tail_from = 0;
+  tail_chunk = 0;
+  if (nz <= 1 || kchunk < nz || slots <= 0 || tiles <= slots) return;
+  const long long full = tiles / slots * slots, rest = tiles - full;
+  if (rest == 0) return;
+  int best = 1;
+  if (const char *v = std::getenv("PN_GRID_TAIL_CHUNKS")) {
+    best = std::max(1, std::min(std::atoi(v), nz));
+  } else {
+    constexpr double o = 4.0;
+    double best_t = 0.0;
+    for (int c = 1; c <= std::min(8, nz); c++) {
+      const int len = (nz + c - 1) / c;
+      const int cc = (nz + len - 1) / len;
+      const double waves = (double)((rest * cc + slots - 1) / slots);
+      const double t = waves * (len + o);
+      if (c == 1 || t < best_t - 1e-9) {
+        best_t = t;
+        best = c;
+      }
+    }
+  }
+  if (best <= 1) return;
+  tail_from = (int)full;
+  tail_chunk = (nz + best - 1) / best;
 }
 
 int grid_chunk_layers(int precision, int nx, int ny, int nz, bool tma, int tile_rows) {

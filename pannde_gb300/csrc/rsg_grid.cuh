@@ -92,11 +92,40 @@ struct GridArgs {
   int32_t r_elo, r_ehi;
   int32_t r_elo_s, r_ehi_s;
   unsigned long long *path_count;  // [2] blocks that took the FP64 / double-float path, or null
+  // tail split (tensor-copy kernel, one launch per solver; set by the launcher):
+  // tail_chunk > 0 runs a 1D grid whose first tail_from blocks are the first
+  // tail_from tiles' whole columns and whose others cut each remaining tile's
+  // column into chunks of tail_chunk layers, chunk-major (the last partial wave
+  // of whole columns would leave most SMs idle); 0: the 3D grid of kchunk chunks
+  int32_t tail_from, tail_chunk;
 };
+
+// where a thread's scan of its (block, layer) slot starts: the entries are
+// sorted by local index (key & 0xffff), so in a long slot (a transducer patch
+// puts a few hundred entries in one) a binary search finds the first entry of
+// local index t, or the first past them, in log2(hi - lo) loads; a short slot
+// is scanned from its start.  The scan skips entries of smaller local index
+// and stops at the first larger one.
+#ifdef __CUDACC__
+__device__ __forceinline__ int first_local(const int32_t *__restrict__ key, int lo, int hi, int t) {
+  if (hi - lo <= 32) return lo;  // a short slot: scanned from its start (independent loads)
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if ((__ldg(key + mid) & 0xffff) < t) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+#endif
 
 constexpr int32_t kNoLayer = INT32_MIN;  // no layer index (layers run from -1 to nz)
 
 constexpr int kGridChunkMax = 64;     // cell layers per z chunk, at most
+
+// tail split of a one-chunk launch (GridArgs::tail_from / tail_chunk) for
+// `tiles` tile columns of nz layers on `slots` resident blocks; tail_chunk 0:
+// none.  PN_GRID_TAIL_CHUNKS overrides the chunks per tail column (1: none).
+void grid_tail_split(int nz, int kchunk, long long tiles, long long slots, int &tail_from, int &tail_chunk);
 constexpr int kGridTmaRowsMax = 32;   // stiffness rows the tensor-copy kernel stages
 
 // block tiles: 32 x TY threads, one warp per row; TY = 8 everywhere, 16 as

@@ -64,11 +64,17 @@ struct GridMaps {
 // block per SM with 8-byte storage).  Slots per ring: stress PD + 1 (+ 2 with
 // OWN_SMEM), velocity + dt/rho PD + 1, material PD + 3 (read in the stress
 // half, two iterations after its layer's).
+#ifndef PN_GRID_F32_OWN_STRESS
+#define PN_GRID_F32_OWN_STRESS 1  // FP32: old stress from the tile (four stress slots)
+#endif
+#ifndef PN_GRID_F32_MIN_BLOCKS
+#define PN_GRID_F32_MIN_BLOCKS 0  // FP32: resident blocks per SM the kernel is compiled for
+#endif
 template <int ESZ, int TY>
 struct Geo {
   static constexpr int NT = TX * TY;
   static constexpr int PD = 1;
-  static constexpr bool OWN_SMEM = ESZ == 4;
+  static constexpr bool OWN_SMEM = ESZ == 4 && PN_GRID_F32_OWN_STRESS;
   static constexpr int NS = PD + 1 + (OWN_SMEM ? 2 : 0);
   static constexpr int NV = PD + 1;
   static constexpr int NM = PD + 3;
@@ -264,7 +270,7 @@ constexpr int32_t kErrWait = 1;
 // it marks its tile for the FP64 path in the next step (range_flags_write).
 template <typename K, int SYM, int TY, bool BATCH = false, bool RANGE = false>
 __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::S> &a, const GridMaps *M,
-                                               int bx, int by, int bz, int gxc, int step) {
+                                               int bx, int by, int k0, int kc, int gxc, int step) {
   using N = GNum<K>;
   using R = typename N::R;
   using St = typename N::S;
@@ -310,7 +316,7 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
   // columns of the tile (and its apron) hold no solid cell at or above ktop:
   // the march ends there, and a chunk above it has nothing to do
   const int ktop = a.ktop ? min(nz, __ldg(a.ktop + blk)) : nz;
-  const int k0 = bz * a.kchunk, k1 = min(ktop, k0 + a.kchunk);
+  const int k1 = min(ktop, k0 + kc);
   if (k0 >= ktop) return;
   const bool last_chunk = k1 == ktop;
 
@@ -489,9 +495,14 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
         ay = ay + bly;
         az = az + blz;
         const int2 fr = sRf[k - k0 + 1];
-        for (int e = fr.x; e < fr.y; e++) {  // force sources of this block and layer
+        // this node's force sources (the batch kernel scans its slots whole:
+        // the searches cost it registers for a fourth block per SM)
+        for (int e = BATCH ? fr.x : first_local(a.f_key, fr.x, fr.y, t); e < fr.y; e++) {
           const int key = __ldg(a.f_key + e);
-          if ((key & 0xffff) != t) continue;
+          if ((key & 0xffff) != t) {
+            if (!BATCH && (key & 0xffff) > t) break;
+            continue;
+          }
           const R w = N::val(a.f_w[e]), sg = N::val(sigrow[__ldg(a.f_sig + e)]);
           const int d = key >> 16;
           if (d == 0) ax = madd(w, sg, ax);
@@ -541,8 +552,12 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
           }
           const int2 sr = sRs[k - k0 + 1];
           if (rec < a.rec_cap) {
-            for (int e = sr.x; e < sr.y; e++) {  // sensor traces
-              if (__ldg(a.s_key + e) != t) continue;
+            for (int e = BATCH ? sr.x : first_local(a.s_key, sr.x, sr.y, t); e < sr.y; e++) {  // sensor traces
+              const int lk = __ldg(a.s_key + e);
+              if (lk != t) {
+                if (!BATCH && lk > t) break;
+                continue;
+              }
               double *tr = a.traces + (rec * a.n_sens + __ldg(a.s_idx + e)) * 3;
               tr[0] = out(0);
               tr[1] = out(1);
@@ -606,9 +621,12 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
           for (int f = 0; f < 6; f++) acc[f] = N::ld(a.S_in[f], cg);
         }
         const int2 mr = sRm[kc - k0];
-        for (int ee = mr.x; ee < mr.y; ee++) {  // moment sources of this block and cell layer
+        for (int ee = BATCH ? mr.x : first_local(a.m_key, mr.x, mr.y, t); ee < mr.y; ee++) {  // this cell's moments
           const int key = __ldg(a.m_key + ee);
-          if ((key & 0xffff) != t) continue;
+          if ((key & 0xffff) != t) {
+            if (!BATCH && (key & 0xffff) > t) break;
+            continue;
+          }
           const R w = N::val(a.m_w[ee]), sg = N::val(sigrow[__ldg(a.m_sig + ee)]);
           const int kk = key >> 16;
 #pragma unroll
@@ -691,13 +709,14 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
 // (flag_phase + step) % 3, or-ed by this step's blocks (+1), cleared for the
 // step after next by each tile's first chunk (+2).  Block-uniform.
 template <int TY>
-__device__ __forceinline__ bool fp64_path(const GridArgs<double> &a, int bx, int by, int bz, int gxc, int step) {
+__device__ __forceinline__ bool fp64_path(const GridArgs<double> &a, int bx, int by, int k0, int kc, int gxc,
+                                          int step) {
   constexpr int NT = TX * TY;
   const int t = threadIdx.x;
   const int gyc = a.ny / (TY - 1) + 1, nt = gxc * gyc;
   const int blk = by * gxc + bx;
   const int phase = (a.flag_phase + step) % 3;
-  if (bz == 0 && t == 0) a.rflags[((phase + 2) % 3) * nt + blk] = 0;
+  if (k0 == 0 && t == 0) a.rflags[((phase + 2) % 3) * nt + blk] = 0;
   bool f = false;
   if (t < 9) {
     const int dx = t % 3 - 1, dy = t / 3 - 1, x = bx + dx, y = by + dy;
@@ -708,7 +727,7 @@ __device__ __forceinline__ bool fp64_path(const GridArgs<double> &a, int bx, int
   }
   const int nz = a.nz;
   const int ktop = a.ktop ? min(nz, __ldg(a.ktop + blk)) : nz;
-  const int k0 = bz * a.kchunk, k1 = min(ktop, k0 + a.kchunk);
+  const int k1 = min(ktop, k0 + kc);
   if (k0 < ktop && a.sigval) {
     const double *sigrow = a.sigval + (int64_t)min(step, a.sig_rows - 1) * a.sig_stride;
     const uint32_t lo = (uint32_t)a.r_elo_s, hi = (uint32_t)a.r_ehi_s;
@@ -727,6 +746,36 @@ __device__ __forceinline__ bool fp64_path(const GridArgs<double> &a, int bx, int
   return __syncthreads_or(f) != 0;
 }
 
+// tile (bx, by) and layer range [k0, k0 + kc) of this block of a single
+// solver's launch: the 3D grid (x, y, chunk of kchunk layers), or with a
+// tail split (tail_chunk > 0) the 1D grid of whole columns, then the
+// remaining tiles' chunks of tail_chunk layers, chunk-major
+template <int TY, typename T>
+__device__ __forceinline__ void block_coords(const GridArgs<T> &a, int &bx, int &by, int &k0, int &kc, int &gxc) {
+  gxc = a.nx / (TX - 1) + 1;
+  if (a.tail_chunk > 0) {
+    const int id = blockIdx.x, tiles = gxc * (a.ny / (TY - 1) + 1);
+    int tile;
+    if (id < a.tail_from) {
+      tile = id;
+      k0 = 0;
+      kc = a.kchunk;
+    } else {
+      const int rest = tiles - a.tail_from, j = id - a.tail_from;
+      tile = a.tail_from + j % rest;
+      k0 = (j / rest) * a.tail_chunk;
+      kc = a.tail_chunk;
+    }
+    bx = tile % gxc;
+    by = tile / gxc;
+  } else {
+    bx = blockIdx.x;
+    by = blockIdx.y;
+    k0 = blockIdx.z * a.kchunk;
+    kc = a.kchunk;
+  }
+}
+
 // The FP64 form's kernels: MODE 0 runs each block on its path; with the two
 // paths as two launches (PN_F64H_TWO_LAUNCHES), MODE 1 runs the double-float
 // blocks and MODE 2 the FP64 ones (the other blocks return at once), so each
@@ -739,24 +788,25 @@ __device__ __forceinline__ bool fp64_path(const GridArgs<double> &a, int bx, int
 #define PN_F64H_TWO_LAUNCHES 0
 #endif
 template <typename K, int SYM, bool BATCH>
-__device__ __forceinline__ void f64h_path(const GridArgs<double> &a, const GridMaps *M, int bx, int by, int bz,
-                                          int gxc, int step) {
-  grid_block_tma<K, SYM, 8, BATCH, true>(a, M, bx, by, bz, gxc, step);
+__device__ __forceinline__ void f64h_path(const GridArgs<double> &a, const GridMaps *M, int bx, int by, int k0,
+                                          int kc, int gxc, int step) {
+  grid_block_tma<K, SYM, 8, BATCH, true>(a, M, bx, by, k0, kc, gxc, step);
 }
 
 template <int SYM, bool BATCH, int MODE>
-__device__ __forceinline__ void f64h_block(const GridArgs<double> &a, int bx, int by, int bz, int gxc, int step) {
+__device__ __forceinline__ void f64h_block(const GridArgs<double> &a, int bx, int by, int k0, int kc, int gxc,
+                                           int step) {
   const GridMaps *M = reinterpret_cast<const GridMaps *>(a.tmaps);
-  const bool fp64 = fp64_path<8>(a, bx, by, bz, gxc, step);
+  const bool fp64 = fp64_path<8>(a, bx, by, k0, kc, gxc, step);
   if ((MODE == 1 && fp64) || (MODE == 2 && !fp64)) return;
   if (threadIdx.x == 0 && a.path_count) atomicAdd(a.path_count + (fp64 ? 0 : 1), 1ull);
   if constexpr (MODE != 1) {
     if (fp64) {
-      f64h_path<double, SYM, BATCH>(a, M, bx, by, bz, gxc, step);
+      f64h_path<double, SYM, BATCH>(a, M, bx, by, k0, kc, gxc, step);
       return;
     }
   }
-  if constexpr (MODE != 2) f64h_path<df64d, SYM, BATCH>(a, M, bx, by, bz, gxc, step);
+  if constexpr (MODE != 2) f64h_path<df64d, SYM, BATCH>(a, M, bx, by, k0, kc, gxc, step);
 }
 
 // resident blocks per SM the FP64 form's kernel is compiled for (its register
@@ -768,7 +818,9 @@ __device__ __forceinline__ void f64h_block(const GridArgs<double> &a, int bx, in
 template <int SYM, int MODE>
 __global__ void __launch_bounds__(TX * 8, PN_F64H_MIN_BLOCKS)
     k_grid_tma_f64h(const __grid_constant__ GridArgs<double> a, int step) {
-  f64h_block<SYM, false, MODE>(a, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x, step);
+  int bx, by, k0, kc, gxc;
+  block_coords<8>(a, bx, by, k0, kc, gxc);
+  f64h_block<SYM, false, MODE>(a, bx, by, k0, kc, gxc, step);
 }
 
 template <int SYM, int MODE>
@@ -785,7 +837,8 @@ __global__ void __launch_bounds__(TX * 8, PN_F64H_MIN_BLOCKS)
   const GridArgs<double> &a = args[lo];
   const int local = id - __ldg(block_start + lo);
   const int gxc = a.nx / (TX - 1) + 1, gyc = a.ny / 7 + 1;
-  f64h_block<SYM, true, MODE>(a, local % gxc, (local / gxc) % gyc, local / (gxc * gyc), gxc, step);
+  f64h_block<SYM, true, MODE>(a, local % gxc, (local / gxc) % gyc, local / (gxc * gyc) * a.kchunk, a.kchunk, gxc,
+                              step);
 }
 
 // minimum blocks per SM each storage type is compiled for (the register cap
@@ -794,13 +847,15 @@ __global__ void __launch_bounds__(TX * 8, PN_F64H_MIN_BLOCKS)
 // cap of 4 blocks measured 6% slower)
 // (32 x 16 tiles with 8-byte storage: shared memory holds one block per SM)
 template <typename R, int TY> struct GMinBlocks { static constexpr int v = TY == 8 ? 3 : 1; };
-template <int TY> struct GMinBlocks<float, TY> { static constexpr int v = 0; };
+template <int TY> struct GMinBlocks<float, TY> { static constexpr int v = PN_GRID_F32_MIN_BLOCKS; };
 
 template <typename R, int SYM, int TY>
 __global__ void __launch_bounds__(TX *TY, GMinBlocks<R, TY>::v)
     k_grid_tma(const GridArgs<typename GNum<R>::S> a, int step) {
   const GridMaps *M = reinterpret_cast<const GridMaps *>(a.tmaps);
-  grid_block_tma<R, SYM, TY>(a, M, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x, step);
+  int bx, by, k0, kc, gxc;
+  block_coords<TY>(a, bx, by, k0, kc, gxc);
+  grid_block_tma<R, SYM, TY>(a, M, bx, by, k0, kc, gxc, step);
 }
 
 template <typename R, int SYM, int TY>
@@ -818,7 +873,8 @@ __global__ void __launch_bounds__(TX *TY, GMinBlocks<R, TY>::v)
   const GridMaps *M = reinterpret_cast<const GridMaps *>(a.tmaps);
   const int local = id - __ldg(block_start + lo);
   const int gxc = a.nx / (TX - 1) + 1, gyc = a.ny / (TY - 1) + 1;
-  grid_block_tma<R, SYM, TY, true>(a, M, local % gxc, (local / gxc) % gyc, local / (gxc * gyc), gxc, step);
+  grid_block_tma<R, SYM, TY, true>(a, M, local % gxc, (local / gxc) % gyc, local / (gxc * gyc) * a.kchunk, a.kchunk,
+                                   gxc, step);
 }
 
 template <typename R, int SYM, int TY>
@@ -850,6 +906,21 @@ struct SetupT {
   }
 };
 
+// grid of a single solver's launch: chunks (kchunk, when the caller left it
+// 0) and the tail split; grid.x == 0: a chunk longer than the kernel stages
+template <int TY, typename T>
+dim3 single_grid(GridArgs<T> &b, int sms, int per_sm) {
+  const unsigned gx = (unsigned)(b.nx / (TX - 1) + 1), gy = (unsigned)(b.ny / (TY - 1) + 1);
+  if (b.kchunk <= 0) b.kchunk = grid_chunk_for(b.nz, (long long)gx * gy, sms, per_sm);
+  if (b.kchunk > KC_MAX) return dim3(0, 1, 1);
+  grid_tail_split(b.nz, b.kchunk, (long long)gx * gy, (long long)sms * per_sm, b.tail_from, b.tail_chunk);
+  if (b.tail_chunk > 0) {
+    const long long tiles = (long long)gx * gy, cuts = (b.nz + b.tail_chunk - 1) / b.tail_chunk;
+    return dim3((unsigned)(b.tail_from + (tiles - b.tail_from) * cuts), 1, 1);
+  }
+  return dim3(gx, gy, (unsigned)((b.nz + b.kchunk - 1) / b.kchunk));
+}
+
 template <typename R, int SYM, int TY>
 cudaError_t launch_t(const GridArgs<typename GNum<R>::S> &a, cudaStream_t st) {
   using S = SetupT<R, SYM, TY>;
@@ -857,10 +928,8 @@ cudaError_t launch_t(const GridArgs<typename GNum<R>::S> &a, cudaStream_t st) {
   cudaError_t e = S::ensure(sms, per_sm);
   if (e != cudaSuccess) return e;
   GridArgs<typename GNum<R>::S> b = a;
-  const unsigned gx = (unsigned)(a.nx / (TX - 1) + 1), gy = (unsigned)(a.ny / (TY - 1) + 1);
-  if (b.kchunk <= 0) b.kchunk = grid_chunk_for(a.nz, (long long)gx * gy, sms, per_sm);
-  if (b.kchunk > KC_MAX) return cudaErrorInvalidValue;
-  const dim3 grid(gx, gy, (unsigned)((a.nz + b.kchunk - 1) / b.kchunk));
+  const dim3 grid = single_grid<TY>(b, sms, per_sm);
+  if (grid.x == 0) return cudaErrorInvalidValue;
   k_grid_tma<R, SYM, TY><<<grid, TX * TY, S::smem, st>>>(b, 0);
   return cudaGetLastError();
 }
@@ -913,10 +982,8 @@ cudaError_t launch_h(const GridArgs<double> &a, cudaStream_t st) {
   cudaError_t e = SetupT<double, SYM, 8>::ensure(sms, per_sm);
   if (e != cudaSuccess) return e;
   GridArgs<double> b = a;
-  const unsigned gx = (unsigned)(a.nx / (TX - 1) + 1), gy = (unsigned)(a.ny / 7 + 1);
-  if (b.kchunk <= 0) b.kchunk = grid_chunk_for(a.nz, (long long)gx * gy, sms, per_sm);
-  if (b.kchunk > KC_MAX) return cudaErrorInvalidValue;
-  const dim3 grid(gx, gy, (unsigned)((a.nz + b.kchunk - 1) / b.kchunk));
+  const dim3 grid = single_grid<8>(b, sms, per_sm);
+  if (grid.x == 0) return cudaErrorInvalidValue;
   if constexpr (PN_F64H_TWO_LAUNCHES != 0) {
     e = launch_h_mode<SYM, 1>(b, grid, st);
     return e == cudaSuccess ? launch_h_mode<SYM, 2>(b, grid, st) : e;
