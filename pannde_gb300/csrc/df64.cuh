@@ -130,6 +130,54 @@ template <typename T> __device__ __forceinline__ void diffsum22(T a, T b, T c, T
   sum = ab + cd;
 }
 
+// The stencil's pair differences kept unnormalised (lo not yet bounded by
+// ulp(hi) / 2) until the add that consumes them renormalises anyway (3 flops
+// fewer per value); Lazy<T> is T itself for the native types.
+template <typename T> struct Lazy { using type = T; };
+template <> struct Lazy<df64> { using type = df64_unnorm; };
+__device__ __forceinline__ df64_unnorm sub_unnorm(df64_unnorm a, df64_unnorm b) {
+  const df64 s = two_sum(a.hi, -b.hi);
+  return {s.hi, __fadd_rn(s.lo, __fsub_rn(a.lo, b.lo))};
+}
+__device__ __forceinline__ df64_unnorm add_unnorm(df64_unnorm a, df64_unnorm b) {
+  const df64 s = two_sum(a.hi, b.hi);
+  return {s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo))};
+}
+__device__ __forceinline__ df64_unnorm diff22_u(df64 b, df64 c, df64 a, df64 d) {
+  return sub_unnorm(add_lazy(b, c), add_lazy(a, d));
+}
+__device__ __forceinline__ df64_unnorm sum22_u(df64 a, df64 b, df64 c, df64 d) {
+  return add_unnorm(add_lazy(a, b), add_lazy(c, d));
+}
+__device__ __forceinline__ void diffsum22_u(df64 a, df64 b, df64 c, df64 d, df64_unnorm &diff, df64_unnorm &sum) {
+  const df64_unnorm ab = add_lazy(a, b), cd = add_lazy(c, d);
+  diff = sub_unnorm(cd, ab);
+  sum = add_unnorm(ab, cd);
+}
+__device__ __forceinline__ void diffdiff22_u(df64 a, df64 b, df64 c, df64 d, df64_unnorm &dx, df64_unnorm &dy) {
+  const df64_unnorm u = sub_lazy(c, a), w = sub_lazy(b, d);
+  dx = add_unnorm(u, w);
+  dy = sub_unnorm(u, w);
+}
+__device__ __forceinline__ df64 add_uu(df64_unnorm a, df64_unnorm b) { return add_norm(a, b); }
+__device__ __forceinline__ df64 sub_uu(df64_unnorm a, df64_unnorm b) { return sub_norm(a, b); }
+__device__ __forceinline__ df64_unnorm to_u(df64 a) { return {a.hi, a.lo}; }
+__device__ __forceinline__ df64 norm_u(df64_unnorm a) { return quick_two_sum(a.hi, a.lo); }
+template <typename T> __device__ __forceinline__ T diff22_u(T b, T c, T a, T d) { return diff22(b, c, a, d); }
+template <typename T> __device__ __forceinline__ T sum22_u(T a, T b, T c, T d) { return sum22(a, b, c, d); }
+template <typename T> __device__ __forceinline__ void diffsum22_u(T a, T b, T c, T d, T &diff, T &sum) {
+  diffsum22(a, b, c, d, diff, sum);
+}
+template <typename T> __device__ __forceinline__ void diffdiff22_u(T a, T b, T c, T d, T &dx, T &dy) {
+  diffdiff22(a, b, c, d, dx, dy);
+}
+template <typename T> __device__ __forceinline__ T add_unnorm(T a, T b) { return a + b; }
+template <typename T> __device__ __forceinline__ T sub_unnorm(T a, T b) { return a - b; }
+template <typename T> __device__ __forceinline__ T add_uu(T a, T b) { return a + b; }
+template <typename T> __device__ __forceinline__ T sub_uu(T a, T b) { return a - b; }
+template <typename T> __device__ __forceinline__ T to_u(T a) { return a; }
+template <typename T> __device__ __forceinline__ T norm_u(T a) { return a; }
+
 // c + sum_j a_j * b_j with one renormalisation at the end (the rows of the
 // stiffness product): each product's high part joins the running sum through
 // an error-free two_sum, its error terms and the low words are summed as

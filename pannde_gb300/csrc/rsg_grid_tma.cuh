@@ -396,9 +396,10 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
   // per cell layer: A = (x, y differences) + z sum, B = the same - z sum; a
   // node's acceleration is A of the layer above + B of the layer below
   R blx = R(), bly = R(), blz = R();  // B of the layer below
-  R spx[3], spy[3], ss[3];
+  using L = typename Lazy<R>::type;  // pair differences before renormalisation
+  L spx[3], spy[3], ss[3];
 #pragma unroll
-  for (int c = 0; c < 3; c++) spx[c] = spy[c] = ss[c] = R();
+  for (int c = 0; c < 3; c++) spx[c] = spy[c] = ss[c] = L();
   const int ra = ty * G::BWC + oc + tx;  // cell (i-1, j-1) in the cell tile
   const int rv = ty * G::BWN + on + tx;  // node (i, j) in the node tile
   int waited = k0 - 2;                   // last layer this thread has waited for
@@ -453,47 +454,49 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
       const int ib = ra + 1, id = ra + G::BWC, ic = id + 1;
       R A, B, C, D;
       A = cellv(0, ra); B = cellv(0, ib); C = cellv(0, ic); D = cellv(0, id);
-      const R px0 = diff22(B, C, A, D);
+      const L px0 = diff22_u(B, C, A, D);
       A = cellv(1, ra); B = cellv(1, ib); C = cellv(1, ic); D = cellv(1, id);
-      const R py1 = diff22(C, D, A, B);
+      const L py1 = diff22_u(C, D, A, B);
       A = cellv(2, ra); B = cellv(2, ib); C = cellv(2, ic); D = cellv(2, id);
-      const R s2 = sum22(A, B, C, D);
+      const L s2 = sum22_u(A, B, C, D);
       A = cellv(3, ra); B = cellv(3, ib); C = cellv(3, ic); D = cellv(3, id);
-      R py3, s3;
-      diffsum22(A, B, C, D, py3, s3);
+      L py3, s3;
+      diffsum22_u(A, B, C, D, py3, s3);
       A = cellv(4, ra); B = cellv(4, ib); C = cellv(4, ic); D = cellv(4, id);
-      R px4, s4;
-      diffsum22(A, D, B, C, px4, s4);
+      L px4, s4;
+      diffsum22_u(A, D, B, C, px4, s4);
       A = cellv(5, ra); B = cellv(5, ib); C = cellv(5, ic); D = cellv(5, id);
-      R px5, py5;
-      diffdiff22(A, B, C, D, px5, py5);
+      L px5, py5;
+      diffdiff22_u(A, B, C, D, px5, py5);
       // x: Sxx along x, Sxy along y, Sxz along z; y: Sxy, Syy, Syz; z: Sxz, Syz, Szz
       R tx, ty, tz, ax, ay, az, nbx, nby, nbz;
+      L axu, ayu, azu;  // A of this layer (renormalised when B of the layer below joins)
       if constexpr (CUBIC) {  // 0.25/h folded into dt/rho and the force weights
-        tx = px0 + py5;
-        ty = px5 + py1;
-        tz = px4 + py3;
-        ax = tx + s4;
-        ay = ty + s3;
-        az = tz + s2;
-        nbx = tx - s4;
-        nby = ty - s3;
-        nbz = tz - s2;
+        tx = add_uu(px0, py5);
+        ty = add_uu(px5, py1);
+        tz = add_uu(px4, py3);
+        axu = add_unnorm(to_u(tx), s4);
+        ayu = add_unnorm(to_u(ty), s3);
+        azu = add_unnorm(to_u(tz), s2);
+        nbx = sub_uu(to_u(tx), s4);
+        nby = sub_uu(to_u(ty), s3);
+        nbz = sub_uu(to_u(tz), s2);
       } else {
-        tx = madd(gy, py5, gx * px0);
-        ty = madd(gy, py1, gx * px5);
-        tz = madd(gy, py3, gx * px4);
-        ax = madd(gz, s4, tx);
-        ay = madd(gz, s3, ty);
-        az = madd(gz, s2, tz);
-        nbx = madd(-gz, s4, tx);
-        nby = madd(-gz, s3, ty);
-        nbz = madd(-gz, s2, tz);
+        tx = madd(gy, norm_u(py5), gx * norm_u(px0));
+        ty = madd(gy, norm_u(py1), gx * norm_u(px5));
+        tz = madd(gy, norm_u(py3), gx * norm_u(px4));
+        const R n4 = norm_u(s4), n3 = norm_u(s3), n2 = norm_u(s2);
+        axu = to_u(madd(gz, n4, tx));
+        ayu = to_u(madd(gz, n3, ty));
+        azu = to_u(madd(gz, n2, tz));
+        nbx = madd(-gz, n4, tx);
+        nby = madd(-gz, n3, ty);
+        nbz = madd(-gz, n2, tz);
       }
       if (k >= k0) {
-        ax = ax + blx;
-        ay = ay + bly;
-        az = az + blz;
+        ax = add_uu(axu, to_u(blx));
+        ay = add_uu(ayu, to_u(bly));
+        az = add_uu(azu, to_u(blz));
         const int2 fr = sRf[k - k0 + 1];
         // this node's force sources (the batch kernel scans its slots whole:
         // the searches cost it registers for a fourth block per SM)
@@ -575,28 +578,29 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
     if (k - 1 >= k0 && k - 1 <= k1 && tx < TX - 1 && ty < TY - 1) {
       const Sm *Vt = sVt + ((k - 1) & 1) * 3 * NT;
       const int ia = t, ib = t + 1, ic = t + TX + 1, id = t + TX;
-      R px[3], py[3], s[3];
+      L px[3], py[3], s[3];
 #pragma unroll
       for (int c = 0; c < 3; c++) {
         const R A = N::tval(Vt[c * NT + ia]), B = N::tval(Vt[c * NT + ib]);
         const R C = N::tval(Vt[c * NT + ic]), D = N::tval(Vt[c * NT + id]);
-        px[c] = diff22(B, C, A, D);
-        diffsum22(A, B, C, D, py[c], s[c]);
+        px[c] = diff22_u(B, C, A, D);
+        diffsum22_u(A, B, C, D, py[c], s[c]);
       }
       const int kc = k - 2;
       if (kc >= k0 && cell_own) {
-        const R d00 = spx[0] + px[0], d10 = spy[0] + py[0], d20 = s[0] - ss[0];
-        const R d01 = spx[1] + px[1], d11 = spy[1] + py[1], d21 = s[1] - ss[1];
-        const R d02 = spx[2] + px[2], d12 = spy[2] + py[2], d22 = s[2] - ss[2];
         R e[6];
         if constexpr (CUBIC) {  // 0.25/h folded into dt*C
-          e[0] = d00;
-          e[1] = d11;
-          e[2] = d22;
-          e[3] = d12 + d21;
-          e[4] = d02 + d20;
-          e[5] = d01 + d10;
+          e[0] = add_uu(spx[0], px[0]);
+          e[1] = add_uu(spy[1], py[1]);
+          e[2] = sub_uu(s[2], ss[2]);
+          // shear: two layer sums, each left unnormalised, and one renormalised add
+          e[3] = add_uu(add_unnorm(spy[2], py[2]), sub_unnorm(s[1], ss[1]));
+          e[4] = add_uu(add_unnorm(spx[2], px[2]), sub_unnorm(s[0], ss[0]));
+          e[5] = add_uu(add_unnorm(spx[1], px[1]), add_unnorm(spy[0], py[0]));
         } else {
+          const R d00 = add_uu(spx[0], px[0]), d10 = add_uu(spy[0], py[0]), d20 = sub_uu(s[0], ss[0]);
+          const R d01 = add_uu(spx[1], px[1]), d11 = add_uu(spy[1], py[1]), d21 = sub_uu(s[1], ss[1]);
+          const R d02 = add_uu(spx[2], px[2]), d12 = add_uu(spy[2], py[2]), d22 = sub_uu(s[2], ss[2]);
           e[0] = gx * d00;
           e[1] = gy * d11;
           e[2] = gz * d22;
