@@ -68,6 +68,9 @@ def parse():
     p.add_argument("--batch-sample-steps", type=int, default=300)
     p.add_argument("--batch-form", default="auto", choices=["auto", "table", "grid"],
                    help="device form of the batch members (auto: grid, the brackets are lattices)")
+    p.add_argument("--batch-kind", default="brackets", choices=["brackets", "plates"],
+                   help="batch members: the seeded L-brackets (config 4), or full-box aluminium plates of "
+                        "150-178 x 140-170 x 24 cells (a traffic comparison)")
     p.add_argument("--no-serving", action="store_true", help="skip the serving leg")
     p.add_argument("--no-pipes", action="store_true", help="skip the arithmetic pipe-rate leg")
     p.add_argument("--no-holes", action="store_true",
@@ -366,7 +369,8 @@ def state_transfer_leg(case, prec, torch, reps=3):
     return out
 
 
-def batch_leg(n_members, sample_steps, torch, steps_total=3000, form="auto", peak=None, peak_kind=None):
+def batch_leg(n_members, sample_steps, torch, steps_total=3000, form="auto", peak=None, peak_kind=None,
+              kind="brackets"):
     """Batched sims/hour: n_members seeded L-brackets (legs 60-220 cells, 12-30
     thick, 40-160 deep, 0.1 mm voxels, a 1-6 mm crack at the inner fillet as
     disconnected faces; every sixth with an acoustic-fluid column and a
@@ -377,14 +381,21 @@ def batch_leg(n_members, sample_steps, torch, steps_total=3000, form="auto", pea
     launch per step for all members plus the two small fix-up launches of the
     split sites (form="table": the connectivity-table kernels, two launches
     per step).  A sample of the steps is timed with CUDA events on the
-    batch's stream; the per-step cost does not change along the run."""
+    batch's stream; the per-step cost does not change along the run.
+    kind="plates": full-box aluminium plates instead, for comparing the
+    kernel's DRAM traffic on members without the brackets' geometry."""
     from pannde_gb300 import cases
     from pannde_gb300.solver import Batch, Solver
     warm = 25  # long enough for the launch-shape tuning (2 rounds x up to 6 shapes x 2 steps + 1) to run untimed
     quantum = 25  # steps per pn_batch_solve call: equal calls replay a captured CUDA graph
     sample_steps = max(quantum, sample_steps // quantum * quantum)
     t0 = time.perf_counter()
-    cs = [cases.bracket_case(1000 + i, nsteps=steps_total, water_column=(i % 6 == 0)) for i in range(n_members)]
+    if kind == "plates":
+        cs = [cases.al_plate_case(nx=150 + 7 * (i % 5), ny=140 + 5 * (i % 7), nz=24, nsteps=steps_total,
+                                  radius=1e-3, n_sensors=8, seed=i) for i in range(n_members)]
+    else:
+        cs = [cases.bracket_case(1000 + i, nsteps=steps_total, water_column=(i % 6 == 0))
+              for i in range(n_members)]
     solvers = [Solver.from_case(c, precision="f32", capacity=warm + 2 * quantum + sample_steps, form=form)
                for c in cs]
     setup_s = time.perf_counter() - t0
@@ -415,7 +426,7 @@ def batch_leg(n_members, sample_steps, torch, steps_total=3000, form="auto", pea
     roof = None
     if peak:
         achieved = alg / per_step_s / 1e9
-        traffic = profile_figures("brackets%d" % n_members, forms[0], "f32", "traffic").get("batch_step")
+        traffic = profile_figures("%s%d" % (kind, n_members), forms[0], "f32", "traffic").get("batch_step")
         roof = {"bound": "hbm", "kernel": "batch step (fused step launch + split-site fix-up)",
                 "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "peak_source": peak_kind, "traffic": traffic, "algorithmic_bytes": alg,
@@ -427,8 +438,10 @@ def batch_leg(n_members, sample_steps, torch, steps_total=3000, form="auto", pea
             "steps_per_call": quantum, "graph_launches": plan["graph_launches"],
             "tuned_shape": {"tile": f"32x{plan['tile_rows']}", "z_chunks_per_column": plan["shape"] or "launcher"},
             "dtype": "f32", "form": ",".join(forms), "setup_s": round(setup_s, 1), "roofline": roof,
-            "workload": f"{n_members} seeded L-brackets with a disconnected-face crack, every sixth with a "
-                        "water column (pressure source), FP32, one pn_batch_solve over all members"}
+            "workload": (f"{n_members} full-box aluminium plates (150-178 x 140-170 x 24 cells), FP32, one "
+                         "pn_batch_solve over all members" if kind == "plates" else
+                         f"{n_members} seeded L-brackets with a disconnected-face crack, every sixth with a "
+                         "water column (pressure source), FP32, one pn_batch_solve over all members")}
 
 
 def serving_leg(n_requests, rate, torch, seed=7, subset=8):
@@ -627,7 +640,7 @@ def main():
             line["configs"] = {"holes": holes_leg(args.steps, args.warmup, torch, peak, peak_kind)}
         if ws == 1 and not args.no_batch:
             line["batch"] = batch_leg(args.batch_members, args.batch_sample_steps, torch, form=args.batch_form,
-                                      peak=peak, peak_kind=peak_kind)
+                                      peak=peak, peak_kind=peak_kind, kind=args.batch_kind)
         if ws == 1 and not args.no_serving:
             line["serving"] = serving_leg(args.serving_requests, args.serving_rate, torch,
                                          subset=args.serving_fp64_subset)

@@ -333,17 +333,25 @@ __device__ __forceinline__ void grid_block_tma(const GridArgs<typename GNum<K>::
   auto mslot = [&](int L) { return base + G::OFF_M + (ucount(L) % G::NM) * G::MBOX; };
   auto bar_of = [&](int L) { return bars + 8u * (ucount(L) % G::NS); };
   auto parity = [&](int L) { return (ucount(L) / G::NS) & 1u; };
-  auto issue = [&](int L) {  // thread 0: copies of layer L
+  // The chunk's first layer k0 - 1 gives only the partial sums of its cell
+  // layer (stress boxes); no node velocity or cell stress of it is computed
+  // here, so its velocity, dt/rho and material boxes are not copied.  The top
+  // layer k1 gives the velocity of node layer k1 but no cell stress: no
+  // material box.  (A chunk above the lattice's first layer re-reads two
+  // layers; these are the bytes of them it does not need.)
+  auto issue = [&](int L) {  // the issuing thread: copies of layer L
     if (L == a.test_skip_layer) return;  // failure-path test: this layer's wait runs out
     const uint32_t bar = bar_of(L);
     unsigned char *sl = sslot(L), *vl = vslot(L);
-    mbar_expect_tx(bar, G::TX_BYTES);
+    const bool first = L == k0 - 1, top = L == k1;
+    mbar_expect_tx(bar, first ? 6u * G::SBOX_BYTES : top ? G::TX_BYTES - G::MBOX_BYTES : G::TX_BYTES);
 #pragma unroll
     for (int f = 0; f < 6; f++) tma_load_3d(smem_u32(sl + f * G::SBOX), &M->S[f], xs_c, j0 - 1, L, bar);
+    if (first) return;
 #pragma unroll
     for (int c = 0; c < 3; c++) tma_load_3d(smem_u32(vl + c * G::VBOX), &M->V[c], xs_n, j0, L, bar);
     tma_load_3d(smem_u32(vl + 3 * G::VBOX), &M->coef, xs_n, j0, L, bar);
-    tma_load_3d(smem_u32(mslot(L)), &M->mat, xs_m, j0, L, bar);
+    if (!top) tma_load_3d(smem_u32(mslot(L)), &M->mat, xs_m, j0, L, bar);
   };
 
   if (t == 0) {
