@@ -493,22 +493,59 @@ int grid_put_state(pn_solver *s, const double *const *V, const double *const *S)
   const int64_t gn = g.node_len(), gc = g.cell_sites();
   const int b = s->cur ^ 1;
   ensure_grid_maps(s);
-  if (!s->d_nonfinite) s->d_nonfinite = s->alloc<int32_t>(2 * sizeof(int32_t));
-  ck(cudaMemsetAsync(s->d_nonfinite, 0, 2 * sizeof(int32_t), s->stream), "memset");
+  if (!s->d_nonfinite) s->d_nonfinite = s->alloc<int32_t>(4 * sizeof(int32_t));
+  ck(cudaMemsetAsync(s->d_nonfinite, 0, 4 * sizeof(int32_t), s->stream), "memset");
+  // the FP64 form: the conversion kernels flag the tiles of out-of-range
+  // values for the next step directly (word 2: a split-site copy was out of
+  // range, which puts every tile on the FP64 path for one step instead)
+  const int64_t tiles = (int64_t)(g.nx / (kGridTileX - 1) + 1) * (g.ny / (kGridTileRows - 1) + 1);
+  StateRangeFlags rv{}, rs{};
+  if (s->d_rflags) {  // staged: a refused state leaves the solver's flags as they were
+    if (!s->d_rflags_stage) s->d_rflags_stage = s->alloc<uint32_t>((size_t)tiles * sizeof(uint32_t));
+    ck(cudaMemsetAsync(s->d_rflags_stage, 0, (size_t)tiles * sizeof(uint32_t), s->stream), "memset");
+    rv.flags = s->d_rflags_stage;
+    rv.unplaced = s->d_nonfinite + 2;
+    rv.gxc = g.nx / (kGridTileX - 1) + 1;
+    rv.ty_own = kGridTileRows - 1;
+    rs = rv;
+    rv.lattice_len = (int64_t)g.pnx * (g.ny + 1) * (g.nz + 1);
+    rv.pitch = g.pnx;
+    rv.rows = g.ny + 1;
+    rv.e_lo = (uint32_t)s->r_elo;
+    rv.e_hi = (uint32_t)s->r_ehi;
+    rs.lattice_len = (int64_t)g.pcx * g.ny * g.nz;
+    rs.pitch = g.pcx;
+    rs.rows = g.ny;
+    rs.e_lo = (uint32_t)s->r_elo_s;
+    rs.e_hi = (uint32_t)s->r_ehi_s;
+    rs.cell = 1;
+  }
   for (int k = 0; k < 3; k++) {
     ck(cudaMemsetAsync(s->V[b][k], 0, (size_t)gn * s->esz, s->stream), "memset");
-    if (V && V[k]) s->put_field(s->V[b][k], V[k], (size_t)s->mesh.n_nodes, s->d_nmap, s->d_nonfinite);
+    if (V && V[k])
+      s->put_field(s->V[b][k], V[k], (size_t)s->mesh.n_nodes, s->d_nmap, s->d_nonfinite, s->d_rflags ? &rv : nullptr);
   }
   for (int k = 0; k < 6; k++) {
     ck(cudaMemsetAsync(s->S[b][k], 0, (size_t)gc * s->esz, s->stream), "memset");
-    if (S && S[k]) s->put_field(s->S[b][k], S[k], (size_t)s->mesh.n_cells, s->d_cmap, s->d_nonfinite + 1);
+    if (S && S[k])
+      s->put_field(s->S[b][k], S[k], (size_t)s->mesh.n_cells, s->d_cmap, s->d_nonfinite + 1,
+                   s->d_rflags ? &rs : nullptr);
   }
-  int32_t bad[2] = {0, 0};
+  int32_t bad[3] = {0, 0, 0};
   ck(cudaMemcpyAsync(bad, s->d_nonfinite, sizeof(bad), cudaMemcpyDeviceToHost, s->stream), "finite check");
   ck(cudaStreamSynchronize(s->stream), "set_state");
   if (bad[0] || bad[1]) return (bad[0] ? 1 : 0) | (bad[1] ? 2 : 0);
   s->cur = b;
-  grid_reset_range_flags(s);  // the new state's ranges are not known: FP64 for one step
+  if (s->d_rflags) {
+    if (bad[2]) {
+      grid_reset_range_flags(s);  // a split-site copy out of range: FP64 for one step
+    } else {
+      ck(cudaMemsetAsync(s->d_rflags, 0, (size_t)(3 * tiles) * sizeof(uint32_t), s->stream), "memset");
+      ck(cudaMemcpyAsync(s->d_rflags + (s->step % 3) * tiles, s->d_rflags_stage, (size_t)tiles * sizeof(uint32_t),
+                         cudaMemcpyDeviceToDevice, s->stream),
+         "range flags");
+    }
+  }
   return 0;
 }
 

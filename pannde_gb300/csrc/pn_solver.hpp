@@ -102,7 +102,9 @@ struct pn_solver {
   // and the force weights (the kernel's g is then 1); 1.0 when not folded
   double gfold = 1.0;
   int32_t *d_err = nullptr;  // device error word of the grid kernels
-  int32_t *d_nonfinite = nullptr;  // [2] set_state's NaN / infinity flags (velocity, stress)
+  uint32_t *d_rflags_stage = nullptr;  // FP64 form: set_state's tile flags before the state is accepted
+  int32_t *d_nonfinite = nullptr;  // [4] set_state's NaN / infinity flags (velocity, stress), and
+                                   // (FP64 form) an out-of-range value at a split site's copy
   // split sites (grid.copy_node / fix_cell): the step's fix-up tables, rebuilt
   // when sources or sensors change; host lists of the copies' forces and
   // sensors and the fix cells' moments (per copy / fix cell, in order)
@@ -253,16 +255,18 @@ struct pn_solver {
   }
   // host FP64 field[n] -> dst[map[i]] in the storage type (map null: dst[i]);
   // *nonfinite (device, when given) becomes 1 if a value is NaN or infinite
-  void put_field(void *dst, const double *host, size_t n, const int64_t *map, int32_t *nonfinite = nullptr) {
+  // (rf: the FP64 form's tile flags of out-of-range values, see rsg_state.cuh)
+  void put_field(void *dst, const double *host, size_t n, const int64_t *map, int32_t *nonfinite = nullptr,
+                 const pn::StateRangeFlags *rf = nullptr) {
     if (n == 0) return;
     if (const void *dv = device_view(host)) {
-      pn::ck(pn::launch_state_store(precision, (const double *)dv, (int64_t)n, map, dst, stream, nonfinite),
+      pn::ck(pn::launch_state_store(precision, (const double *)dv, (int64_t)n, map, dst, stream, nonfinite, rf),
              "put_field kernel");
       return;
     }
     double *st = stage();
     pn::ck(cudaMemcpyAsync(st, host, n * 8, cudaMemcpyHostToDevice, stream), "put_field copy");
-    pn::ck(pn::launch_state_store(precision, st, (int64_t)n, map, dst, stream, nonfinite), "put_field kernel");
+    pn::ck(pn::launch_state_store(precision, st, (int64_t)n, map, dst, stream, nonfinite, rf), "put_field kernel");
   }
   // src[map[i]] (or src[i]) in the storage type -> host FP64 field[n]
   void get_field(double *host, const void *src, size_t n, const int64_t *map) {

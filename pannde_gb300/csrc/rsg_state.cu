@@ -15,6 +15,7 @@
 #include <cstdint>
 
 #include "../../include/pannde_gb300.h"
+#include "df64.cuh"
 #include "rsg_state.cuh"
 
 namespace {
@@ -34,11 +35,25 @@ template <> __device__ __forceinline__ double cvt_out<float2>(float2 v) {
   return __dadd_rn((double)v.x, (double)v.y);
 }
 
+// the tile flag bits of an out-of-range value at lattice index j
+__device__ __forceinline__ void flag_value(const pn::StateRangeFlags &rf, int64_t j) {
+  if (j >= rf.lattice_len) {
+    *rf.unplaced = 1;
+    return;
+  }
+  const int x = (int)(j % rf.pitch), y = (int)((j / rf.pitch) % rf.rows);
+  const int bx = x / 31, tx = x - 31 * bx, by = y / rf.ty_own, ty = y - rf.ty_own * by;
+  uint32_t bits = 1u | (tx == 0 ? 2u : 0u) | (ty == 0 ? 8u : 0u);
+  if (rf.cell) bits |= (tx == 30 ? 4u : 0u) | (ty == rf.ty_own - 1 ? 16u : 0u);
+  atomicOr(rf.flags + (int64_t)by * rf.gxc + bx, bits);
+}
+
 // dst[map ? map[i] : i] = cvt(src[i]), i < n
 template <typename R>
 __global__ void __launch_bounds__(256) k_state_store(const double *__restrict__ src, int64_t n,
                                                      const int64_t *__restrict__ map,
-                                                     R *__restrict__ dst, int32_t *nonfinite) {
+                                                     R *__restrict__ dst, int32_t *nonfinite,
+                                                     const pn::StateRangeFlags rf) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   bool bad = false;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
@@ -47,6 +62,7 @@ __global__ void __launch_bounds__(256) k_state_store(const double *__restrict__ 
     // NaN or infinity: every exponent bit set
     bad = bad || (__double_as_longlong(v) & 0x7ff0000000000000LL) == 0x7ff0000000000000LL;
     dst[j] = cvt_in<R>(v);
+    if (rf.flags && !pn::in_df64_range(v, rf.e_lo, rf.e_hi)) flag_value(rf, j);
   }
   if (bad && nonfinite) *nonfinite = 1;
 }
@@ -91,13 +107,15 @@ int blocks_for(int64_t n) {
 namespace pn {
 
 cudaError_t launch_state_store(int precision, const double *src, int64_t n, const int64_t *map,
-                               void *dst, cudaStream_t st, int32_t *nonfinite) {
+                               void *dst, cudaStream_t st, int32_t *nonfinite, const StateRangeFlags *rf) {
   if (n <= 0) return cudaSuccess;
   const int nb = blocks_for(n);
+  StateRangeFlags f{};
+  if (rf) f = *rf;
   switch (precision) {
-    case PN_PREC_F32: k_state_store<float><<<nb, 256, 0, st>>>(src, n, map, (float *)dst, nonfinite); break;
-    case PN_PREC_DF64: k_state_store<float2><<<nb, 256, 0, st>>>(src, n, map, (float2 *)dst, nonfinite); break;
-    default: k_state_store<double><<<nb, 256, 0, st>>>(src, n, map, (double *)dst, nonfinite); break;
+    case PN_PREC_F32: k_state_store<float><<<nb, 256, 0, st>>>(src, n, map, (float *)dst, nonfinite, StateRangeFlags{}); break;
+    case PN_PREC_DF64: k_state_store<float2><<<nb, 256, 0, st>>>(src, n, map, (float2 *)dst, nonfinite, StateRangeFlags{}); break;
+    default: k_state_store<double><<<nb, 256, 0, st>>>(src, n, map, (double *)dst, nonfinite, f); break;
   }
   return cudaGetLastError();
 }

@@ -53,9 +53,9 @@ def plate():
 
 
 def test_developed_state_takes_double_float(cuda_device):
-    """A random state of ordinary magnitudes: after the first step (FP64 for
-    every tile: nothing is known of a new state) the blocks take the
-    double-float path."""
+    """A random state of ordinary magnitudes: set_state flags no tile (every
+    value is inside the double-float range), so the blocks take the
+    double-float path from the first step."""
     c = plate()
     rng = np.random.default_rng(3)
     V0 = [rng.uniform(-1e-3, 1e-3, c.mesh.n_nodes) for _ in range(3)]
@@ -105,3 +105,23 @@ def test_tone_burst_front_matches_fp64_path(cuda_device, monkeypatch):
     for i in range(tr.shape[1]):
         assert rel(tr[:, i], tr2[:, i]) <= 1e-10
     assert counts[1] > 0, counts
+
+
+def test_set_state_flags_only_the_tiles_it_must(cuda_device):
+    """set_state flags the tiles of its out-of-range values for the first
+    step (and the neighbours that read their edges): the rest start on the
+    double-float path at once.  96 x 40 x 6 cells = 4 x 6 tile columns, one
+    block each; values near 1e-200 in the last four node columns (the tiles
+    of bx = 3, whose first column the tiles of bx = 2 read)."""
+    c = plate()
+    V0 = [np.zeros(c.mesh.n_nodes) for _ in range(3)]
+    S0 = [np.zeros(c.mesh.n_cells) for _ in range(6)]
+    rng = np.random.default_rng(9)
+    far = np.flatnonzero(c.mesh.x > c.mesh.x.max() - 3.5 * 0.1e-3)
+    V0[2][far] = rng.uniform(-1, 1, far.size) * 1e-200
+    with Solver(c.mesh, c, c.dt, "f64", "grid") as s:
+        s.set_state(V0, S0)
+        s.solve(1)
+        fp64, df = s.path_counts()
+    assert fp64 + df == 24, (fp64, df)
+    assert fp64 == 12 and df == 12, (fp64, df)
