@@ -48,6 +48,16 @@ struct pn_batch {
   cudaGraphExec_t exec = nullptr;
   ChunkSignature exec_sig{};
   int64_t graph_launches = 0, graph_captures = 0;
+  // grid-form launch orders already built, by the members, their tile rows
+  // and chunk lengths (built on the host: reused across calls; cleared when
+  // members are added or removed)
+  struct Order {
+    std::vector<const void *> members;
+    std::vector<int> kchunk;
+    int rows = 0;
+    std::vector<int> ids;
+  };
+  std::vector<Order> orders;
 
   ~pn_batch() {
     if (exec) cudaGraphExecDestroy(exec);
@@ -367,8 +377,34 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision, const Stage &stage, 
     // staged; members are re-tiled first when the shape's rows differ
     Staging g{};
     int staged_shape = -1;
+    // pn_batch_solve's launch order (the tensor-copy kernel): the blocks with
+    // layers to march, longest first (stable: equal columns stay in member and
+    // tile order, neighbours together); the staged prefix table holds it
+    // after the members' block prefixes, sized for the shape with the most
+    // blocks so that the staging is not reallocated between shapes.  The
+    // allocation-free call keeps the plain numbering (no room in its scratch).
+    const bool ordered = tma && may_alloc;
+    std::vector<int> order;
+    int listed = 0;  // blocks launched
+    size_t start_ints = 2 * (n + 1);
+    if (ordered) {
+      size_t most = 0;
+      for (auto &sh : shapes) {
+        size_t blocks = 0;
+        for (pn_solver *s : b->members) {
+          const int kc = sh.second == 0 ? pn::grid_chunk_layers(precision, s->grid.nx, s->grid.ny, s->grid.nz, tma,
+                                                                sh.first)
+                                        : std::min(pn::kGridChunkMax, std::max(1, (s->grid.nz + sh.second - 1) /
+                                                                                       sh.second));
+          blocks += (size_t)(s->grid.nx / (tx - 1) + 1) * (s->grid.ny / (sh.first - 1) + 1) *
+                    ((s->grid.nz + kc - 1) / kc);
+        }
+        most = std::max(most, blocks);
+      }
+      start_ints = std::max(start_ints, (size_t)(n + 1) + most);
+    }
     auto prepare = [&](int c) {
-      if (c == staged_shape) return bs[n];
+      if (c == staged_shape) return listed;
       const int rows = shapes[c].first;
       bool retile = false;
       for (pn_solver *s : b->members) retile = retile || s->tile_rows != rows;
@@ -414,16 +450,64 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision, const Stage &stage, 
         split[m + 1] = split[m] + a.n_copies;
         split[n + 1 + m + 1] = split[n + 1 + m] + a.n_fix;
       }
-      g = stage(sizeof(pn::GridArgs<T>) * n, 2 * (n + 1));
+      listed = bs[n];
+      const pn_batch::Order *cached = nullptr;
+      if (ordered) {
+        pn_batch::Order key;
+        key.rows = rows;
+        for (int m = 0; m < n; m++) {
+          key.members.push_back(b->members[m]);
+          key.kchunk.push_back(ga[0][m].kchunk);
+        }
+        for (const pn_batch::Order &o : b->orders)
+          if (o.rows == key.rows && o.members == key.members && o.kchunk == key.kchunk) cached = &o;
+        if (!cached) {
+          if (b->orders.size() >= 8) b->orders.erase(b->orders.begin());
+          b->orders.push_back(std::move(key));
+        }
+      }
+      if (ordered && cached) {
+        order = cached->ids;
+        listed = (int)order.size();
+      } else if (ordered) {
+        // layers each block marches: its chunk of its tile column, up to the
+        // column's top solid layer
+        std::vector<std::pair<int, int>> work;  // (layers, block)
+        work.reserve((size_t)bs[n]);
+        for (int m = 0; m < n; m++) {
+          pn_solver *s = b->members[m];
+          const pn::GridArgs<T> &a = ga[0][m];
+          const std::vector<int32_t> top = pn::grid_tile_tops(s->grid, rows);
+          const int tiles = (int)top.size();
+          for (int id = bs[m]; id < bs[m + 1]; id++) {
+            const int local = id - bs[m], tile = local % tiles, k0 = local / tiles * a.kchunk;
+            const int layers = std::min(std::min(top[(size_t)tile], a.nz), k0 + a.kchunk) - k0;
+            // (a column's first chunk always runs: the FP64 form's blocks clear
+            // their tile's flag word there)
+            if (layers > 0 || k0 == 0) work.emplace_back(std::max(layers, 0), id);
+          }
+        }
+        std::stable_sort(work.begin(), work.end(),
+                         [](const std::pair<int, int> &x, const std::pair<int, int> &y) { return x.first > y.first; });
+        order.resize(work.size());
+        for (size_t q = 0; q < work.size(); q++) order[q] = work[q].second;
+        listed = (int)order.size();
+        b->orders.back().ids = order;
+      }
+      g = stage(sizeof(pn::GridArgs<T>) * n, start_ints);
       for (int p = 0; p < 2; p++)
         pn::ck(cudaMemcpyAsync(g.args[p], ga[p].data(), sizeof(pn::GridArgs<T>) * n, cudaMemcpyHostToDevice,
                                b->stream), "batch args");
       pn::ck(cudaMemcpyAsync(g.start[0], bs.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, b->stream),
              "batch blocks");
+      if (ordered && listed > 0)
+        pn::ck(cudaMemcpyAsync(g.start[0] + n + 1, order.data(), sizeof(int) * (size_t)listed,
+                               cudaMemcpyHostToDevice, b->stream),
+               "batch block order");
       pn::ck(cudaMemcpyAsync(g.start[1], split.data(), sizeof(int) * split.size(), cudaMemcpyHostToDevice,
                              b->stream), "batch split sites");
       staged_shape = c;
-      return bs[n];
+      return listed;
     };
     sym = 2;  // the most general symmetry class among the members
     for (pn_solver *s : b->members) sym = std::min(sym, s->sym);
@@ -462,7 +546,8 @@ void solve_grid(pn_batch *b, int32_t nsteps, int precision, const Stage &stage, 
                 L.n_members = n;
                 L.args = g.args[k & 1];
                 L.block_start = g.start[0];
-                L.total_blocks = bs[n];
+                L.total_blocks = listed;
+                L.order = ordered ? g.start[0] + n + 1 : nullptr;
                 L.sym = sym;
                 L.tile_rows = shapes[c].first;
                 L.range_flags = range_flags ? 1 : 0;
@@ -544,6 +629,7 @@ int pn_batch_add(pn_batch *b, pn_solver *m) {
   if (m->precision == PN_PREC_F64_EXACT) return berr(PN_ERR_INVALID, "the exact FP64 form is not batched");
   if (m->has_mask_sources()) return berr(PN_ERR_INVALID, "window-mask sources need pn_solver_solve_signals");
   b->members.push_back(m);
+  b->orders.clear();
   return PN_OK;
 }
 
@@ -552,6 +638,7 @@ int pn_batch_remove(pn_batch *b, pn_solver *m) {
   auto it = std::find(b->members.begin(), b->members.end(), m);
   if (it == b->members.end()) return berr(PN_ERR_INVALID, "solver not in the batch");
   b->members.erase(it);
+  b->orders.clear();
   return PN_OK;
 }
 

@@ -149,6 +149,11 @@ struct GridBatchLaunch {
   int sym;                 // most general symmetry class among the members
   int tile_rows;           // TY of every member's tiles
   int range_flags;         // FP64 form: every member has path flags (rflags)
+  // launch order of the blocks (tensor-copy kernel): block i of the launch is
+  // block order[i] of the member-major numbering, total_blocks entries; null:
+  // the numbering itself.  pn_batch_solve lists the blocks that have layers to
+  // march, longest first, so that no long column starts in the last wave
+  const int *order = nullptr;
 };
 cudaError_t launch_grid_batch(const GridBatchLaunch &b, int precision, int step, cudaStream_t st);
 cudaError_t launch_grid_f32(const GridArgs<float> &a, int sym, cudaStream_t st);

@@ -838,8 +838,8 @@ __global__ void __launch_bounds__(TX * 8, PN_F64H_MIN_BLOCKS)
 template <int SYM, int MODE>
 __global__ void __launch_bounds__(TX * 8, PN_F64H_MIN_BLOCKS)
     k_grid_tma_f64h_batch(const GridArgs<double> *__restrict__ args, const int *__restrict__ block_start,
-                          int n_members, int step) {
-  const int id = blockIdx.x;
+                          const int *__restrict__ order, int n_members, int step) {
+  const int id = order ? __ldg(order + blockIdx.x) : (int)blockIdx.x;
   int lo = 0, hi = n_members;
   while (hi - lo > 1) {
     const int mid = (lo + hi) >> 1;
@@ -873,8 +873,8 @@ __global__ void __launch_bounds__(TX *TY, GMinBlocks<R, TY>::v)
 template <typename R, int SYM, int TY>
 __global__ void __launch_bounds__(TX *TY, GMinBlocks<R, TY>::v)
     k_grid_tma_batch(const GridArgs<typename GNum<R>::S> *__restrict__ args, const int *__restrict__ block_start,
-                     int n_members, int step) {
-  const int id = blockIdx.x;
+                     const int *__restrict__ order, int n_members, int step) {
+  const int id = order ? __ldg(order + blockIdx.x) : (int)blockIdx.x;
   int lo = 0, hi = n_members;
   while (hi - lo > 1) {
     const int mid = (lo + hi) >> 1;
@@ -954,7 +954,7 @@ cudaError_t launch_batch_t(const GridBatchLaunch &b, int step, cudaStream_t st) 
   if (e != cudaSuccess) return e;
   if (b.total_blocks <= 0) return cudaSuccess;
   k_grid_tma_batch<R, SYM, TY><<<b.total_blocks, TX * TY, S::smem, st>>>(
-      (const GridArgs<typename GNum<R>::S> *)b.args, b.block_start, b.n_members, step);
+      (const GridArgs<typename GNum<R>::S> *)b.args, b.block_start, b.order, b.n_members, step);
   return cudaGetLastError();
 }
 
@@ -1009,7 +1009,7 @@ cudaError_t launch_batch_h_mode(const GridBatchLaunch &b, int step, cudaStream_t
   cudaError_t e = SetupH<SYM, MODE>::ensure();
   if (e != cudaSuccess) return e;
   k_grid_tma_f64h_batch<SYM, MODE><<<b.total_blocks, TX * 8, SetupH<SYM, MODE>::smem, st>>>(
-      (const GridArgs<double> *)b.args, b.block_start, b.n_members, step);
+      (const GridArgs<double> *)b.args, b.block_start, b.order, b.n_members, step);
   return cudaGetLastError();
 }
 
