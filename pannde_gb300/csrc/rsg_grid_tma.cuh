@@ -22,8 +22,15 @@
 //   C(k-2)  stress of cell layer k-2 from node layers k-2 (partial sums in
 //           registers) and k-1 (computed tile (k-1)&1, complete since the
 //           previous barrier) (HostRSGTDUT.hpp:278-293)
-// and thread 0 first issues the copies of layer k+1 into slot (k+1)&3, whose
-// previous layer k-3 was last read before the previous barrier.
+// and the first thread of the last warp (the tile's apron row, which has no
+// stress half) first issues the copies of layer k+1 into its slot, whose
+// previous layer was last read before the previous barrier.
+//
+// A single solver's launch is the 3D grid (x tiles, y tiles, z chunks), or,
+// when whole columns leave a last partial wave of resident blocks, a 1D grid
+// whose last wave's columns are cut into shorter chunks (block_coords).  The
+// sparse sources and sensors of a (tile, layer) slot are sorted by node: a
+// thread finds its own by a binary search in a long slot.
 //
 // Every wait is bounded (about one second of %globaltimer); a wait that gives
 // up records an error word for the host, the block drains its own copies in
